@@ -1,0 +1,333 @@
+#!/usr/bin/env python3
+"""Benchmark: BRMerge SpGEMM GFLOP/s and HBM-roofline fraction on one GB300.
+
+Workload (default): C = A*A, A = R-MAT(a,b,c,d = .57,.19,.19,.05) with n = 2^18
+and 2.35*n samples (duplicates removed: ~607k nnz, ~9.0e7 intermediate
+products), float64, BRMerge-Precise, plain per-call GPU path.  A "step" is
+one SpGEMM call.  GFLOP/s = 2 * intermediate products / time, the
+reference's definition (BRMerge-SpGEMM/src/brmerge_precise.cpp:65-69).
+
+* value   -- device-resident inputs: brm_symbolic + brm_numeric (C ABI)
+             timed with CUDA events on the call's stream, L2 flushed between
+             steps (the inputs fit in L2).
+* e2e     -- the reference-facing host call brm_precise: pinned host inputs
+             copied in, C copied back to host memory, wall clock per call.
+* roofline -- numeric phase (the dominant phase): algorithmic bytes
+             bytes(A) + bytes(B) + bytes(C) over its CUDA-event duration,
+             against the measured HBM copy bandwidth in MEASURED_PEAKS.json.
+* cpu_baseline -- the oracle restatement of BRMerge-Precise (OpenMP, all
+             host cores) on the same input.
+
+--impl reference times the reference algorithm on the host cores instead
+(oracle/_ref when it was built here, else the oracle restatement).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+RMAT_SCALE = 18
+RMAT_EDGE_FACTOR = 2.35
+
+
+def csr_bytes(M: int, nnz: int, vbytes: int) -> int:
+    return 4 * (M + 1) + nnz * (4 + vbytes)
+
+
+def make_workload(name: str):
+    import brmerge_gb300 as brm
+    if name == "rmat":
+        n = 1 << RMAT_SCALE
+        A = brm.gen_rmat(RMAT_SCALE, int(RMAT_EDGE_FACTOR * n), seed=0)
+        desc = {"workload": "rmat_n2^18_ef2.35_AxA", "n": n, "a": 0.57, "b": 0.19, "c": 0.19,
+                "seed": 0}
+    elif name == "er":
+        A = brm.gen_er(16384, 8, seed=0)
+        desc = {"workload": "er_n16384_8perrow_AxA", "n": 16384, "seed": 0}
+    elif name == "stencil":
+        A = brm.gen_stencil27(128)
+        desc = {"workload": "stencil27_128^3_AxA", "n": 128 ** 3}
+    else:
+        raise SystemExit(f"unknown workload {name}")
+    return A, desc
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """Samples nvidia-smi clocks and throttle reasons during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.idx = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.idx), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax = max(smax, float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[4:8]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def max_over_ranks(x: float, ws: int) -> float:
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def cpu_baseline(A, budget_s: float = 20.0):
+    """The oracle restatement on all host cores: 1 warm-up + timed calls,
+    bounded by budget_s (BRMerge-SpGEMM/src/brmerge_precise.cpp:68-82)."""
+    import oracle
+    oracle.build(with_ref=False)
+    nt = oracle.max_threads()
+    flop = oracle.compute_flop(A, A)
+    t0 = time.perf_counter()
+    oracle.precise(A, A, nt)
+    one = time.perf_counter() - t0
+    reps = max(1, min(10, int(budget_s / max(one, 1e-3))))
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        oracle.precise(A, A, nt)
+    dt = (time.perf_counter() - t0) / reps
+    return {"value": round(2 * flop / dt / 1e9, 4), "unit": "GFLOP/s", "cores": nt,
+            "kind": "port",
+            "sample": f"full workload, 1 warm-up + mean of {reps} calls, {dt * 1e3:.1f} ms/call"}
+
+
+def run_reference(args):
+    """--impl reference: the reference algorithm on the host cores."""
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    import oracle
+    oracle.build(with_ref=False)
+    A, desc = make_workload(args.workload)
+    use_ref = oracle.ref_available()
+    nt = oracle.max_threads()
+    flop = oracle.compute_flop(A, A)
+
+    def call():
+        if use_ref:
+            oracle.ref_precise(A, A, nt)
+        else:
+            oracle.precise(A, A, nt)
+
+    for _ in range(args.warmup):
+        call()
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        call()
+        times.append(time.perf_counter() - t0)
+    tot = sum(times)
+    value = 2 * flop * args.steps / tot / 1e9
+    kind = "reference" if use_ref else "port"
+    line = {
+        "metric": "SpGEMM GFLOP/s (BRMerge-Precise, C=A*A)", "value": round(value, 4),
+        "unit": "GFLOP/s", "impl": "reference", "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(tot / args.steps * 1e3, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic", "config": desc,
+        "cpu_baseline": {"value": round(value, 4), "unit": "GFLOP/s", "cores": nt, "kind": kind,
+                         "sample": "full workload per step"},
+        "e2e": {"value": round(value, 4), "unit": "GFLOP/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import torch
+    import brmerge_gb300 as brm
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", local if ws > 1 else 0)
+    torch.cuda.set_device(dev)
+    A, desc = make_workload(args.workload)
+    products = brm.compute_flop_host(A, A)
+    stream = torch.cuda.current_stream(dev)
+    ctx = brm.Context(stream=stream)
+    dA = brm.DeviceCSR.from_host(A, dev)
+    # the configured workload is C = A*A: B is the same device matrix
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    def step(timed_events=None):
+        if timed_events:
+            timed_events[0].record(stream)
+        crpt, cnnz = ctx.symbolic(dA, dA)
+        if timed_events:
+            timed_events[1].record(stream)
+        C = ctx.numeric(dA, dA, crpt, cnnz)
+        if timed_events:
+            timed_events[2].record(stream)
+        return C, cnnz
+
+    for _ in range(args.warmup):
+        C, cnnz = step()
+    torch.cuda.synchronize(dev)
+    ev = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(args.steps)]
+    barrier(ws)
+    torch.cuda.synchronize(dev)
+    with ClockSampler(dev.index if dev.index is not None else 0) as clk:
+        for i in range(args.steps):
+            flush.fill_(float(i))  # write 512 MB (> 129 MB L2) between steps
+            C, cnnz = step(ev[i])
+        torch.cuda.synchronize(dev)
+    barrier(ws)
+    step_ms = [e[0].elapsed_time(e[2]) for e in ev]
+    num_ms = [e[1].elapsed_time(e[2]) for e in ev]
+    total_s = max_over_ranks(sum(step_ms) / 1e3, ws)
+    value = 2 * products * args.steps * ws / total_s / 1e9
+
+    vb = 8
+    alg_bytes = csr_bytes(A.M, A.nnz, vb) * 2 + csr_bytes(A.M, cnnz, vb)
+    num_s = statistics.mean(num_ms) / 1e3
+    peak, peak_kind = peaks()
+    achieved = alg_bytes / num_s / 1e9
+    call_achieved = alg_bytes / (sum(step_ms) / args.steps / 1e3) / 1e9
+
+    # e2e through the host drop-in (brm_precise): pinned inputs, host outputs
+    pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()
+    hA = brm.CSR(A.M, A.N, pin(A.rpt), pin(A.col), pin(A.val))
+    for _ in range(max(1, args.warmup)):
+        brm.brmerge_precise(hA, hA)
+    e2e_t = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        Ch = brm.brmerge_precise(hA, hA)
+        e2e_t.append(time.perf_counter() - t0)
+    e2e_s = max_over_ranks(sum(e2e_t), ws)
+    e2e_val = 2 * products * args.steps * ws / e2e_s / 1e9
+    h2d = csr_bytes(A.M, A.nnz, vb)  # A and B are the same host arrays: copied once
+    d2h = csr_bytes(A.M, len(Ch.col), vb)
+
+    if rank != 0:
+        return
+    cpu = cpu_baseline(A, budget_s=args.cpu_budget) if not args.no_cpu else None
+    launches_per_step = 9 + (1 if ctx.last_device_error < 0 else 0)
+    line = {
+        "metric": "SpGEMM GFLOP/s (BRMerge-Precise, C=A*A)",
+        "value": round(value, 3), "unit": "GFLOP/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(statistics.mean(step_ms), 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic",
+        "config": dict(desc, products=int(products), nnz_A=int(A.nnz), nnz_C=int(cnnz),
+                       method="precise", l2="flushed (512 MB write) between steps",
+                       parallelism="replicas" if ws > 1 else "single_gpu",
+                       call_hbm_frac=round(call_achieved / peak, 4)),
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak,
+                     "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": None,
+                     "kernel": "numeric phase", "peak_kind": peak_kind,
+                     "algorithmic_bytes": int(alg_bytes)},
+        "e2e": {"value": round(e2e_val, 3), "unit": "GFLOP/s", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h)},
+        "clocks": clk.summary(),
+        "gpu_launches": launches_per_step * args.steps,
+    }
+    if cpu is not None:
+        line["cpu_baseline"] = cpu
+    print(json.dumps(line), flush=True)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=["rmat", "er", "stencil"], default="rmat")
+    ap.add_argument("--cpu-budget", type=float, default=15.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,106 @@
+"""Build recipe for the native parts of brmerge_gb300 (no cmake).
+
+* libbrmerge.so   -- the CUDA library behind include/brmerge.h, compiled for
+                     sm_103a only (-gencode arch=compute_103a,code=sm_103a);
+* libbrm_host.so  -- host-only helpers (synthetic generators, include/brm_gen.h).
+
+Translation units are compiled in parallel into _build/ and linked in-tree
+next to this file.  Output is only rebuilt when a source is newer.
+"""
+from __future__ import annotations
+
+import concurrent.futures as cf
+import os
+import shutil
+import subprocess
+import sys
+from pathlib import Path
+
+PKG = Path(__file__).resolve().parent
+ROOT = PKG.parent
+CSRC = PKG / "csrc"
+INCLUDE = ROOT / "include"
+BUILD = PKG / "_build"
+
+CUDA_SOURCES = [
+    "brm_api.cu",
+    "brm_analyze.cu",
+    "brm_symbolic.cu",
+    "brm_numeric_f64.cu",
+    "brm_numeric_f32.cu",
+]
+HOST_SOURCES = ["host/gen.cpp"]
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+
+def _nvcc() -> str:
+    cand = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not Path(cand).exists():
+        raise RuntimeError("nvcc not found; the CUDA 13 toolkit is required to build libbrmerge.so")
+    return cand
+
+
+def _newer(target: Path, deps: list[Path]) -> bool:
+    if not target.exists():
+        return True
+    t = target.stat().st_mtime
+    return any(d.stat().st_mtime > t for d in deps)
+
+
+def _run(cmd: list[str]) -> None:
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("build step failed:\n" + " ".join(cmd) + "\n" + r.stdout + r.stderr)
+
+
+def build_cuda(verbose: bool = False, debug: bool = False) -> Path:
+    nvcc = _nvcc()
+    BUILD.mkdir(exist_ok=True)
+    out = PKG / "libbrmerge.so"
+    headers = list(CSRC.glob("*.cuh")) + list(CSRC.glob("*.h")) + [INCLUDE / "brmerge.h"]
+    flags = ARCH + [
+        "-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall",
+        "-I", str(INCLUDE), "-I", str(CSRC),
+    ]
+    if verbose:
+        flags += ["-Xptxas", "-v"]
+    objs = []
+    jobs = []
+    for src in CUDA_SOURCES:
+        s = CSRC / src
+        o = BUILD / (Path(src).stem + ".o")
+        objs.append(o)
+        if _newer(o, [s] + headers):
+            jobs.append([nvcc] + flags + ["-c", str(s), "-o", str(o)])
+    with cf.ThreadPoolExecutor(max_workers=max(1, min(len(jobs), os.cpu_count() or 4))) as ex:
+        list(ex.map(_run, jobs))
+    if jobs or _newer(out, objs):
+        tmp = out.with_suffix(".so.tmp")
+        _run([nvcc] + ARCH + ["-shared", "-cudart", "static", "-o", str(tmp)] + [str(o) for o in objs])
+        os.replace(tmp, out)
+    return out
+
+
+def build_host() -> Path:
+    cxx = shutil.which("g++") or "g++"
+    out = PKG / "libbrm_host.so"
+    srcs = [CSRC / s for s in HOST_SOURCES]
+    if _newer(out, srcs + [INCLUDE / "brm_gen.h"]):
+        tmp = out.with_suffix(".so.tmp")
+        _run([cxx, "-O2", "-std=c++17", "-fPIC", "-shared", "-Wall", "-I", str(INCLUDE)]
+             + [str(s) for s in srcs] + ["-o", str(tmp)])
+        os.replace(tmp, out)
+    return out
+
+
+def build(verbose: bool = False) -> None:
+    with cf.ThreadPoolExecutor(max_workers=2) as ex:
+        f1 = ex.submit(build_cuda, verbose)
+        f2 = ex.submit(build_host)
+        f1.result()
+        f2.result()
+
+
+if __name__ == "__main__":
+    build(verbose="-v" in sys.argv)
+    print("built", PKG / "libbrmerge.so", PKG / "libbrm_host.so")

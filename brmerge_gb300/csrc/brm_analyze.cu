@@ -1,0 +1,335 @@
+// brm_analyze.cu -- row analysis, device scans, Upper compaction, validation.
+#include <climits>
+
+#include "brm_common.cuh"
+#include "brm_kernels.h"
+
+namespace brm {
+
+// ---------------------------------------------------------------------------
+// Row analysis.  Replaces compute_flop (spgemm.h:31-56) and the flop-balanced
+// static row ranges (spgemm.h:496-503): on the GPU the balance comes from
+// binning rows by their product count and handing heavy rows out first.
+// One warp per row; each block appends its rows to the bin lists with one
+// global atomic per bin.
+// ---------------------------------------------------------------------------
+constexpr int kAnaThreads = 256;
+constexpr int kAnaRowsPerWarp = 8;
+
+__global__ void __launch_bounds__(kAnaThreads) k_analyze(CsrDev A, CsrDev B, PlanDev P)
+{
+    constexpr int NW = kAnaThreads / 32;
+    constexpr int RPB = NW * kAnaRowsPerWarp;
+    __shared__ int s_cnt[kNumBins];
+    __shared__ int s_base[kNumBins];
+    __shared__ int s_bin[RPB];
+    __shared__ int s_idx[RPB];
+    __shared__ unsigned long long s_flop[NW];
+    __shared__ int s_maxk[NW];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (threadIdx.x < kNumBins)
+        s_cnt[threadIdx.x] = 0;
+    __syncthreads();
+    const int M = A.M, K = B.M;
+    const int row0 = blockIdx.x * RPB;
+    unsigned long long wflop = 0;
+    int wmaxk = 0;
+    for (int r = 0; r < kAnaRowsPerWarp; r++) {
+        const int slot = w * kAnaRowsPerWarp + r;
+        const int row = row0 + slot;
+        if (row >= M) {
+            if (lane == 0)
+                s_bin[slot] = -1;
+            continue;
+        }
+        const int a0 = A.rpt[row], a1 = A.rpt[row + 1];
+        long long f = 0;
+        int nl = 0, leaf = -1;
+        bool bad = false;
+        for (int j = a0 + lane; j < a1; j += 32) {
+            int b = A.col[j];
+            int len = 0;
+            if ((unsigned)b < (unsigned)K)
+                len = B.rpt[b + 1] - B.rpt[b];
+            else
+                bad = true;
+            f += len;
+            if (len > 0) {
+                nl++;
+                leaf = j - a0;
+            }
+        }
+        f = warp_sum(f);
+        nl = warp_sum(nl);
+        leaf = warp_max(leaf);
+        bad = __any_sync(kFull, bad);
+        if (lane == 0) {
+            if (bad)
+                atomicOr(&P.cnt->err, kErrBadInput);
+            if (f > INT_MAX) {
+                atomicOr(&P.cnt->err, kErrOverflow);
+                f = INT_MAX;
+            }
+            int bin;
+            if (f == 0)
+                bin = kBinEmpty;
+            else if (nl == 1)
+                bin = kBinCopy;
+            else if (f <= kWarpMaxFlop)
+                bin = kBinWarp;
+            else if (f > kHeavyFlop)
+                bin = kBinHeavy;
+            else
+                bin = kBinMid;
+            P.flop[row] = (int)f;
+            P.spill[row] = 0;
+            if (bin == kBinEmpty)
+                P.nnz[row] = 0;
+            else if (bin == kBinCopy) {
+                P.nnz[row] = (int)f;
+                P.copy_leaf[row] = leaf;
+            }
+            s_bin[slot] = bin;
+            s_idx[slot] = bin == kBinEmpty ? 0 : atomicAdd(&s_cnt[bin], 1);
+            wflop += (unsigned long long)f;
+            wmaxk = max(wmaxk, a1 - a0);
+        }
+    }
+    if (lane == 0) {
+        s_flop[w] = wflop;
+        s_maxk[w] = wmaxk;
+    }
+    __syncthreads();
+    if (threadIdx.x < kNumBins)
+        s_base[threadIdx.x] =
+            s_cnt[threadIdx.x] ? atomicAdd(&P.cnt->bin_count[threadIdx.x], s_cnt[threadIdx.x]) : 0;
+    if (threadIdx.x == 0) {
+        unsigned long long t = 0;
+        int mk = 0;
+        for (int i = 0; i < NW; i++) {
+            t += s_flop[i];
+            mk = max(mk, s_maxk[i]);
+        }
+        if (t)
+            atomicAdd(&P.cnt->total_flop, t);
+        atomicMax(&P.cnt->max_k, mk);
+    }
+    __syncthreads();
+    for (int slot = threadIdx.x; slot < RPB; slot += kAnaThreads) {
+        int bin = s_bin[slot];
+        if (bin > kBinEmpty)
+            P.rows[(size_t)bin * M + s_base[bin] + s_idx[slot]] = row0 + slot;
+    }
+}
+
+void launch_analyze(const CsrDev &A, const CsrDev &B, const PlanDev &P, cudaStream_t s)
+{
+    if (A.M <= 0)
+        return;
+    constexpr int RPB = (kAnaThreads / 32) * kAnaRowsPerWarp;
+    int grid = (A.M + RPB - 1) / RPB;
+    k_analyze<<<grid, kAnaThreads, 0, s>>>(A, B, P);
+}
+
+// ---------------------------------------------------------------------------
+// Exclusive scan (reduce, scan of tile sums, downsweep), out[n] = total.
+// Replaces opt_prefix_sum (spgemm.h:179-187) for crpt and scan_floprC.
+// ---------------------------------------------------------------------------
+constexpr int kScanThreads = 512;
+constexpr int kScanItems = 8;
+constexpr int kScanTile = kScanThreads * kScanItems;
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_reduce(const int *in, int n,
+                                                              long long *tile_sums)
+{
+    __shared__ long long ws[kScanThreads / 32 + 1];
+    const long long base = (long long)blockIdx.x * kScanTile;
+    long long s = 0;
+#pragma unroll
+    for (int i = 0; i < kScanItems; i++) {
+        long long idx = base + (long long)i * kScanThreads + threadIdx.x;
+        if (idx < n)
+            s += in[idx];
+    }
+    long long t = block_sum<kScanThreads>(s, ws);
+    if (threadIdx.x == 0)
+        tile_sums[blockIdx.x] = t;
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_tiles(long long *tile_sums, int ntiles)
+{
+    __shared__ long long ws[kScanThreads / 32 + 1];
+    long long carry = 0;
+    for (int base = 0; base < ntiles; base += kScanThreads) {
+        int idx = base + threadIdx.x;
+        long long v = idx < ntiles ? tile_sums[idx] : 0;
+        long long tot;
+        long long ex = block_excl_scan<kScanThreads>(v, ws, &tot);
+        if (idx < ntiles)
+            tile_sums[idx] = carry + ex;
+        carry += tot;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0)
+        tile_sums[ntiles] = carry;
+}
+
+template <typename OutT>
+__global__ void __launch_bounds__(kScanThreads) k_scan_down(const int *in, int n,
+                                                            const long long *tile_sums,
+                                                            OutT *out, Counters *cnt)
+{
+    __shared__ long long ws[kScanThreads / 32 + 1];
+    const long long base = (long long)blockIdx.x * kScanTile;
+    // blocked arrangement: thread t owns items [t*I, t*I+I) of the tile
+    long long v[kScanItems];
+    long long s = 0;
+#pragma unroll
+    for (int i = 0; i < kScanItems; i++) {
+        long long idx = base + (long long)threadIdx.x * kScanItems + i;
+        v[i] = idx < n ? in[idx] : 0;
+        s += v[i];
+    }
+    long long tot;
+    long long ex = block_excl_scan<kScanThreads>(s, ws, &tot);
+    long long run = tile_sums[blockIdx.x] + ex;
+#pragma unroll
+    for (int i = 0; i < kScanItems; i++) {
+        long long idx = base + (long long)threadIdx.x * kScanItems + i;
+        if (idx < n) {
+            if (sizeof(OutT) == 4 && run > INT_MAX) {
+                if (cnt)
+                    atomicOr(&cnt->err, kErrOverflow);
+                out[idx] = (OutT)INT_MAX;
+            } else {
+                out[idx] = (OutT)run;
+            }
+        }
+        run += v[i];
+    }
+    if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) {
+        long long total = tile_sums[gridDim.x];
+        if (cnt)
+            cnt->cnnz = total;
+        if (sizeof(OutT) == 4 && total > INT_MAX) {
+            if (cnt)
+                atomicOr(&cnt->err, kErrOverflow);
+            out[n] = (OutT)INT_MAX;
+        } else {
+            out[n] = (OutT)total;
+        }
+    }
+}
+
+size_t scan_tmp_bytes(int n)
+{
+    size_t tiles = (size_t)(n + kScanTile - 1) / kScanTile;
+    return (tiles + 2) * sizeof(long long);
+}
+
+template <typename OutT>
+static void scan_impl(const int *in, OutT *out, int n, Counters *cnt, void *tmp, cudaStream_t s)
+{
+    long long *ts = (long long *)tmp;
+    int tiles = (n + kScanTile - 1) / kScanTile;
+    if (tiles == 0)
+        tiles = 1;
+    k_scan_reduce<<<tiles, kScanThreads, 0, s>>>(in, n, ts);
+    k_scan_tiles<<<1, kScanThreads, 0, s>>>(ts, tiles);
+    k_scan_down<OutT><<<tiles, kScanThreads, 0, s>>>(in, n, ts, out, cnt);
+}
+
+void launch_scan_i32(const int *in, int *out, int n, Counters *cnt, void *tmp, cudaStream_t s)
+{
+    scan_impl<int>(in, out, n, cnt, tmp, s);
+}
+
+void launch_scan_i64(const int *in, long long *out, int n, void *tmp, cudaStream_t s)
+{
+    scan_impl<long long>(in, out, n, nullptr, tmp, s);
+}
+
+// ---------------------------------------------------------------------------
+// Upper compaction (spgemm.h:429-444): one warp per row, C_bar -> C.
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(256) k_compact(int M, const long long *scan_flop, const int *len,
+                                                 const int *bar_col, const T *bar_val,
+                                                 const int *crpt, int *ccol, T *cval)
+{
+    const int lane = threadIdx.x & 31;
+    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    for (int row = gw; row < M; row += nw) {
+        const long long src = scan_flop[row];
+        const int dst = crpt[row];
+        const int n = len[row];
+        for (int q = lane; q < n; q += 32) {
+            ccol[dst + q] = bar_col[src + q];
+            cval[dst + q] = bar_val[src + q];
+        }
+    }
+}
+
+void launch_compact(int dtype, const PlanDev &P, const int *bar_col, const void *bar_val,
+                    const int *crpt, int *ccol, void *cval, cudaStream_t s)
+{
+    if (P.M <= 0)
+        return;
+    int grid = (P.M + 7) / 8;
+    if (grid > 65535 * 4)
+        grid = 65535 * 4;
+    if (dtype == 0)
+        k_compact<double><<<grid, 256, 0, s>>>(P.M, P.scan_flop, P.nnz, bar_col,
+                                                (const double *)bar_val, crpt, ccol, (double *)cval);
+    else
+        k_compact<float><<<grid, 256, 0, s>>>(P.M, P.scan_flop, P.nnz, bar_col,
+                                               (const float *)bar_val, crpt, ccol, (float *)cval);
+}
+
+// ---------------------------------------------------------------------------
+// CSR validation (the invariants the reference's reader enforces,
+// CSR.cpp:454-477): rpt[0] == 0, rpt non-decreasing, rpt[M] == nnz, columns in
+// [0, ncols) and strictly increasing within each row.  One warp per row;
+// *bad_row receives the smallest offending row (atomicMin), -1 if none was
+// seen (the host initialises it to INT_MAX).
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_validate(CsrDev X, int ncols, int *bad_row)
+{
+    const int lane = threadIdx.x & 31;
+    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    if (gw == 0 && lane == 0) {
+        if (X.rpt[0] != 0)
+            atomicMin(bad_row, 0);
+        if (X.rpt[X.M] != X.nnz)
+            atomicMin(bad_row, X.M > 0 ? X.M - 1 : 0);
+    }
+    for (int row = gw; row < X.M; row += nw) {
+        const int s = X.rpt[row], e = X.rpt[row + 1];
+        bool bad = (s > e) || (s < 0) || (e > X.nnz);
+        if (!bad) {
+            for (int j = s + lane; j < e; j += 32) {
+                int c = X.col[j];
+                if ((unsigned)c >= (unsigned)ncols)
+                    bad = true;
+                else if (j + 1 < e && X.col[j + 1] <= c)
+                    bad = true;
+            }
+        }
+        if (__any_sync(kFull, bad) && lane == 0)
+            atomicMin(bad_row, row);
+    }
+}
+
+void launch_validate(const CsrDev &X, int ncols, int *bad_row, cudaStream_t s)
+{
+    int grid = (X.M + 7) / 8;
+    if (grid < 1)
+        grid = 1;
+    if (grid > 65535 * 4)
+        grid = 65535 * 4;
+    k_validate<<<grid, 256, 0, s>>>(X, ncols, bad_row);
+}
+
+}  // namespace brm

@@ -1,0 +1,838 @@
+// brm_api.cu -- host orchestration behind the C ABI in include/brmerge.h.
+//
+// Phase order follows brmerge_precise (BRMerge-SpGEMM/inc/spgemm.h:468-735)
+// and brmerge_upper (spgemm.h:220-457); every phase is a kernel launch on
+// the context's stream.  The only host synchronisations are the ones the
+// interface needs: nnz(C) after the symbolic phase (the caller allocates C),
+// and the error word after the numeric phase.
+#include <chrono>
+#include <climits>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+
+#include "brm_kernels.h"
+#include "brmerge.h"
+
+namespace {
+
+struct DevBuf {
+    void *p = nullptr;
+    size_t cap = 0;
+};
+
+constexpr int kNumEvents = 12;
+
+}  // namespace
+
+struct brm_context_s {
+    int device = 0;
+    int num_sms = 0;
+    cudaStream_t stream = nullptr;
+    bool validate = false;
+    // plan workspace
+    void *ws = nullptr;
+    size_t ws_bytes = 0;
+    int ws_M = -1;
+    brm::PlanDev plan{};
+    void *scan_tmp = nullptr;
+    int *d_bad = nullptr;
+    brm::Counters *h_cnt = nullptr;  // pinned mirror of the device counters
+    int *h_bad = nullptr;            // pinned
+    // spill scratch
+    DevBuf spill;
+    // Upper upper-bound buffer
+    DevBuf bar_col, bar_val;
+    // plan identity (symbolic -> numeric)
+    bool planned = false;
+    const int *a_rpt = nullptr, *a_col = nullptr, *b_rpt = nullptr, *b_col = nullptr;
+    int pM = 0, pK = 0, pN = 0;
+    unsigned long long spill_bytes = 0;
+    int last_err = 0;
+    // device copies for the host drop-ins
+    DevBuf io_arpt, io_acol, io_aval, io_brpt, io_bcol, io_bval, io_crpt, io_ccol, io_cval;
+    cudaEvent_t ev[kNumEvents] = {};
+};
+
+namespace {
+
+int cuda_status(cudaError_t e)
+{
+    if (e == cudaSuccess)
+        return BRM_SUCCESS;
+    if (e == cudaErrorMemoryAllocation)
+        return BRM_ERR_ALLOC;
+    if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver)
+        return BRM_ERR_NO_DEVICE;
+    return BRM_ERR_CUDA;
+}
+
+#define BRM_CK(call)                                  \
+    do {                                              \
+        cudaError_t e_ = (call);                      \
+        if (e_ != cudaSuccess) {                      \
+            (void)cudaGetLastError();                 \
+            return cuda_status(e_);                   \
+        }                                             \
+    } while (0)
+
+#define BRM_TRY(call)              \
+    do {                           \
+        int s_ = (call);           \
+        if (s_ != BRM_SUCCESS)     \
+            return s_;             \
+    } while (0)
+
+size_t a256(size_t x) { return (x + 255) & ~size_t(255); }
+
+int grow(DevBuf &b, size_t bytes)
+{
+    if (bytes <= b.cap && b.p)
+        return BRM_SUCCESS;
+    if (b.p) {
+        cudaFree(b.p);
+        b.p = nullptr;
+        b.cap = 0;
+    }
+    size_t want = bytes < 256 ? 256 : bytes;
+    BRM_CK(cudaMalloc(&b.p, want));
+    b.cap = want;
+    return BRM_SUCCESS;
+}
+
+void release(DevBuf &b)
+{
+    if (b.p)
+        cudaFree(b.p);
+    b.p = nullptr;
+    b.cap = 0;
+}
+
+size_t workspace_bytes(int M)
+{
+    size_t m = (size_t)(M > 0 ? M : 1);
+    size_t b = 0;
+    b += a256(4 * m);                       // flop
+    b += a256(4 * (m + 1));                 // nnz
+    b += a256(4 * (size_t)brm::kNumBins * m);  // rows
+    b += a256(4 * m);                       // copy_leaf
+    b += a256(m);                           // spill flags
+    b += a256(4 * m);                       // spill_rows
+    b += a256(8 * m);                       // spill_off
+    b += a256(8 * (m + 1));                 // scan_flop
+    b += a256(sizeof(brm::Counters));
+    b += a256(brm::scan_tmp_bytes((int)m + 1));
+    b += a256(4);                           // bad row
+    return b;
+}
+
+int ensure_workspace(brm_context ctx, int M)
+{
+    if (ctx->ws && M <= ctx->ws_M)
+        return BRM_SUCCESS;
+    if (ctx->ws) {
+        cudaFree(ctx->ws);
+        ctx->ws = nullptr;
+    }
+    size_t bytes = workspace_bytes(M);
+    BRM_CK(cudaMalloc(&ctx->ws, bytes));
+    ctx->ws_bytes = bytes;
+    ctx->ws_M = M;
+    size_t m = (size_t)(M > 0 ? M : 1);
+    unsigned char *p = (unsigned char *)ctx->ws;
+    size_t off = 0;
+    auto take = [&](size_t n) {
+        unsigned char *r = p + off;
+        off += a256(n);
+        return r;
+    };
+    brm::PlanDev &P = ctx->plan;
+    P.flop = (int *)take(4 * m);
+    P.nnz = (int *)take(4 * (m + 1));
+    P.rows = (int *)take(4 * (size_t)brm::kNumBins * m);
+    P.copy_leaf = (int *)take(4 * m);
+    P.spill = (unsigned char *)take(m);
+    P.spill_rows = (int *)take(4 * m);
+    P.spill_off = (unsigned long long *)take(8 * m);
+    P.scan_flop = (long long *)take(8 * (m + 1));
+    P.cnt = (brm::Counters *)take(sizeof(brm::Counters));
+    ctx->scan_tmp = take(brm::scan_tmp_bytes((int)m + 1));
+    ctx->d_bad = (int *)take(4);
+    return BRM_SUCCESS;
+}
+
+brm::CsrDev to_dev(const brm_csr *X)
+{
+    brm::CsrDev d;
+    d.M = X->M;
+    d.N = X->N;
+    d.nnz = X->nnz;
+    d.rpt = X->rpt;
+    d.col = X->col;
+    d.val = X->val;
+    return d;
+}
+
+int check_pair(const brm_csr *A, const brm_csr *B)
+{
+    if (!A || !B)
+        return BRM_ERR_INVALID_VALUE;
+    if (A->M < 0 || A->N < 0 || B->M < 0 || B->N < 0 || A->nnz < 0 || B->nnz < 0)
+        return BRM_ERR_INVALID_VALUE;
+    if (A->N != B->M)
+        return BRM_ERR_INVALID_VALUE;
+    if (!A->rpt || !B->rpt)
+        return BRM_ERR_INVALID_VALUE;
+    if ((A->nnz > 0 && !A->col) || (B->nnz > 0 && !B->col))
+        return BRM_ERR_INVALID_VALUE;
+    return BRM_SUCCESS;
+}
+
+int device_err_status(int err)
+{
+    if (err == 0)
+        return BRM_SUCCESS;
+    if (err & brm::kErrOverflow)
+        return BRM_ERR_OVERFLOW;
+    if (err & brm::kErrBadInput)
+        return BRM_ERR_INVALID_CSR;
+    return BRM_ERR_INTERNAL;
+}
+
+int validate_one(brm_context ctx, const brm_csr *X, int ncols, int *bad_row)
+{
+    BRM_TRY(ensure_workspace(ctx, ctx->ws_M > 0 ? ctx->ws_M : 1));
+    BRM_CK(cudaMemsetAsync(ctx->d_bad, 0x7f, sizeof(int), ctx->stream));
+    brm::launch_validate(to_dev(X), ncols, ctx->d_bad, ctx->stream);
+    BRM_CK(cudaGetLastError());
+    BRM_CK(cudaMemcpyAsync(ctx->h_bad, ctx->d_bad, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    BRM_CK(cudaStreamSynchronize(ctx->stream));
+    const int b = *ctx->h_bad;  // 0x7f7f7f7f: the memset pattern, no offending row
+    *bad_row = (b == 0x7f7f7f7f) ? -1 : b;
+    return *bad_row < 0 ? BRM_SUCCESS : BRM_ERR_INVALID_CSR;
+}
+
+int validate_pair(brm_context ctx, const brm_csr *A, const brm_csr *B)
+{
+    int bad = -1;
+    BRM_TRY(validate_one(ctx, A, A->N, &bad));
+    BRM_TRY(validate_one(ctx, B, B->N, &bad));
+    return BRM_SUCCESS;
+}
+
+void ev_record(brm_context ctx, bool on, int i)
+{
+    if (on)
+        cudaEventRecord(ctx->ev[i], ctx->stream);
+}
+
+double ev_sec(brm_context ctx, int a, int b)
+{
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, ctx->ev[a], ctx->ev[b]) != cudaSuccess)
+        return 0.0;
+    return ms * 1e-3;
+}
+
+// Analysis + symbolic (+ crpt scan for Precise).  Leaves ctx->h_cnt filled.
+// Event indices: 0 start, 1 after analysis, 2 after symbolic, 3 after scan.
+int plan_phase(brm_context ctx, const brm_csr *A, const brm_csr *B, int *crpt, bool upper,
+               bool timed)
+{
+    BRM_TRY(ensure_workspace(ctx, A->M));
+    if (ctx->validate)
+        BRM_TRY(validate_pair(ctx, A, B));
+    brm::CsrDev a = to_dev(A), b = to_dev(B);
+    brm::PlanDev P = ctx->plan;
+    P.M = A->M;
+    ctx->plan.M = A->M;
+    cudaStream_t s = ctx->stream;
+    ev_record(ctx, timed, 0);
+    BRM_CK(cudaMemsetAsync(P.cnt, 0, sizeof(brm::Counters), s));
+    brm::launch_analyze(a, b, P, s);
+    ev_record(ctx, timed, 1);
+    brm::launch_symbolic(a, b, P, ctx->num_sms, upper, s);
+    ev_record(ctx, timed, 2);
+    if (upper)
+        brm::launch_scan_i64(P.flop, P.scan_flop, A->M, ctx->scan_tmp, s);
+    else
+        brm::launch_scan_i32(P.nnz, crpt, A->M, P.cnt, ctx->scan_tmp, s);
+    ev_record(ctx, timed, 3);
+    BRM_CK(cudaGetLastError());
+    BRM_CK(cudaMemcpyAsync(ctx->h_cnt, P.cnt, sizeof(brm::Counters), cudaMemcpyDeviceToHost, s));
+    BRM_CK(cudaStreamSynchronize(s));
+    ctx->last_err = ctx->h_cnt->err;
+    BRM_TRY(device_err_status(ctx->h_cnt->err));
+    ctx->planned = true;
+    ctx->a_rpt = A->rpt;
+    ctx->a_col = A->col;
+    ctx->b_rpt = B->rpt;
+    ctx->b_col = B->col;
+    ctx->pM = A->M;
+    ctx->pK = A->N;
+    ctx->pN = B->N;
+    ctx->spill_bytes = ctx->h_cnt->spill_bytes;
+    return BRM_SUCCESS;
+}
+
+bool plan_matches(brm_context ctx, const brm_csr *A, const brm_csr *B)
+{
+    return ctx->planned && ctx->a_rpt == A->rpt && ctx->a_col == A->col && ctx->b_rpt == B->rpt &&
+           ctx->b_col == B->col && ctx->pM == A->M && ctx->pK == A->N && ctx->pN == B->N;
+}
+
+int numeric_launch(brm_context ctx, brm_dtype dtype, bool upper, const brm_csr *A,
+                   const brm_csr *B, const int *crpt, int *ccol, void *cval)
+{
+    if (ctx->spill_bytes)
+        BRM_TRY(grow(ctx->spill, ctx->spill_bytes));
+    cudaStream_t s = ctx->stream;
+    brm::PlanDev P = ctx->plan;
+    BRM_CK(cudaMemsetAsync(&P.cnt->work_num, 0, 2 * sizeof(int), s));  // work_num, err
+    brm::CsrDev a = to_dev(A), b = to_dev(B);
+    if (dtype == BRM_F64)
+        brm::launch_numeric_f64(upper, a, b, P, crpt, ccol, cval, ctx->spill.p, ctx->spill_bytes,
+                                ctx->num_sms, s);
+    else
+        brm::launch_numeric_f32(upper, a, b, P, crpt, ccol, cval, ctx->spill.p, ctx->spill_bytes,
+                                ctx->num_sms, s);
+    BRM_CK(cudaGetLastError());
+    return BRM_SUCCESS;
+}
+
+int read_err(brm_context ctx)
+{
+    BRM_CK(cudaMemcpyAsync(&ctx->h_cnt->err, &ctx->plan.cnt->err, sizeof(int),
+                           cudaMemcpyDeviceToHost, ctx->stream));
+    BRM_CK(cudaStreamSynchronize(ctx->stream));
+    ctx->last_err = ctx->h_cnt->err;
+    return device_err_status(ctx->h_cnt->err);
+}
+
+int check_dtype(brm_dtype d) { return (d == BRM_F64 || d == BRM_F32) ? BRM_SUCCESS : BRM_ERR_INVALID_VALUE; }
+
+size_t vsize(brm_dtype d) { return d == BRM_F64 ? 8 : 4; }
+
+// Upper after plan_phase(upper): numeric into C_bar, scan of the real row
+// sizes, compaction into the caller's C.  Events 4.. as in upper timing.
+int upper_numeric_into_bar(brm_context ctx, brm_dtype dtype, const brm_csr *A, const brm_csr *B)
+{
+    unsigned long long tf = ctx->h_cnt->total_flop;
+    BRM_TRY(grow(ctx->bar_col, (size_t)tf * 4));
+    BRM_TRY(grow(ctx->bar_val, (size_t)tf * vsize(dtype)));
+    return numeric_launch(ctx, dtype, true, A, B, nullptr, (int *)ctx->bar_col.p, ctx->bar_val.p);
+}
+
+std::mutex g_mu;
+brm_context g_ctx = nullptr;
+
+int default_ctx(brm_context *out)
+{
+    if (!g_ctx) {
+        BRM_TRY(brm_create(&g_ctx));
+        g_ctx->validate = true;
+    }
+    *out = g_ctx;
+    return BRM_SUCCESS;
+}
+
+double now_sec()
+{
+    using namespace std::chrono;
+    return duration<double>(steady_clock::now().time_since_epoch()).count();
+}
+
+// Host drop-in shared by the four host entry points.
+template <typename T>
+int host_call(bool upper, const int *arpt, const int *acol, const T *aval, const int *brpt,
+              const int *bcol, const T *bval, int **crpt_, int **ccol_, T **cval_, int M, int K,
+              int N, int *cnnz_, brm_precise_timing *pt, brm_upper_timing *ut)
+{
+    if (!crpt_ || !ccol_ || !cval_ || !cnnz_ || M < 0 || K < 0 || N < 0 || !arpt || !brpt)
+        return BRM_ERR_INVALID_VALUE;
+    const brm_dtype dtype = sizeof(T) == 8 ? BRM_F64 : BRM_F32;
+    std::lock_guard<std::mutex> lock(g_mu);
+    double t_start = now_sec();
+    brm_context ctx;
+    BRM_TRY(default_ctx(&ctx));
+    cudaStream_t s = ctx->stream;
+    const int nnzA = arpt[M], nnzB = brpt[K];
+    if (nnzA < 0 || nnzB < 0 || (nnzA > 0 && (!acol || !aval)) || (nnzB > 0 && (!bcol || !bval)))
+        return BRM_ERR_INVALID_VALUE;
+    const bool same = (arpt == brpt && acol == bcol && aval == bval && M == K);
+    BRM_TRY(grow(ctx->io_arpt, 4 * ((size_t)M + 1)));
+    BRM_TRY(grow(ctx->io_acol, 4 * (size_t)nnzA));
+    BRM_TRY(grow(ctx->io_aval, sizeof(T) * (size_t)nnzA));
+    BRM_CK(cudaMemcpyAsync(ctx->io_arpt.p, arpt, 4 * ((size_t)M + 1), cudaMemcpyHostToDevice, s));
+    BRM_CK(cudaMemcpyAsync(ctx->io_acol.p, acol, 4 * (size_t)nnzA, cudaMemcpyHostToDevice, s));
+    BRM_CK(cudaMemcpyAsync(ctx->io_aval.p, aval, sizeof(T) * (size_t)nnzA, cudaMemcpyHostToDevice, s));
+    brm_csr A{M, K, nnzA, (const int *)ctx->io_arpt.p, (const int *)ctx->io_acol.p, ctx->io_aval.p};
+    brm_csr B = A;
+    B.N = N;
+    if (!same) {
+        BRM_TRY(grow(ctx->io_brpt, 4 * ((size_t)K + 1)));
+        BRM_TRY(grow(ctx->io_bcol, 4 * (size_t)nnzB));
+        BRM_TRY(grow(ctx->io_bval, sizeof(T) * (size_t)nnzB));
+        BRM_CK(cudaMemcpyAsync(ctx->io_brpt.p, brpt, 4 * ((size_t)K + 1), cudaMemcpyHostToDevice, s));
+        BRM_CK(cudaMemcpyAsync(ctx->io_bcol.p, bcol, 4 * (size_t)nnzB, cudaMemcpyHostToDevice, s));
+        BRM_CK(cudaMemcpyAsync(ctx->io_bval.p, bval, sizeof(T) * (size_t)nnzB, cudaMemcpyHostToDevice, s));
+        B = brm_csr{K, N, nnzB, (const int *)ctx->io_brpt.p, (const int *)ctx->io_bcol.p, ctx->io_bval.p};
+    }
+    BRM_TRY(grow(ctx->io_crpt, 4 * ((size_t)M + 1)));
+    double t_pre = now_sec();
+    int cnnz = 0;
+    double t_sym0 = 0, t_sym1 = 0, t_num0 = 0, t_num1 = 0;
+    if (!upper) {
+        t_sym0 = now_sec();
+        BRM_TRY(brm_symbolic(ctx, &A, &B, (int *)ctx->io_crpt.p, &cnnz));
+        t_sym1 = now_sec();
+        BRM_TRY(grow(ctx->io_ccol, 4 * (size_t)cnnz));
+        BRM_TRY(grow(ctx->io_cval, sizeof(T) * (size_t)cnnz));
+        t_num0 = now_sec();
+        BRM_TRY(brm_numeric(ctx, dtype, &A, &B, (const int *)ctx->io_crpt.p, (int *)ctx->io_ccol.p,
+                            ctx->io_cval.p));
+        t_num1 = now_sec();
+    } else {
+        t_sym0 = now_sec();
+        BRM_TRY(plan_phase(ctx, &A, &B, nullptr, true, false));
+        BRM_TRY(upper_numeric_into_bar(ctx, dtype, &A, &B));
+        brm::launch_scan_i32(ctx->plan.nnz, (int *)ctx->io_crpt.p, M, ctx->plan.cnt, ctx->scan_tmp, s);
+        BRM_CK(cudaGetLastError());
+        BRM_CK(cudaMemcpyAsync(ctx->h_cnt, ctx->plan.cnt, sizeof(brm::Counters), cudaMemcpyDeviceToHost, s));
+        BRM_CK(cudaStreamSynchronize(s));
+        ctx->last_err = ctx->h_cnt->err;
+        BRM_TRY(device_err_status(ctx->h_cnt->err));
+        cnnz = (int)ctx->h_cnt->cnnz;
+        t_sym1 = now_sec();
+        BRM_TRY(grow(ctx->io_ccol, 4 * (size_t)cnnz));
+        BRM_TRY(grow(ctx->io_cval, sizeof(T) * (size_t)cnnz));
+        t_num0 = now_sec();
+        brm::launch_compact(dtype == BRM_F64 ? 0 : 1, ctx->plan, (const int *)ctx->bar_col.p,
+                            ctx->bar_val.p, (const int *)ctx->io_crpt.p, (int *)ctx->io_ccol.p,
+                            ctx->io_cval.p, s);
+        BRM_CK(cudaGetLastError());
+        BRM_TRY(read_err(ctx));
+        t_num1 = now_sec();
+    }
+    int *crpt = (int *)std::malloc(4 * ((size_t)M + 1));
+    int *ccol = (int *)std::malloc(4 * (size_t)(cnnz > 0 ? cnnz : 1));
+    T *cval = (T *)std::malloc(sizeof(T) * (size_t)(cnnz > 0 ? cnnz : 1));
+    if (!crpt || !ccol || !cval) {
+        std::free(crpt);
+        std::free(ccol);
+        std::free(cval);
+        return BRM_ERR_ALLOC;
+    }
+    cudaError_t e1 = cudaMemcpyAsync(crpt, ctx->io_crpt.p, 4 * ((size_t)M + 1), cudaMemcpyDeviceToHost, s);
+    cudaError_t e2 = cudaMemcpyAsync(ccol, ctx->io_ccol.p, 4 * (size_t)cnnz, cudaMemcpyDeviceToHost, s);
+    cudaError_t e3 = cudaMemcpyAsync(cval, ctx->io_cval.p, sizeof(T) * (size_t)cnnz, cudaMemcpyDeviceToHost, s);
+    cudaError_t e4 = cudaStreamSynchronize(s);
+    if (e1 != cudaSuccess || e2 != cudaSuccess || e3 != cudaSuccess || e4 != cudaSuccess) {
+        std::free(crpt);
+        std::free(ccol);
+        std::free(cval);
+        (void)cudaGetLastError();
+        return BRM_ERR_CUDA;
+    }
+    double t_end = now_sec();
+    *crpt_ = crpt;
+    *ccol_ = ccol;
+    *cval_ = cval;
+    *cnnz_ = cnnz;
+    if (pt) {
+        std::memset(pt, 0, sizeof(*pt));
+        pt->pre_allocate = t_pre - t_start;
+        pt->symbolic = t_sym1 - t_sym0;
+        pt->allocate_C = t_num0 - t_sym1;
+        pt->compute = t_num1 - t_num0;
+        pt->cleanup = t_end - t_num1;
+        pt->total = t_end - t_start;
+    }
+    if (ut) {
+        std::memset(ut, 0, sizeof(*ut));
+        ut->pre_allocate = t_pre - t_start;
+        ut->compute = t_sym1 - t_sym0;
+        ut->allocate_C = t_num0 - t_sym1;
+        ut->copy = t_num1 - t_num0;
+        ut->cleanup = t_end - t_num1;
+        ut->total = t_end - t_start;
+    }
+    return BRM_SUCCESS;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *brm_status_string(int status)
+{
+    switch (status) {
+    case BRM_SUCCESS: return "success";
+    case BRM_ERR_INVALID_VALUE: return "invalid argument";
+    case BRM_ERR_INVALID_CSR: return "input violates the CSR invariants";
+    case BRM_ERR_ALLOC: return "allocation failed";
+    case BRM_ERR_CUDA: return "CUDA runtime error";
+    case BRM_ERR_OVERFLOW: return "nnz(C) does not fit int32";
+    case BRM_ERR_NOT_PLANNED: return "numeric phase without a matching symbolic phase";
+    case BRM_ERR_INTERNAL: return "device-side invariant failed";
+    case BRM_ERR_TIMEOUT: return "bounded device wait expired";
+    case BRM_ERR_NO_DEVICE: return "no CUDA device";
+    case BRM_ERR_CAPACITY: return "request exceeds a fixed capacity";
+    default: return "unknown status";
+    }
+}
+
+int brm_create(brm_context *out)
+{
+    if (!out)
+        return BRM_ERR_INVALID_VALUE;
+    *out = nullptr;
+    int dev = 0;
+    BRM_CK(cudaGetDevice(&dev));
+    brm_context ctx = new (std::nothrow) brm_context_s();
+    if (!ctx)
+        return BRM_ERR_ALLOC;
+    ctx->device = dev;
+    cudaError_t e = cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e == cudaSuccess)
+        e = cudaMallocHost(&ctx->h_cnt, sizeof(brm::Counters));
+    if (e == cudaSuccess)
+        e = cudaMallocHost(&ctx->h_bad, sizeof(int));
+    for (int i = 0; i < kNumEvents && e == cudaSuccess; i++)
+        e = cudaEventCreate(&ctx->ev[i]);
+    if (e == cudaSuccess) {
+        // keep freed stream-ordered allocations cached in this process so
+        // repeated calls do not return memory to the driver between calls
+        cudaMemPool_t pool;
+        if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+            unsigned long long keep = ~0ull;
+            cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+        }
+        (void)cudaGetLastError();
+    }
+    if (e != cudaSuccess) {
+        brm_destroy(ctx);
+        (void)cudaGetLastError();
+        return cuda_status(e);
+    }
+    *out = ctx;
+    return BRM_SUCCESS;
+}
+
+int brm_destroy(brm_context ctx)
+{
+    if (!ctx)
+        return BRM_ERR_INVALID_VALUE;
+    if (ctx->stream)
+        cudaStreamSynchronize(ctx->stream);
+    else
+        cudaDeviceSynchronize();
+    if (ctx->ws)
+        cudaFree(ctx->ws);
+    release(ctx->spill);
+    release(ctx->bar_col);
+    release(ctx->bar_val);
+    release(ctx->io_arpt);
+    release(ctx->io_acol);
+    release(ctx->io_aval);
+    release(ctx->io_brpt);
+    release(ctx->io_bcol);
+    release(ctx->io_bval);
+    release(ctx->io_crpt);
+    release(ctx->io_ccol);
+    release(ctx->io_cval);
+    if (ctx->h_cnt)
+        cudaFreeHost(ctx->h_cnt);
+    if (ctx->h_bad)
+        cudaFreeHost(ctx->h_bad);
+    for (int i = 0; i < kNumEvents; i++)
+        if (ctx->ev[i])
+            cudaEventDestroy(ctx->ev[i]);
+    delete ctx;
+    return BRM_SUCCESS;
+}
+
+int brm_set_stream(brm_context ctx, void *stream)
+{
+    if (!ctx)
+        return BRM_ERR_INVALID_VALUE;
+    ctx->stream = (cudaStream_t)stream;
+    return BRM_SUCCESS;
+}
+
+int brm_set_validate(brm_context ctx, int on)
+{
+    if (!ctx)
+        return BRM_ERR_INVALID_VALUE;
+    ctx->validate = on != 0;
+    return BRM_SUCCESS;
+}
+
+int brm_last_device_error(brm_context ctx) { return ctx ? ctx->last_err : -1; }
+
+int brm_symbolic(brm_context ctx, const brm_csr *A, const brm_csr *B, int *crpt, int *cnnz)
+{
+    if (!ctx || !crpt || !cnnz)
+        return BRM_ERR_INVALID_VALUE;
+    BRM_TRY(check_pair(A, B));
+    ctx->planned = false;
+    BRM_TRY(plan_phase(ctx, A, B, crpt, false, false));
+    *cnnz = (int)ctx->h_cnt->cnnz;
+    return BRM_SUCCESS;
+}
+
+int brm_numeric(brm_context ctx, brm_dtype dtype, const brm_csr *A, const brm_csr *B,
+                const int *crpt, int *ccol, void *cval)
+{
+    if (!ctx || !crpt)
+        return BRM_ERR_INVALID_VALUE;
+    BRM_TRY(check_dtype(dtype));
+    BRM_TRY(check_pair(A, B));
+    if (!plan_matches(ctx, A, B))
+        return BRM_ERR_NOT_PLANNED;
+    if (ctx->h_cnt->cnnz > 0 && (!ccol || !cval))
+        return BRM_ERR_INVALID_VALUE;
+    if ((A->nnz > 0 && !A->val) || (B->nnz > 0 && !B->val))
+        return BRM_ERR_INVALID_VALUE;
+    BRM_TRY(numeric_launch(ctx, dtype, false, A, B, crpt, ccol, cval));
+    return read_err(ctx);
+}
+
+int brm_precise_device(brm_context ctx, brm_dtype dtype, const brm_csr *A, const brm_csr *B,
+                       int **crpt_, int **ccol_, void **cval_, int *cnnz_,
+                       brm_precise_timing *timing)
+{
+    if (!ctx || !crpt_ || !ccol_ || !cval_ || !cnnz_)
+        return BRM_ERR_INVALID_VALUE;
+    BRM_TRY(check_dtype(dtype));
+    BRM_TRY(check_pair(A, B));
+    const bool timed = timing != nullptr;
+    double t0 = now_sec();
+    int *crpt = nullptr;
+    BRM_CK(cudaMallocAsync((void **)&crpt, 4 * ((size_t)A->M + 1), ctx->stream));
+    double t1 = now_sec();
+    ctx->planned = false;
+    int st = plan_phase(ctx, A, B, crpt, false, timed);
+    if (st != BRM_SUCCESS) {
+        cudaFreeAsync(crpt, ctx->stream);
+        return st;
+    }
+    int cnnz = (int)ctx->h_cnt->cnnz;
+    int *ccol = nullptr;
+    void *cval = nullptr;
+    double t2 = now_sec();
+    cudaError_t e = cudaMallocAsync((void **)&ccol, 4 * (size_t)(cnnz > 0 ? cnnz : 1), ctx->stream);
+    if (e == cudaSuccess)
+        e = cudaMallocAsync(&cval, vsize(dtype) * (size_t)(cnnz > 0 ? cnnz : 1), ctx->stream);
+    if (e != cudaSuccess) {
+        cudaFreeAsync(crpt, ctx->stream);
+        if (ccol)
+            cudaFreeAsync(ccol, ctx->stream);
+        (void)cudaGetLastError();
+        return cuda_status(e);
+    }
+    double t3 = now_sec();
+    ev_record(ctx, timed, 4);
+    st = numeric_launch(ctx, dtype, false, A, B, crpt, ccol, cval);
+    ev_record(ctx, timed, 5);
+    if (st == BRM_SUCCESS)
+        st = read_err(ctx);
+    if (st != BRM_SUCCESS) {
+        cudaFreeAsync(crpt, ctx->stream);
+        cudaFreeAsync(ccol, ctx->stream);
+        cudaFreeAsync(cval, ctx->stream);
+        return st;
+    }
+    double t4 = now_sec();
+    *crpt_ = crpt;
+    *ccol_ = ccol;
+    *cval_ = cval;
+    *cnnz_ = cnnz;
+    if (timed) {
+        std::memset(timing, 0, sizeof(*timing));
+        timing->pre_allocate = t1 - t0;
+        timing->compute_flop = ev_sec(ctx, 0, 1);
+        timing->symbolic = ev_sec(ctx, 1, 2);
+        timing->prefix_sum_nnz = ev_sec(ctx, 2, 3);
+        timing->allocate_C = t3 - t2;
+        timing->compute = ev_sec(ctx, 4, 5);
+        timing->total = t4 - t0;
+    }
+    return BRM_SUCCESS;
+}
+
+int brm_upper_device(brm_context ctx, brm_dtype dtype, const brm_csr *A, const brm_csr *B,
+                     int **crpt_, int **ccol_, void **cval_, int *cnnz_, brm_upper_timing *timing)
+{
+    if (!ctx || !crpt_ || !ccol_ || !cval_ || !cnnz_)
+        return BRM_ERR_INVALID_VALUE;
+    BRM_TRY(check_dtype(dtype));
+    BRM_TRY(check_pair(A, B));
+    const bool timed = timing != nullptr;
+    double t0 = now_sec();
+    ctx->planned = false;
+    BRM_TRY(plan_phase(ctx, A, B, nullptr, true, timed));
+    double t1 = now_sec();
+    BRM_TRY(grow(ctx->bar_col, (size_t)ctx->h_cnt->total_flop * 4));
+    BRM_TRY(grow(ctx->bar_val, (size_t)ctx->h_cnt->total_flop * vsize(dtype)));
+    double t2 = now_sec();
+    int *crpt = nullptr;
+    BRM_CK(cudaMallocAsync((void **)&crpt, 4 * ((size_t)A->M + 1), ctx->stream));
+    ev_record(ctx, timed, 4);
+    int st = numeric_launch(ctx, dtype, true, A, B, nullptr, (int *)ctx->bar_col.p, ctx->bar_val.p);
+    ev_record(ctx, timed, 5);
+    if (st == BRM_SUCCESS) {
+        brm::launch_scan_i32(ctx->plan.nnz, crpt, A->M, ctx->plan.cnt, ctx->scan_tmp, ctx->stream);
+        ev_record(ctx, timed, 6);
+        cudaError_t e = cudaMemcpyAsync(ctx->h_cnt, ctx->plan.cnt, sizeof(brm::Counters),
+                                        cudaMemcpyDeviceToHost, ctx->stream);
+        if (e == cudaSuccess)
+            e = cudaStreamSynchronize(ctx->stream);
+        st = cuda_status(e);
+        if (st == BRM_SUCCESS) {
+            ctx->last_err = ctx->h_cnt->err;
+            st = device_err_status(ctx->h_cnt->err);
+        }
+    }
+    if (st != BRM_SUCCESS) {
+        cudaFreeAsync(crpt, ctx->stream);
+        return st;
+    }
+    int cnnz = (int)ctx->h_cnt->cnnz;
+    double t3 = now_sec();
+    int *ccol = nullptr;
+    void *cval = nullptr;
+    cudaError_t e = cudaMallocAsync((void **)&ccol, 4 * (size_t)(cnnz > 0 ? cnnz : 1), ctx->stream);
+    if (e == cudaSuccess)
+        e = cudaMallocAsync(&cval, vsize(dtype) * (size_t)(cnnz > 0 ? cnnz : 1), ctx->stream);
+    if (e != cudaSuccess) {
+        cudaFreeAsync(crpt, ctx->stream);
+        if (ccol)
+            cudaFreeAsync(ccol, ctx->stream);
+        (void)cudaGetLastError();
+        return cuda_status(e);
+    }
+    double t4 = now_sec();
+    ev_record(ctx, timed, 7);
+    brm::launch_compact(dtype == BRM_F64 ? 0 : 1, ctx->plan, (const int *)ctx->bar_col.p,
+                        ctx->bar_val.p, crpt, ccol, cval, ctx->stream);
+    ev_record(ctx, timed, 8);
+    st = read_err(ctx);
+    if (st != BRM_SUCCESS) {
+        cudaFreeAsync(crpt, ctx->stream);
+        cudaFreeAsync(ccol, ctx->stream);
+        cudaFreeAsync(cval, ctx->stream);
+        return st;
+    }
+    double t5 = now_sec();
+    *crpt_ = crpt;
+    *ccol_ = ccol;
+    *cval_ = cval;
+    *cnnz_ = cnnz;
+    if (timed) {
+        std::memset(timing, 0, sizeof(*timing));
+        timing->compute_flop = ev_sec(ctx, 0, 1);
+        timing->load_balance = ev_sec(ctx, 1, 2);
+        timing->prefix_sum_flop = ev_sec(ctx, 2, 3);
+        timing->allocate_hook = t2 - t1;
+        timing->compute = ev_sec(ctx, 4, 5);
+        timing->prefix_sum_nnz = ev_sec(ctx, 5, 6);
+        timing->allocate_C = t4 - t3;
+        timing->copy = ev_sec(ctx, 7, 8);
+        timing->total = t5 - t0;
+    }
+    return BRM_SUCCESS;
+}
+
+int brm_device_free(brm_context ctx, void *p)
+{
+    if (!p)
+        return BRM_SUCCESS;
+    BRM_CK(cudaFreeAsync(p, ctx ? ctx->stream : nullptr));
+    return BRM_SUCCESS;
+}
+
+int brm_precise(const int *arpt, const int *acol, const double *aval, const int *brpt,
+                const int *bcol, const double *bval, int **crpt, int **ccol, double **cval,
+                int M, int K, int N, int *cnnz, brm_precise_timing *timing)
+{
+    return host_call<double>(false, arpt, acol, aval, brpt, bcol, bval, crpt, ccol, cval, M, K, N,
+                             cnnz, timing, nullptr);
+}
+
+int brm_upper(const int *arpt, const int *acol, const double *aval, const int *brpt,
+              const int *bcol, const double *bval, int **crpt, int **ccol, double **cval, int M,
+              int K, int N, int *cnnz, brm_upper_timing *timing)
+{
+    return host_call<double>(true, arpt, acol, aval, brpt, bcol, bval, crpt, ccol, cval, M, K, N,
+                             cnnz, nullptr, timing);
+}
+
+int brm_precise_f32(const int *arpt, const int *acol, const float *aval, const int *brpt,
+                    const int *bcol, const float *bval, int **crpt, int **ccol, float **cval,
+                    int M, int K, int N, int *cnnz, brm_precise_timing *timing)
+{
+    return host_call<float>(false, arpt, acol, aval, brpt, bcol, bval, crpt, ccol, cval, M, K, N,
+                            cnnz, timing, nullptr);
+}
+
+int brm_upper_f32(const int *arpt, const int *acol, const float *aval, const int *brpt,
+                  const int *bcol, const float *bval, int **crpt, int **ccol, float **cval,
+                  int M, int K, int N, int *cnnz, brm_upper_timing *timing)
+{
+    return host_call<float>(true, arpt, acol, aval, brpt, bcol, bval, crpt, ccol, cval, M, K, N,
+                            cnnz, nullptr, timing);
+}
+
+void brm_free(void *p) { std::free(p); }
+
+int brm_compute_flop(brm_context ctx, const brm_csr *A, const brm_csr *B, long long *products)
+{
+    if (!ctx || !products)
+        return BRM_ERR_INVALID_VALUE;
+    BRM_TRY(check_pair(A, B));
+    BRM_TRY(ensure_workspace(ctx, A->M));
+    brm::PlanDev P = ctx->plan;
+    P.M = A->M;
+    ctx->planned = false;
+    BRM_CK(cudaMemsetAsync(P.cnt, 0, sizeof(brm::Counters), ctx->stream));
+    brm::launch_analyze(to_dev(A), to_dev(B), P, ctx->stream);
+    BRM_CK(cudaGetLastError());
+    BRM_CK(cudaMemcpyAsync(ctx->h_cnt, P.cnt, sizeof(brm::Counters), cudaMemcpyDeviceToHost,
+                           ctx->stream));
+    BRM_CK(cudaStreamSynchronize(ctx->stream));
+    ctx->last_err = ctx->h_cnt->err;
+    BRM_TRY(device_err_status(ctx->h_cnt->err));
+    *products = (long long)ctx->h_cnt->total_flop;
+    return BRM_SUCCESS;
+}
+
+int brm_upper_bound(brm_context ctx, brm_dtype dtype, const brm_csr *A, const brm_csr *B,
+                    long long *products, long long *bytes)
+{
+    if (!bytes)
+        return BRM_ERR_INVALID_VALUE;
+    BRM_TRY(check_dtype(dtype));
+    long long f = 0;
+    BRM_TRY(brm_compute_flop(ctx, A, B, &f));
+    if (products)
+        *products = f;
+    const long long s = (long long)vsize(dtype);
+    *bytes = 2 * f * (4 + s) + 4LL * ((long long)A->M + 1) + (long long)workspace_bytes(A->M);
+    return BRM_SUCCESS;
+}
+
+int brm_validate(brm_context ctx, const brm_csr *X, int ncols, int *bad_row)
+{
+    if (!ctx || !X || !bad_row || X->M < 0 || ncols < 0 || !X->rpt)
+        return BRM_ERR_INVALID_VALUE;
+    if (X->nnz > 0 && !X->col)
+        return BRM_ERR_INVALID_VALUE;
+    if (X->M == 0) {
+        *bad_row = -1;
+        return BRM_SUCCESS;
+    }
+    return validate_one(ctx, X, ncols, bad_row);
+}
+
+}  // extern "C"

@@ -1,0 +1,196 @@
+// brm_common.cuh -- shared device helpers for the BRMerge SpGEMM kernels.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace brm {
+
+constexpr int kWarp = 32;
+constexpr unsigned kFull = 0xffffffffu;
+
+// Value arithmetic with explicit IEEE round-to-nearest and no contraction:
+// the merge order fixes every rounding, so products and sums stay separate.
+__device__ __forceinline__ double vmul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float vmul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double vadd(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ float vadd(float a, float b) { return __fadd_rn(a, b); }
+
+__device__ __forceinline__ unsigned lanemask_lt()
+{
+    unsigned m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
+
+template <typename T>
+__device__ __forceinline__ T warp_incl_scan(T v)
+{
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        T n = __shfl_up_sync(kFull, v, o);
+        if (lane >= o)
+            v += n;
+    }
+    return v;
+}
+
+template <typename T>
+__device__ __forceinline__ T warp_sum(T v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+        v += __shfl_xor_sync(kFull, v, o);
+    return v;
+}
+
+template <typename T>
+__device__ __forceinline__ T warp_max(T v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        T n = __shfl_xor_sync(kFull, v, o);
+        v = n > v ? n : v;
+    }
+    return v;
+}
+
+template <typename T>
+__device__ __forceinline__ T warp_min(T v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        T n = __shfl_xor_sync(kFull, v, o);
+        v = n < v ? n : v;
+    }
+    return v;
+}
+
+// Block-wide exclusive scan of one value per thread.  `ws` is shared
+// scratch of NT/32+1 entries.  Returns the exclusive prefix; *total gets
+// the block sum.  Contains three __syncthreads().
+template <int NT, typename T>
+__device__ __forceinline__ T block_excl_scan(T v, T *ws, T *total)
+{
+    constexpr int NW = NT / 32;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    T inc = warp_incl_scan(v);
+    __syncthreads();  // ws may still be read by a previous block-wide call
+    if (lane == 31)
+        ws[w] = inc;
+    __syncthreads();
+    if (w == 0) {
+        T s = lane < NW ? ws[lane] : T(0);
+        T si = warp_incl_scan(s);
+        if (lane < NW)
+            ws[lane] = si - s;
+        if (lane == NW - 1)
+            ws[NW] = si;
+    }
+    __syncthreads();
+    T r = ws[w] + inc - v;
+    *total = ws[NW];
+    return r;
+}
+
+template <int NT, typename T>
+__device__ __forceinline__ T block_sum(T v, T *ws)
+{
+    constexpr int NW = NT / 32;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    T s = warp_sum(v);
+    __syncthreads();
+    if (lane == 0)
+        ws[w] = s;
+    __syncthreads();
+    T t = T(0);
+    for (int i = 0; i < NW; i++)
+        t += ws[i];
+    return t;
+}
+
+template <int NT, typename T>
+__device__ __forceinline__ T block_max(T v, T *ws)
+{
+    constexpr int NW = NT / 32;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    T s = warp_max(v);
+    __syncthreads();
+    if (lane == 0)
+        ws[w] = s;
+    __syncthreads();
+    T t = ws[0];
+    for (int i = 1; i < NW; i++)
+        t = ws[i] > t ? ws[i] : t;
+    return t;
+}
+
+template <int NT, typename T>
+__device__ __forceinline__ T block_min(T v, T *ws)
+{
+    constexpr int NW = NT / 32;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    T s = warp_min(v);
+    __syncthreads();
+    if (lane == 0)
+        ws[w] = s;
+    __syncthreads();
+    T t = ws[0];
+    for (int i = 1; i < NW; i++)
+        t = ws[i] < t ? ws[i] : t;
+    return t;
+}
+
+// Split level of two distinct leaves of the binary merge tree: the tree
+// level (0-based) at which leaves a and b are combined minus one, i.e. the
+// index of the highest differing bit.
+__device__ __forceinline__ int split_level(int a, int b) { return 31 - __clz(a ^ b); }
+
+// Order-exact reduction of one column's contributions.
+//
+// The reference merges the k lists of a row pairwise, adjacent pairs first
+// (BRMerge-SpGEMM/inc/spgemm.h:639-707): list l of level L+1 is the merge of
+// lists 2l and 2l+1 of level L, an odd last list passes through, and equal
+// columns are added as left + right (:651-653).  For one column that is a
+// binary trie over the leaf index l: siblings combine as left + right and a
+// node with one present child passes that child's value through unchanged.
+// ShiftReduce evaluates that trie for leaves presented in increasing order:
+// consecutive leaves a < b are joined at split_level(a, b), and a lower split
+// binds tighter (operator-precedence parsing).  The stack holds at most one
+// entry per tree level.
+template <typename T, int DEPTH = 33>
+struct ShiftReduce {
+    T val[DEPTH];
+    int op[DEPTH];  // op[i] = split level between entries i and i+1
+    int n;
+    int last;
+    __device__ __forceinline__ void init(int leaf, T v)
+    {
+        val[0] = v;
+        n = 1;
+        last = leaf;
+    }
+    __device__ __forceinline__ void push(int leaf, T v)
+    {
+        int s = split_level(last, leaf);
+        while (n >= 2 && op[n - 2] < s) {
+            val[n - 2] = vadd(val[n - 2], val[n - 1]);
+            n--;
+        }
+        op[n - 1] = s;
+        val[n] = v;
+        n++;
+        last = leaf;
+    }
+    __device__ __forceinline__ T finish()
+    {
+        while (n >= 2) {
+            val[n - 2] = vadd(val[n - 2], val[n - 1]);
+            n--;
+        }
+        return val[0];
+    }
+};
+
+}  // namespace brm

@@ -1,0 +1,51 @@
+// brm_kernels.h -- host-side launchers of the BRMerge kernels (one GPU, one stream).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "brm_plan.h"
+
+namespace brm {
+
+// Row analysis: products per row, row bins and lists, total products
+// (replaces compute_flop and the static load balance, spgemm.h:31-56, :496-503).
+void launch_analyze(const CsrDev &A, const CsrDev &B, const PlanDev &P, cudaStream_t s);
+
+// Exclusive scans with out[n] = total.  The int32 form ORs kErrOverflow into
+// cnt->err and stores the int64 total in cnt->cnnz (spgemm.h:564-578).
+void launch_scan_i32(const int *in, int *out, int n, Counters *cnt, void *tmp, cudaStream_t s);
+void launch_scan_i64(const int *in, long long *out, int n, void *tmp, cudaStream_t s);
+size_t scan_tmp_bytes(int n);
+
+// Symbolic phase: exact nnz per row (spgemm.h:505-562).  `only_heavy`
+// restricts the row CTA pass to rows above kCap products (the Upper path uses
+// it only to route rows to the spill path).
+void launch_symbolic(const CsrDev &A, const CsrDev &B, const PlanDev &P, int num_sms,
+                     bool only_heavy, cudaStream_t s);
+
+// Numeric phase (spgemm.h:580-721).  Precise: rows are written at crpt[row].
+// Upper: rows are written at scan_flop[row] into (bar_col, bar_val) and their
+// lengths into P.nnz (spgemm.h:266-410).
+void launch_numeric(int dtype, bool upper, const CsrDev &A, const CsrDev &B, const PlanDev &P,
+                    const int *crpt, int *ccol, void *cval, void *spill_scratch,
+                    unsigned long long spill_bytes, int num_sms, cudaStream_t s);
+
+// Upper compaction: C[crpt[i]..] = C_bar[scan_flop[i]..] (spgemm.h:429-444).
+void launch_compact(int dtype, const PlanDev &P, const int *bar_col, const void *bar_val,
+                    const int *crpt, int *ccol, void *cval, cudaStream_t s);
+
+// Input validation: row pointers monotone and in range, columns in range and
+// strictly increasing per row (the invariants CSR.cpp:454-477 enforces on
+// read).  Writes the first offending row (or -1) to *bad_row (device int).
+void launch_validate(const CsrDev &X, int ncols, int *bad_row, cudaStream_t s);
+
+}  // namespace brm
+
+namespace brm {
+void launch_numeric_f64(bool upper, const CsrDev &A, const CsrDev &B, const PlanDev &P,
+                        const int *crpt, int *ccol, void *cval, void *spill_scratch,
+                        unsigned long long spill_bytes, int num_sms, cudaStream_t s);
+void launch_numeric_f32(bool upper, const CsrDev &A, const CsrDev &B, const PlanDev &P,
+                        const int *crpt, int *ccol, void *cval, void *spill_scratch,
+                        unsigned long long spill_bytes, int num_sms, cudaStream_t s);
+}  // namespace brm

@@ -1,0 +1,35 @@
+// brm_numeric_f32.cu -- numeric phase launchers for float values.
+#include "brm_kernels.h"
+#include "brm_rows.cuh"
+
+namespace brm {
+
+template <bool UPPER>
+static void numeric_f32(const CsrDev &A, const CsrDev &B, const PlanDev &P, const int *crpt,
+                       int *ccol, float *cval, void *spill_scratch, unsigned long long spill_bytes,
+                       int num_sms, cudaStream_t s)
+{
+    k_copy_numeric<float, UPPER><<<num_sms * 8, 256, 0, s>>>(A, B, P, crpt, ccol, cval);
+    k_warp_numeric<float, UPPER><<<num_sms * 8, 256, 0, s>>>(A, B, P, crpt, ccol, cval);
+    const size_t smem = NumLayout<float>::bytes;
+    cudaFuncSetAttribute(k_rows_numeric<float, UPPER>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)smem);
+    k_rows_numeric<float, UPPER><<<num_sms, kRowThreads, smem, s>>>(A, B, P, crpt, ccol, cval);
+    if (spill_bytes)
+        k_spill_numeric<float, UPPER><<<num_sms * 4, 32, 0, s>>>(
+            A, B, P, crpt, ccol, cval, (unsigned char *)spill_scratch, spill_bytes);
+}
+
+void launch_numeric_f32(bool upper, const CsrDev &A, const CsrDev &B, const PlanDev &P,
+                       const int *crpt, int *ccol, void *cval, void *spill_scratch,
+                       unsigned long long spill_bytes, int num_sms, cudaStream_t s)
+{
+    if (A.M <= 0)
+        return;
+    if (upper)
+        numeric_f32<true>(A, B, P, crpt, ccol, (float *)cval, spill_scratch, spill_bytes, num_sms, s);
+    else
+        numeric_f32<false>(A, B, P, crpt, ccol, (float *)cval, spill_scratch, spill_bytes, num_sms, s);
+}
+
+}  // namespace brm

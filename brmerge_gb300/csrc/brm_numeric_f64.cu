@@ -1,0 +1,35 @@
+// brm_numeric_f64.cu -- numeric phase launchers for double values.
+#include "brm_kernels.h"
+#include "brm_rows.cuh"
+
+namespace brm {
+
+template <bool UPPER>
+static void numeric_f64(const CsrDev &A, const CsrDev &B, const PlanDev &P, const int *crpt,
+                       int *ccol, double *cval, void *spill_scratch, unsigned long long spill_bytes,
+                       int num_sms, cudaStream_t s)
+{
+    k_copy_numeric<double, UPPER><<<num_sms * 8, 256, 0, s>>>(A, B, P, crpt, ccol, cval);
+    k_warp_numeric<double, UPPER><<<num_sms * 8, 256, 0, s>>>(A, B, P, crpt, ccol, cval);
+    const size_t smem = NumLayout<double>::bytes;
+    cudaFuncSetAttribute(k_rows_numeric<double, UPPER>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)smem);
+    k_rows_numeric<double, UPPER><<<num_sms, kRowThreads, smem, s>>>(A, B, P, crpt, ccol, cval);
+    if (spill_bytes)
+        k_spill_numeric<double, UPPER><<<num_sms * 4, 32, 0, s>>>(
+            A, B, P, crpt, ccol, cval, (unsigned char *)spill_scratch, spill_bytes);
+}
+
+void launch_numeric_f64(bool upper, const CsrDev &A, const CsrDev &B, const PlanDev &P,
+                       const int *crpt, int *ccol, void *cval, void *spill_scratch,
+                       unsigned long long spill_bytes, int num_sms, cudaStream_t s)
+{
+    if (A.M <= 0)
+        return;
+    if (upper)
+        numeric_f64<true>(A, B, P, crpt, ccol, (double *)cval, spill_scratch, spill_bytes, num_sms, s);
+    else
+        numeric_f64<false>(A, B, P, crpt, ccol, (double *)cval, spill_scratch, spill_bytes, num_sms, s);
+}
+
+}  // namespace brm

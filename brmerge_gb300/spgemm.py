@@ -1,0 +1,310 @@
+"""BRMerge SpGEMM entry points, mirroring the reference's interface.
+
+Host forms (reference signatures, BRMerge-SpGEMM/inc/spgemm.h:460-464,
+:737-741): ``brmerge_precise(A, B, C, timing)`` and ``brmerge_upper(A, B, C,
+timing)`` take host CSR matrices and fill C.  They call the C ABI's host
+drop-ins (brm_precise / brm_upper), which run every phase on the GPU.
+
+Device forms: ``Context`` wraps a brm_context and works on ``DeviceCSR``
+matrices whose arrays are torch CUDA tensors (torch is used only for device
+memory and streams).
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, fields
+
+import numpy as np
+
+from . import _native
+from .csr import CSR
+
+F64, F32 = 0, 1
+
+
+def _dtype_code(val_dtype) -> int:
+    dt = np.dtype(val_dtype)
+    if dt == np.float64:
+        return F64
+    if dt == np.float32:
+        return F32
+    raise TypeError(f"unsupported value type {dt}; use float64 or float32")
+
+
+class _Timing:
+    _c = None
+
+    def __init__(self):
+        for f in self._names():
+            setattr(self, f, 0.0)
+
+    @classmethod
+    def _names(cls):
+        return [n for n, _ in cls._c._fields_]
+
+    def _load(self, c):
+        for n in self._names():
+            setattr(self, n, float(getattr(c, n)))
+
+    def __iadd__(self, other):
+        for n in self._names():
+            setattr(self, n, getattr(self, n) + getattr(other, n))
+        return self
+
+    def __itruediv__(self, k: float):
+        for n in self._names():
+            setattr(self, n, getattr(self, n) / k)
+        return self
+
+    def as_dict(self):
+        return {n: getattr(self, n) for n in self._names()}
+
+    def reg_print(self, total_flop: float) -> str:
+        """GFLOPS line as the reference's reg_print (Timings.cpp:162-165)."""
+        return f"{total_flop / self.total / 1e9 if self.total else 0.0:f}"
+
+
+class PreciseTiming(_Timing):
+    """Phase times in seconds (Precise_Timing, Timings.h:26-46)."""
+    _c = _native.PreciseTimingC
+
+
+class UpperTiming(_Timing):
+    """Phase times in seconds (Upper_Timing, Timings.h:4-24)."""
+    _c = _native.UpperTimingC
+
+
+def _ptr(a: np.ndarray):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+def _host_call(name_f64: str, name_f32: str, A: CSR, B: CSR, C_out: CSR | None, timing, tcls):
+    if A.N != B.M:
+        raise ValueError(f"A.N ({A.N}) != B.M ({B.M})")
+    code = _dtype_code(A.val.dtype)
+    if _dtype_code(B.val.dtype) != code:
+        raise TypeError("A and B must have the same value type")
+    L = _native.lib()
+    fn = getattr(L, name_f64 if code == F64 else name_f32)
+    vt = C.c_double if code == F64 else C.c_float
+    arrs = [np.ascontiguousarray(x) for x in (A.rpt, A.col, A.val, B.rpt, B.col, B.val)]
+    for a, dt in zip(arrs, (np.int32, np.int32, None, np.int32, np.int32, None)):
+        if dt is not None and a.dtype != dt:
+            raise TypeError("row pointers and columns must be int32")
+    crpt = _native.c_int_p()
+    ccol = _native.c_int_p()
+    cval = C.POINTER(vt)()
+    cnnz = C.c_int(0)
+    tc = tcls._c()
+    st = fn(*[_ptr(a) for a in arrs], C.byref(crpt), C.byref(ccol), C.byref(cval),
+            A.M, A.N, B.N, C.byref(cnnz), C.byref(tc))
+    _native.check(st, name_f64)
+    try:
+        n = cnnz.value
+        rpt = np.ctypeslib.as_array(crpt, shape=(A.M + 1,)).copy()
+        col = np.ctypeslib.as_array(ccol, shape=(n,)).copy() if n else np.zeros(0, np.int32)
+        val = (np.ctypeslib.as_array(cval, shape=(n,)).copy() if n
+               else np.zeros(0, np.float64 if code == F64 else np.float32))
+    finally:
+        L.brm_free(C.cast(crpt, C.c_void_p))
+        L.brm_free(C.cast(ccol, C.c_void_p))
+        L.brm_free(C.cast(cval, C.c_void_p))
+    if timing is not None:
+        timing._load(tc)
+    out = C_out if C_out is not None else CSR(0, 0, np.zeros(1, np.int32), np.zeros(0, np.int32),
+                                              np.zeros(0))
+    out.M, out.N, out.rpt, out.col, out.val = A.M, B.N, rpt, col, val
+    return out
+
+
+def brmerge_precise(A: CSR, B: CSR, C_out: CSR | None = None,
+                    timing: PreciseTiming | None = None) -> CSR:
+    """C = A*B by BRMerge-Precise (spgemm.h:737-741) on the GPU."""
+    return _host_call("brm_precise", "brm_precise_f32", A, B, C_out, timing, PreciseTiming)
+
+
+def brmerge_upper(A: CSR, B: CSR, C_out: CSR | None = None,
+                  timing: UpperTiming | None = None) -> CSR:
+    """C = A*B by BRMerge-Upper (spgemm.h:460-464) on the GPU."""
+    return _host_call("brm_upper", "brm_upper_f32", A, B, C_out, timing, UpperTiming)
+
+
+# ---------------------------------------------------------------------------
+# device-resident form
+# ---------------------------------------------------------------------------
+
+@dataclass
+class DeviceCSR:
+    """CSR on the GPU: rpt/col int32 and val float64/float32 torch CUDA tensors."""
+    M: int
+    N: int
+    rpt: object
+    col: object
+    val: object
+
+    @property
+    def nnz(self) -> int:
+        return int(self.col.numel())
+
+    @staticmethod
+    def from_host(X: CSR, device="cuda", non_blocking=False) -> "DeviceCSR":
+        import torch
+        t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(device, non_blocking=non_blocking)
+        return DeviceCSR(X.M, X.N, t(X.rpt), t(X.col), t(X.val))
+
+    def to_host(self) -> CSR:
+        return CSR(self.M, self.N, self.rpt.cpu().numpy(), self.col.cpu().numpy(),
+                   self.val.cpu().numpy())
+
+    def c(self) -> _native.CsrC:
+        return _native.CsrC(self.M, self.N, self.nnz, self.rpt.data_ptr(),
+                            self.col.data_ptr() if self.col.numel() else None,
+                            self.val.data_ptr() if self.val.numel() else None)
+
+
+class Context:
+    """A brm_context bound to the current CUDA device and a stream."""
+
+    def __init__(self, stream=None, validate: bool = False):
+        self._L = _native.lib()
+        self._h = C.c_void_p()
+        _native.check(self._L.brm_create(C.byref(self._h)), "brm_create")
+        self.set_stream(stream)
+        self.set_validate(validate)
+
+    def close(self):
+        if self._h:
+            self._L.brm_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_stream(self, stream=None):
+        ptr = None
+        if stream is not None:
+            ptr = stream.cuda_stream if hasattr(stream, "cuda_stream") else int(stream)
+        _native.check(self._L.brm_set_stream(self._h, ptr), "brm_set_stream")
+
+    def set_validate(self, on: bool):
+        _native.check(self._L.brm_set_validate(self._h, 1 if on else 0), "brm_set_validate")
+
+    @property
+    def last_device_error(self) -> int:
+        return self._L.brm_last_device_error(self._h)
+
+    def symbolic(self, A: DeviceCSR, B: DeviceCSR):
+        """Returns (crpt tensor [M+1], nnz(C))."""
+        import torch
+        crpt = torch.empty(A.M + 1, dtype=torch.int32, device=A.rpt.device)
+        cnnz = C.c_int(0)
+        a, b = A.c(), B.c()
+        _native.check(self._L.brm_symbolic(self._h, C.byref(a), C.byref(b), crpt.data_ptr(),
+                                           C.byref(cnnz)), "brm_symbolic")
+        return crpt, cnnz.value
+
+    def numeric(self, A: DeviceCSR, B: DeviceCSR, crpt, cnnz: int, out=None) -> DeviceCSR:
+        import torch
+        code = _dtype_code(np.float64 if A.val.dtype == torch.float64 else np.float32)
+        if out is None:
+            ccol = torch.empty(max(cnnz, 0), dtype=torch.int32, device=A.rpt.device)
+            cval = torch.empty(max(cnnz, 0), dtype=A.val.dtype, device=A.rpt.device)
+        else:
+            ccol, cval = out
+        a, b = A.c(), B.c()
+        _native.check(self._L.brm_numeric(self._h, code, C.byref(a), C.byref(b), crpt.data_ptr(),
+                                          ccol.data_ptr() if cnnz else None,
+                                          cval.data_ptr() if cnnz else None), "brm_numeric")
+        return DeviceCSR(A.M, B.N, crpt, ccol[:cnnz], cval[:cnnz])
+
+    def precise(self, A: DeviceCSR, B: DeviceCSR) -> DeviceCSR:
+        crpt, cnnz = self.symbolic(A, B)
+        return self.numeric(A, B, crpt, cnnz)
+
+    def _device_call(self, upper: bool, A: DeviceCSR, B: DeviceCSR, timing=None) -> DeviceCSR:
+        import torch
+        code = _dtype_code(np.float64 if A.val.dtype == torch.float64 else np.float32)
+        pr, pc, pv = C.c_void_p(), C.c_void_p(), C.c_void_p()
+        cnnz = C.c_int(0)
+        a, b = A.c(), B.c()
+        tcls = UpperTiming if upper else PreciseTiming
+        tc = tcls._c()
+        fn = self._L.brm_upper_device if upper else self._L.brm_precise_device
+        _native.check(fn(self._h, code, C.byref(a), C.byref(b), C.byref(pr), C.byref(pc),
+                         C.byref(pv), C.byref(cnnz), C.byref(tc)),
+                      "brm_upper_device" if upper else "brm_precise_device")
+        try:
+            n = cnnz.value
+            dev = A.rpt.device
+            crpt = torch.empty(A.M + 1, dtype=torch.int32, device=dev)
+            ccol = torch.empty(n, dtype=torch.int32, device=dev)
+            cval = torch.empty(n, dtype=A.val.dtype, device=dev)
+            torch.cuda.synchronize(dev)
+            _cuda_copy(crpt, pr.value, crpt.numel() * 4)
+            if n:
+                _cuda_copy(ccol, pc.value, n * 4)
+                _cuda_copy(cval, pv.value, n * cval.element_size())
+        finally:
+            for p in (pr, pc, pv):
+                self._L.brm_device_free(self._h, p)
+            torch.cuda.synchronize(A.rpt.device)
+        if timing is not None:
+            timing._load(tc)
+        return DeviceCSR(A.M, B.N, crpt, ccol, cval)
+
+    def precise_device(self, A: DeviceCSR, B: DeviceCSR, timing=None) -> DeviceCSR:
+        """brm_precise_device (callee-allocated outputs), copied into torch tensors."""
+        return self._device_call(False, A, B, timing)
+
+    def upper(self, A: DeviceCSR, B: DeviceCSR, timing=None) -> DeviceCSR:
+        """brm_upper_device, copied into torch tensors."""
+        return self._device_call(True, A, B, timing)
+
+    def compute_flop(self, A: DeviceCSR, B: DeviceCSR) -> int:
+        out = C.c_longlong(0)
+        a, b = A.c(), B.c()
+        _native.check(self._L.brm_compute_flop(self._h, C.byref(a), C.byref(b), C.byref(out)),
+                      "brm_compute_flop")
+        return out.value
+
+    def upper_bound(self, A: DeviceCSR, B: DeviceCSR, dtype=np.float64):
+        prod, nbytes = C.c_longlong(0), C.c_longlong(0)
+        a, b = A.c(), B.c()
+        _native.check(self._L.brm_upper_bound(self._h, _dtype_code(dtype), C.byref(a), C.byref(b),
+                                              C.byref(prod), C.byref(nbytes)), "brm_upper_bound")
+        return prod.value, nbytes.value
+
+    def validate(self, X: DeviceCSR, ncols: int | None = None) -> int:
+        """-1 if X is valid CSR, else the first offending row."""
+        bad = C.c_int(-1)
+        x = X.c()
+        st = self._L.brm_validate(self._h, C.byref(x), X.N if ncols is None else ncols,
+                                  C.byref(bad))
+        if st not in (0, 2):
+            _native.check(st, "brm_validate")
+        return bad.value
+
+
+class _RawDevice:
+    """A raw device allocation exposed through __cuda_array_interface__."""
+
+    def __init__(self, ptr: int, n: int, typestr: str):
+        self.__cuda_array_interface__ = {
+            "shape": (n,), "typestr": typestr, "data": (ptr, False), "version": 2, "strides": None}
+
+
+def _cuda_copy(dst_tensor, src_ptr: int, nbytes: int) -> None:
+    import torch
+    n = dst_tensor.numel()
+    typestr = {torch.int32: "<i4", torch.float64: "<f8", torch.float32: "<f4"}[dst_tensor.dtype]
+    src = torch.as_tensor(_RawDevice(src_ptr, n, typestr), device=dst_tensor.device)
+    dst_tensor.copy_(src)
+
+
+def compute_flop_host(A: CSR, B: CSR) -> int:
+    """Intermediate products of A*B from host arrays (numpy; no GPU needed)."""
+    blen = np.diff(B.rpt.astype(np.int64))
+    return int(blen[A.col].sum()) if A.nnz else 0

@@ -1,0 +1,178 @@
+/*
+ * brmerge.h -- C ABI of the GB300 BRMerge SpGEMM library (libbrmerge.so).
+ *
+ * C = A * B for CSR matrices with int32 indices and double (or float) values,
+ * computed on one NVIDIA GB300 GPU by hand-written sm_103a kernels.  The
+ * result is identical to the reference's BRMerge-Precise: row pointers and
+ * column indices bit-exact, and double values bit-exact because the kernels
+ * add the partial products of every output entry in the reference's binary
+ * merge-tree order (BRMerge-SpGEMM/inc/spgemm.h:639-707).
+ *
+ * Inputs must be valid CSR as the reference's reader guarantees
+ * (BRMerge-SpGEMM/src/CSR.cpp:454-477): rpt[0] == 0, rpt non-decreasing,
+ * columns in range and strictly increasing within each row.  The host
+ * drop-ins validate their inputs on the GPU by default; the device-pointer
+ * calls validate when brm_set_validate(ctx, 1) is set.
+ *
+ * Every function returns a brm_status (0 on success) instead of the
+ * reference's assert/throw.  A context binds to the device that is current
+ * when it is created and serialises its work on one CUDA stream; separate
+ * contexts may run concurrently on separate streams.
+ */
+#ifndef BRMERGE_H
+#define BRMERGE_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define BRM_VERSION_MAJOR 0
+#define BRM_VERSION_MINOR 1
+
+typedef enum brm_status {
+    BRM_SUCCESS = 0,
+    BRM_ERR_INVALID_VALUE = 1, /* bad argument: null pointer, negative size, A.N != B.M, dtype */
+    BRM_ERR_INVALID_CSR = 2,   /* an input violates the CSR invariants */
+    BRM_ERR_ALLOC = 3,         /* device or host allocation failed */
+    BRM_ERR_CUDA = 4,          /* a CUDA runtime call failed */
+    BRM_ERR_OVERFLOW = 5,      /* nnz(C) does not fit int32 */
+    BRM_ERR_NOT_PLANNED = 6,   /* brm_numeric without a matching brm_symbolic */
+    BRM_ERR_INTERNAL = 7,      /* a device-side invariant failed */
+    BRM_ERR_TIMEOUT = 8,       /* a bounded device wait expired */
+    BRM_ERR_NO_DEVICE = 9,     /* no CUDA device */
+    BRM_ERR_CAPACITY = 10      /* request larger than a fixed capacity */
+} brm_status;
+
+typedef enum brm_dtype { BRM_F64 = 0, BRM_F32 = 1 } brm_dtype;
+
+/* Phase times in seconds; the fields mirror Precise_Timing
+ * (BRMerge-SpGEMM/inc/Timings.h:26-46).  GPU phases are timed with CUDA
+ * events: compute_flop = row analysis and binning, load_balance = 0 (binning
+ * replaces it), symbolic, prefix_sum_nnz = crpt scan, compute = numeric. */
+typedef struct brm_precise_timing {
+    double pre_allocate;
+    double compute_flop;
+    double prefix_sum_flop;
+    double load_balance;
+    double symbolic;
+    double prefix_sum_nnz;
+    double allocate_C;
+    double compute;
+    double cleanup;
+    double total;
+} brm_precise_timing;
+
+/* Mirrors Upper_Timing (BRMerge-SpGEMM/inc/Timings.h:4-24). */
+typedef struct brm_upper_timing {
+    double thread;
+    double pre_allocate;
+    double compute_flop;
+    double prefix_sum_flop;
+    double load_balance;
+    double allocate_hook;
+    double compute;
+    double prefix_sum_nnz;
+    double allocate_C;
+    double copy;
+    double cleanup;
+    double total;
+} brm_upper_timing;
+
+/* A CSR matrix in device memory (borrowed, read-only).  Mirrors the fields
+ * of the reference's CSR class (BRMerge-SpGEMM/inc/CSR.h:7-28); val points
+ * to double or float according to the call's dtype. */
+typedef struct brm_csr {
+    int M;
+    int N;
+    int nnz;
+    const int *rpt;
+    const int *col;
+    const void *val;
+} brm_csr;
+
+typedef struct brm_context_s *brm_context;
+
+/* ---- context ------------------------------------------------------------ */
+int brm_create(brm_context *ctx);
+int brm_destroy(brm_context ctx);
+/* cudaStream_t passed as void*; NULL selects the legacy default stream. */
+int brm_set_stream(brm_context ctx, void *stream);
+int brm_set_validate(brm_context ctx, int on);
+/* Device-side error bits of the last call on this context (diagnostics). */
+int brm_last_device_error(brm_context ctx);
+const char *brm_status_string(int status);
+
+/* ---- symbolic / numeric split (device pointers) -------------------------- */
+
+/* Symbolic phase: products per row, row binning, exact nnz per C row and
+ * crpt (caller-allocated, M+1 ints, device).  *cnnz (host) receives nnz(C);
+ * the call synchronises the context stream to return it.  The plan is kept
+ * in the context for the next brm_numeric on the same A and B.
+ * Replaces spgemm.h:476-578 (compute_flop .. allocate C). */
+int brm_symbolic(brm_context ctx, const brm_csr *A, const brm_csr *B, int *crpt, int *cnnz);
+
+/* Numeric phase: fills ccol/cval (caller-allocated, cnnz entries, device)
+ * in merge-tree order.  Replaces spgemm.h:580-721. */
+int brm_numeric(brm_context ctx, brm_dtype dtype, const brm_csr *A, const brm_csr *B,
+                const int *crpt, int *ccol, void *cval);
+
+/* ---- one-call forms (device pointers, callee-allocated outputs) ----------- */
+
+/* BRMerge-Precise: symbolic then numeric.  Outputs are allocated from the
+ * context's stream-ordered pool; release them with brm_device_free.
+ * Mirrors brmerge_precise (spgemm.h:468-471).  timing may be NULL. */
+int brm_precise_device(brm_context ctx, brm_dtype dtype, const brm_csr *A, const brm_csr *B,
+                       int **crpt, int **ccol, void **cval, int *cnnz,
+                       brm_precise_timing *timing);
+
+/* BRMerge-Upper: merge into an upper-bound buffer at the row-product
+ * offsets, scan the real row sizes, compact.  Mirrors brmerge_upper
+ * (spgemm.h:220-223); output identical to brm_precise_device. */
+int brm_upper_device(brm_context ctx, brm_dtype dtype, const brm_csr *A, const brm_csr *B,
+                     int **crpt, int **ccol, void **cval, int *cnnz, brm_upper_timing *timing);
+
+int brm_device_free(brm_context ctx, void *p);
+
+/* ---- host drop-ins: the reference's argument order ------------------------ */
+
+/* brmerge_precise with host arrays (spgemm.h:468-471): A is M x K, B is
+ * K x N.  *crpt (M+1), *ccol and *cval (cnnz) are malloc'ed by the callee;
+ * release each with brm_free.  timing may be NULL.  Uses a process-wide
+ * context on the current device. */
+int brm_precise(const int *arpt, const int *acol, const double *aval, const int *brpt,
+                const int *bcol, const double *bval, int **crpt, int **ccol, double **cval,
+                int M, int K, int N, int *cnnz, brm_precise_timing *timing);
+int brm_upper(const int *arpt, const int *acol, const double *aval, const int *brpt,
+              const int *bcol, const double *bval, int **crpt, int **ccol, double **cval,
+              int M, int K, int N, int *cnnz, brm_upper_timing *timing);
+int brm_precise_f32(const int *arpt, const int *acol, const float *aval, const int *brpt,
+                    const int *bcol, const float *bval, int **crpt, int **ccol, float **cval,
+                    int M, int K, int N, int *cnnz, brm_precise_timing *timing);
+int brm_upper_f32(const int *arpt, const int *acol, const float *aval, const int *brpt,
+                  const int *bcol, const float *bval, int **crpt, int **ccol, float **cval,
+                  int M, int K, int N, int *cnnz, brm_upper_timing *timing);
+void brm_free(void *p);
+
+/* ---- helpers ---------------------------------------------------------------- */
+
+/* Intermediate products of A*B (compute_flop, spgemm.h:59-66); GFLOP/s in
+ * the reference is 2 * products / time. */
+int brm_compute_flop(brm_context ctx, const brm_csr *A, const brm_csr *B, long long *products);
+
+/* Admission estimate: products of A*B and the device bytes an Upper call
+ * needs at most (upper-bound C_bar plus C sized by the products). */
+int brm_upper_bound(brm_context ctx, brm_dtype dtype, const brm_csr *A, const brm_csr *B,
+                    long long *products, long long *bytes);
+
+/* Checks the CSR invariants of X on the device (columns must be < ncols).
+ * *bad_row = -1 if valid, else the first offending row.  Returns
+ * BRM_SUCCESS or BRM_ERR_INVALID_CSR. */
+int brm_validate(brm_context ctx, const brm_csr *X, int ncols, int *bad_row);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* BRMERGE_H */

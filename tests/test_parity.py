@@ -1,0 +1,298 @@
+"""GPU parity: the CUDA path against the oracle and the reference's golden output.
+
+Integer structure (row pointers, columns) must be bit-exact, and so must
+double values, because the kernels add partial products in the reference's
+merge-tree order.  float32 runs are bit-exact against the float32 oracle
+(same order, same rounding) and within 1e-5 relative of the float64 oracle.
+"""
+import numpy as np
+import pytest
+
+import brmerge_gb300 as brm
+from conftest import GOLDEN_NAMES, assert_same_csr, load_golden
+
+pytestmark = pytest.mark.gpu
+
+F32_RTOL = 1e-5
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    import torch  # noqa: F401
+    c = brm.Context()
+    yield c
+    c.close()
+
+
+def dev(X):
+    return brm.DeviceCSR.from_host(X)
+
+
+def gpu_precise(ctx, A, B):
+    return ctx.precise(dev(A), dev(B)).to_host()
+
+
+def gpu_upper(ctx, A, B):
+    return ctx.upper(dev(A), dev(B)).to_host()
+
+
+def assert_f32_close(C32, R64):
+    assert np.array_equal(C32.rpt, R64.rpt) and np.array_equal(C32.col, R64.col)
+    ref = np.asarray(R64.val, np.float64)
+    err = np.abs(np.asarray(C32.val, np.float64) - ref)
+    # |error| <= 1e-5 * max(1, |ref|): values are sums of products of U[-1,1] entries
+    assert np.all(err <= F32_RTOL * np.maximum(1.0, np.abs(ref))), float(err.max())
+
+
+# ---------------------------------------------------------------------------
+# golden fixtures (produced by the reference itself)
+# ---------------------------------------------------------------------------
+
+@pytest.mark.parametrize("name", GOLDEN_NAMES)
+def test_golden_host_precise(name):
+    A, B, C = load_golden(name)
+    assert_same_csr(brm.brmerge_precise(A, B), C, name)
+
+
+@pytest.mark.parametrize("name", GOLDEN_NAMES)
+def test_golden_host_upper(name):
+    A, B, C = load_golden(name)
+    assert_same_csr(brm.brmerge_upper(A, B), C, name)
+
+
+@pytest.mark.parametrize("name", GOLDEN_NAMES)
+def test_golden_device_split(ctx, name):
+    A, B, C = load_golden(name)
+    assert_same_csr(gpu_precise(ctx, A, B), C, name)
+    assert_same_csr(gpu_upper(ctx, A, B), C, name)
+
+
+# ---------------------------------------------------------------------------
+# seeded inputs against the oracle
+# ---------------------------------------------------------------------------
+
+def _cases():
+    yield "er2048", brm.gen_er(2048, 8, seed=3), None
+    yield "rmat12", brm.gen_rmat(12, int(2.35 * 4096), seed=4), None
+    yield "rmat14", brm.gen_rmat(14, int(2.35 * 16384), seed=5), None
+    yield "stencil10", brm.gen_stencil27(10, seed=6), None
+    yield "lognormal", brm.gen_lognormal(3000, 2500, seed=7), brm.gen_lognormal(2500, 4000, seed=8)
+    yield "uniform_dense", brm.gen_uniform(64, 400, 300, seed=9), brm.gen_uniform(400, 500, 200, seed=10)
+    yield "wide_span", brm.gen_uniform(50, 2000, 80, seed=11), brm.gen_uniform(2000, 1_500_000, 60, seed=12)
+
+
+CASES = list(_cases())
+
+
+@pytest.mark.parametrize("name,A,B", CASES, ids=[c[0] for c in CASES])
+def test_precise_matches_oracle(ctx, oracle_mod, name, A, B):
+    B = A if B is None else B
+    assert_same_csr(gpu_precise(ctx, A, B), oracle_mod.precise(A, B), name)
+
+
+@pytest.mark.parametrize("name,A,B", CASES, ids=[c[0] for c in CASES])
+def test_upper_matches_oracle(ctx, oracle_mod, name, A, B):
+    B = A if B is None else B
+    assert_same_csr(gpu_upper(ctx, A, B), oracle_mod.precise(A, B), name)
+
+
+@pytest.mark.parametrize("name,A,B", CASES[:5], ids=[c[0] for c in CASES[:5]])
+def test_f32(ctx, oracle_mod, name, A, B):
+    B = A if B is None else B
+    A32, B32 = A.astype(np.float32), B.astype(np.float32)
+    C32 = gpu_precise(ctx, A32, B32)
+    assert_same_csr(C32, oracle_mod.precise(A32, B32), name + " f32 order-exact")
+    assert_f32_close(C32, oracle_mod.precise(A, B))
+    assert_same_csr(gpu_upper(ctx, A32, B32), C32, name + " f32 upper")
+
+
+def test_host_drop_in_matches_device(ctx):
+    A = brm.gen_rmat(13, int(2.35 * 8192), seed=13)
+    t = brm.PreciseTiming()
+    C1 = brm.brmerge_precise(A, A, timing=t)
+    assert t.total > 0
+    assert_same_csr(C1, gpu_precise(ctx, A, A), "host vs device")
+
+
+# ---------------------------------------------------------------------------
+# edge cases
+# ---------------------------------------------------------------------------
+
+def _csr(rows, ncols, seed=0):
+    rng = np.random.default_rng(seed)
+    rpt = np.zeros(len(rows) + 1, np.int32)
+    for i, r in enumerate(rows):
+        rpt[i + 1] = rpt[i] + len(r)
+    col = np.array([c for r in rows for c in sorted(r)], np.int32)
+    return brm.CSR(len(rows), ncols, rpt, col, rng.uniform(-1, 1, len(col)))
+
+
+def test_empty_matrices(ctx, oracle_mod):
+    A = _csr([[], [], []], 4)
+    B = _csr([[0], [], [1, 2], []], 5)
+    for C in (brm.brmerge_precise(A, B), gpu_precise(ctx, A, B), gpu_upper(ctx, A, B)):
+        assert C.M == 3 and C.N == 5 and list(C.rpt) == [0, 0, 0, 0] and len(C.col) == 0
+    A2 = _csr([[0, 1], [1, 3]], 4)
+    B2 = _csr([[], [], [], []], 7)
+    C2 = gpu_precise(ctx, A2, B2)
+    assert list(C2.rpt) == [0, 0, 0]
+
+
+def test_single_and_pass_through_lists(ctx, oracle_mod):
+    # rows with exactly one nonempty list among many empty ones (copy rows),
+    # odd list counts, and exact cancellation kept as an explicit zero
+    Brows = [[], [0, 2, 4], [], [1, 2], [2], [], [0, 1, 2, 3, 4]]
+    B = _csr(Brows, 5, 1)
+    Arows = [[0, 1, 2], [1], [0, 2, 5], [1, 3, 4], [0, 1, 3, 4, 6], [3, 4], [6], []]
+    A = _csr(Arows, 7, 2)
+    B.val[B.rpt[3] + 1] = 0.25   # B(3,2)
+    B.val[B.rpt[4]] = 0.25       # B(4,2)
+    A.val[A.rpt[5]] = 1.0        # A(5,3)
+    A.val[A.rpt[5] + 1] = -1.0   # A(5,4)
+    R = oracle_mod.precise(A, B)
+    assert_same_csr(gpu_precise(ctx, A, B), R, "edge")
+    assert_same_csr(gpu_upper(ctx, A, B), R, "edge upper")
+    assert 0.0 in list(R.val)
+
+
+def test_signed_zero_pass_through(ctx, oracle_mod):
+    A = _csr([[0, 1]], 2)
+    B = _csr([[0], [1]], 2)
+    A.val[:] = [1.0, 1.0]
+    B.val[:] = [-0.0, 0.5]
+    C = gpu_precise(ctx, A, B)
+    assert np.signbit(C.val[0]) and C.val[0] == 0.0
+    assert_same_csr(C, oracle_mod.precise(A, B), "-0")
+
+
+def test_long_rows_many_windows(ctx, oracle_mod):
+    # a few very long rows: many lists, thousands of products per row, many
+    # shared columns (windows cut inside one chunk)
+    rng = np.random.default_rng(21)
+    K, N = 3000, 20000
+    Brows = [sorted(rng.choice(N, rng.integers(5, 120), replace=False)) for _ in range(K)]
+    Arows = [sorted(rng.choice(K, k, replace=False)) for k in (2500, 1800, 900, 64, 7)]
+    A, B = _csr(Arows, K, 3), _csr(Brows, N, 4)
+    R = oracle_mod.precise(A, B)
+    assert_same_csr(gpu_precise(ctx, A, B), R, "long rows")
+    assert_same_csr(gpu_upper(ctx, A, B), R, "long rows upper")
+
+
+def test_spill_many_lists(ctx, oracle_mod):
+    # an A row with more lists than the shared-memory list table holds
+    rng = np.random.default_rng(22)
+    K, N = 6000, 5000
+    Brows = [sorted(rng.choice(N, rng.integers(0, 6), replace=False)) for _ in range(K)]
+    Arows = [list(range(0, K, 1)), list(range(0, K, 3)), [5, 9]]
+    A, B = _csr(Arows, K, 5), _csr(Brows, N, 6)
+    R = oracle_mod.precise(A, B)
+    assert_same_csr(gpu_precise(ctx, A, B), R, "spill lists")
+    assert_same_csr(gpu_upper(ctx, A, B), R, "spill lists upper")
+
+
+def test_spill_dense_word(ctx, oracle_mod):
+    # more products inside one 32-column word than a window holds
+    K, N = 400, 64
+    Brows = [list(range(32)) for _ in range(K)]
+    Arows = [list(range(K)), list(range(0, K, 2)), [3]]
+    A, B = _csr(Arows, K, 7), _csr(Brows, N, 8)
+    R = oracle_mod.precise(A, B)
+    assert_same_csr(gpu_precise(ctx, A, B), R, "dense word")
+    assert_same_csr(gpu_upper(ctx, A, B), R, "dense word upper")
+
+
+def test_invalid_input_rejected():
+    A = _csr([[0, 1], [2]], 3)
+    bad = A.copy()
+    bad.col[0], bad.col[1] = bad.col[1], bad.col[0]  # unsorted row
+    with pytest.raises(brm.BrmError) as ei:
+        brm.brmerge_precise(bad, A.copy())
+    assert ei.value.status == 2
+    oob = A.copy()
+    oob.col[2] = 7  # column out of range
+    with pytest.raises(brm.BrmError) as ei:
+        brm.brmerge_precise(A, oob)
+    assert ei.value.status == 2
+    with pytest.raises(ValueError):
+        brm.brmerge_precise(A, _csr([[0]], 1))
+
+
+def test_device_validate(ctx):
+    A = _csr([[0, 1], [2], []], 3)
+    assert ctx.validate(dev(A)) == -1
+    bad = A.copy()
+    bad.col[1] = 0
+    assert ctx.validate(dev(bad)) == 0
+
+
+def test_numeric_requires_plan(ctx):
+    A = brm.gen_er(256, 4, seed=1)
+    dA = dev(A)
+    crpt, n = ctx.symbolic(dA, dA)
+    other = dev(brm.gen_er(256, 4, seed=2))
+    with pytest.raises(brm.BrmError) as ei:
+        ctx.numeric(other, other, crpt, n)
+    assert ei.value.status == 6
+
+
+def test_compute_flop_and_bound(ctx, oracle_mod):
+    A = brm.gen_rmat(12, int(2.35 * 4096), seed=4)
+    dA = dev(A)
+    f = ctx.compute_flop(dA, dA)
+    assert f == oracle_mod.compute_flop(A, A) == brm.compute_flop_host(A, A)
+    p, nbytes = ctx.upper_bound(dA, dA)
+    assert p == f and nbytes >= 24 * f
+
+
+# ---------------------------------------------------------------------------
+# full-size configurations
+# ---------------------------------------------------------------------------
+
+def test_er_config_full(ctx, oracle_mod):
+    """ER n=16384, exactly 8 per row, seed 0 (the CPU configuration)."""
+    A = brm.gen_er(16384, 8, seed=0)
+    assert_same_csr(gpu_precise(ctx, A, A), oracle_mod.precise(A, A), "er16384")
+
+
+def test_rmat_config_full(ctx, oracle_mod):
+    """Power-law R-MAT n=2^18, ~600k nnz, Precise and Upper, bit-exact."""
+    A = brm.gen_rmat(18, int(2.35 * (1 << 18)), seed=0)
+    R = oracle_mod.precise(A, A)
+    assert_same_csr(gpu_precise(ctx, A, A), R, "rmat18 precise")
+    assert_same_csr(gpu_upper(ctx, A, A), R, "rmat18 upper")
+
+
+def test_stencil_config_full_properties(ctx, oracle_mod):
+    """27-point stencil on 128^3: exact structure by closed form, values of
+    sampled row blocks against the oracle (rows of C are independent)."""
+    import torch
+    n = 128
+    A = brm.gen_stencil27(n)
+    dA = dev(A)
+    crpt, cnnz = ctx.symbolic(dA, dA)
+    assert cnnz == (5 * n - 6) ** 3  # 634^3: every row reaches a 5x5x5 box clipped at faces
+    C = ctx.numeric(dA, dA, crpt, cnnz)
+    # row lengths: product over dimensions of the clipped box widths
+    w = np.array([min(x + 2, n - 1) - max(x - 2, 0) + 1 for x in range(n)], np.int64)
+    lens = (w[None, None, :] * w[None, :, None] * w[:, None, None]).reshape(-1)
+    assert np.array_equal(np.diff(crpt.cpu().numpy().astype(np.int64)), lens)
+    rpt = crpt.cpu().numpy()
+    for r0 in (0, 70000, n ** 3 // 2, n ** 3 - 3000):
+        rows = np.arange(r0, r0 + 3000)
+        sub = brm.CSR(len(rows), A.N, np.concatenate([[0], np.cumsum(np.diff(A.rpt)[rows])]).astype(np.int32),
+                      np.concatenate([A.col[A.rpt[i]:A.rpt[i + 1]] for i in rows]),
+                      np.concatenate([A.val[A.rpt[i]:A.rpt[i + 1]] for i in rows]))
+        R = oracle_mod.precise(sub, A)
+        s, e = int(rpt[r0]), int(rpt[r0 + 3000])
+        got = brm.CSR(len(rows), A.N, (rpt[r0:r0 + 3001] - rpt[r0]).astype(np.int32),
+                      C.col[s:e].cpu().numpy(), C.val[s:e].cpu().numpy())
+        assert_same_csr(got, R, f"stencil rows {r0}")
+    torch.cuda.synchronize()
+
+
+def test_repeat_calls_identical(ctx):
+    A = brm.gen_rmat(15, int(2.35 * 32768), seed=9)
+    dA = dev(A)
+    C1 = ctx.precise(dA, dA).to_host()
+    C2 = ctx.precise(dA, dA).to_host()
+    assert_same_csr(C1, C2, "repeat")
