@@ -47,10 +47,11 @@ def _newer(target: Path, deps: list[Path]) -> bool:
     return any(d.stat().st_mtime > t for d in deps)
 
 
-def _run(cmd: list[str]) -> None:
+def _run(cmd: list[str]) -> str:
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("build step failed:\n" + " ".join(cmd) + "\n" + r.stdout + r.stderr)
+    return r.stdout + r.stderr
 
 
 def build_cuda(verbose: bool = False, debug: bool = False) -> Path:
@@ -73,7 +74,9 @@ def build_cuda(verbose: bool = False, debug: bool = False) -> Path:
         if _newer(o, [s] + headers):
             jobs.append([nvcc] + flags + ["-c", str(s), "-o", str(o)])
     with cf.ThreadPoolExecutor(max_workers=max(1, min(len(jobs), os.cpu_count() or 4))) as ex:
-        list(ex.map(_run, jobs))
+        for log in ex.map(_run, jobs):
+            if verbose:
+                print(log)
     if jobs or _newer(out, objs):
         tmp = out.with_suffix(".so.tmp")
         _run([nvcc] + ARCH + ["-shared", "-cudart", "static", "-o", str(tmp)] + [str(o) for o in objs])

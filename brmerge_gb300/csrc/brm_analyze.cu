@@ -42,17 +42,26 @@ __global__ void __launch_bounds__(kAnaThreads) k_analyze(CsrDev A, CsrDev B, Pla
                 s_bin[slot] = -1;
             continue;
         }
-        const int a0 = A.rpt[row], a1 = A.rpt[row + 1];
+        int a0 = A.rpt[row];
+        int a1 = A.rpt[row + 1];
         long long f = 0;
         int nl = 0, leaf = -1;
         bool bad = false;
+        if (a0 < 0 || a1 < a0 || a1 > A.nnz) {  // malformed row pointers: treat the row as empty
+            bad = true;
+            a0 = a1 = 0;
+        }
         for (int j = a0 + lane; j < a1; j += 32) {
             int b = A.col[j];
-            int len = 0;
-            if ((unsigned)b < (unsigned)K)
-                len = B.rpt[b + 1] - B.rpt[b];
-            else
+            int len = 0, bs = 0;
+            if ((unsigned)b < (unsigned)K) {
+                bs = B.rpt[b];
+                len = B.rpt[b + 1] - bs;
+            } else {
                 bad = true;
+            }
+            P.abs[j] = bs;
+            P.alen[j] = len;
             f += len;
             if (len > 0) {
                 nl++;
@@ -77,11 +86,16 @@ __global__ void __launch_bounds__(kAnaThreads) k_analyze(CsrDev A, CsrDev B, Pla
                 bin = kBinCopy;
             else if (f <= kWarpMaxFlop)
                 bin = kBinWarp;
-            else if (f > kHeavyFlop)
-                bin = kBinHeavy;
+            else if (f <= kMidFlop && 2 * nl <= kMidFlop && a1 - a0 <= kMidMaxK)
+                bin = kBinBatch;
+            else if (a1 - a0 <= kSegMaxK)
+                bin = kBinHeavy;  // segmented (brm_seg.cuh)
             else
-                bin = kBinMid;
+                bin = kBinMid;    // row CTA / spill path
             P.flop[row] = (int)f;
+            if (bin == kBinHeavy)
+                P.seg_base[row] = atomicAdd(&P.cnt->seg_cap, seg_bound(f, B.N));
+            P.mid_flop[row] = bin == kBinBatch ? max((int)f, 2 * nl) : 0;  // batch weight
             P.spill[row] = 0;
             if (bin == kBinEmpty)
                 P.nnz[row] = 0;
@@ -90,7 +104,7 @@ __global__ void __launch_bounds__(kAnaThreads) k_analyze(CsrDev A, CsrDev B, Pla
                 P.copy_leaf[row] = leaf;
             }
             s_bin[slot] = bin;
-            s_idx[slot] = bin == kBinEmpty ? 0 : atomicAdd(&s_cnt[bin], 1);
+            s_idx[slot] = (bin == kBinEmpty || bin == kBinBatch) ? 0 : atomicAdd(&s_cnt[bin], 1);
             wflop += (unsigned long long)f;
             wmaxk = max(wmaxk, a1 - a0);
         }
@@ -117,7 +131,7 @@ __global__ void __launch_bounds__(kAnaThreads) k_analyze(CsrDev A, CsrDev B, Pla
     __syncthreads();
     for (int slot = threadIdx.x; slot < RPB; slot += kAnaThreads) {
         int bin = s_bin[slot];
-        if (bin > kBinEmpty)
+        if (bin > kBinEmpty && bin != kBinBatch)
             P.rows[(size_t)bin * M + s_base[bin] + s_idx[slot]] = row0 + slot;
     }
 }

@@ -39,6 +39,10 @@ struct brm_context_s {
     int *d_bad = nullptr;
     brm::Counters *h_cnt = nullptr;  // pinned mirror of the device counters
     int *h_bad = nullptr;            // pinned
+    // per-A-entry list metadata (B-row start and length)
+    DevBuf ameta;
+    // heavy-row segments: descriptors + written list, and the split table
+    DevBuf segbuf, splitbuf;
     // spill scratch
     DevBuf spill;
     // Upper upper-bound buffer
@@ -120,6 +124,11 @@ size_t workspace_bytes(int M)
     b += a256(4 * m);                       // spill_rows
     b += a256(8 * m);                       // spill_off
     b += a256(8 * (m + 1));                 // scan_flop
+    b += a256(4 * m);                       // mid_flop
+    b += a256(8 * (m + 1));                 // mid_pre
+    b += a256(4 * (m + 1));                 // batch_start
+    b += a256(8 * m);                       // seg_base
+    b += a256(4 * m);                       // seg_n
     b += a256(sizeof(brm::Counters));
     b += a256(brm::scan_tmp_bytes((int)m + 1));
     b += a256(4);                           // bad row
@@ -155,9 +164,23 @@ int ensure_workspace(brm_context ctx, int M)
     P.spill_rows = (int *)take(4 * m);
     P.spill_off = (unsigned long long *)take(8 * m);
     P.scan_flop = (long long *)take(8 * (m + 1));
+    P.mid_flop = (int *)take(4 * m);
+    P.mid_pre = (long long *)take(8 * (m + 1));
+    P.batch_start = (int *)take(4 * (m + 1));
+    P.seg_base = (unsigned long long *)take(8 * m);
+    P.seg_n = (int *)take(4 * m);
     P.cnt = (brm::Counters *)take(sizeof(brm::Counters));
     ctx->scan_tmp = take(brm::scan_tmp_bytes((int)m + 1));
     ctx->d_bad = (int *)take(4);
+    return BRM_SUCCESS;
+}
+
+int ensure_ameta(brm_context ctx, int nnzA)
+{
+    const size_t n = (size_t)(nnzA > 0 ? nnzA : 1);
+    BRM_TRY(grow(ctx->ameta, 8 * n));
+    ctx->plan.abs = (int *)ctx->ameta.p;
+    ctx->plan.alen = (int *)ctx->ameta.p + n;
     return BRM_SUCCESS;
 }
 
@@ -240,6 +263,7 @@ int plan_phase(brm_context ctx, const brm_csr *A, const brm_csr *B, int *crpt, b
                bool timed)
 {
     BRM_TRY(ensure_workspace(ctx, A->M));
+    BRM_TRY(ensure_ameta(ctx, A->nnz));
     if (ctx->validate)
         BRM_TRY(validate_pair(ctx, A, B));
     brm::CsrDev a = to_dev(A), b = to_dev(B);
@@ -250,6 +274,19 @@ int plan_phase(brm_context ctx, const brm_csr *A, const brm_csr *B, int *crpt, b
     ev_record(ctx, timed, 0);
     BRM_CK(cudaMemsetAsync(P.cnt, 0, sizeof(brm::Counters), s));
     brm::launch_analyze(a, b, P, s);
+    brm::launch_batches(P, A->M, ctx->scan_tmp, s);
+    // the segment descriptors of heavy rows are sized by the analysis
+    BRM_CK(cudaGetLastError());
+    BRM_CK(cudaMemcpyAsync(ctx->h_cnt, P.cnt, sizeof(brm::Counters), cudaMemcpyDeviceToHost, s));
+    BRM_CK(cudaStreamSynchronize(s));
+    {
+        const size_t cap = (size_t)ctx->h_cnt->seg_cap + 1;
+        BRM_TRY(grow(ctx->segbuf, cap * (sizeof(brm::SegDesc) + sizeof(int))));
+        P.seg = (brm::SegDesc *)ctx->segbuf.p;
+        P.seg_list = (int *)(P.seg + cap);
+        ctx->plan.seg = P.seg;
+        ctx->plan.seg_list = P.seg_list;
+    }
     ev_record(ctx, timed, 1);
     brm::launch_symbolic(a, b, P, ctx->num_sms, upper, s);
     ev_record(ctx, timed, 2);
@@ -289,6 +326,10 @@ int numeric_launch(brm_context ctx, brm_dtype dtype, bool upper, const brm_csr *
     cudaStream_t s = ctx->stream;
     brm::PlanDev P = ctx->plan;
     BRM_CK(cudaMemsetAsync(&P.cnt->work_num, 0, 2 * sizeof(int), s));  // work_num, err
+    BRM_CK(cudaMemsetAsync(&P.cnt->work_bnum, 0, 2 * sizeof(int), s));  // work_bnum, work_seg
+    BRM_TRY(grow(ctx->splitbuf, ((size_t)ctx->h_cnt->table_cap + 1) * sizeof(int)));
+    P.split = (int *)ctx->splitbuf.p;
+    ctx->plan.split = P.split;
     brm::CsrDev a = to_dev(A), b = to_dev(B);
     if (dtype == BRM_F64)
         brm::launch_numeric_f64(upper, a, b, P, crpt, ccol, cval, ctx->spill.p, ctx->spill_bytes,
@@ -530,6 +571,9 @@ int brm_destroy(brm_context ctx)
     if (ctx->ws)
         cudaFree(ctx->ws);
     release(ctx->spill);
+    release(ctx->ameta);
+    release(ctx->segbuf);
+    release(ctx->splitbuf);
     release(ctx->bar_col);
     release(ctx->bar_val);
     release(ctx->io_arpt);
@@ -792,6 +836,7 @@ int brm_compute_flop(brm_context ctx, const brm_csr *A, const brm_csr *B, long l
         return BRM_ERR_INVALID_VALUE;
     BRM_TRY(check_pair(A, B));
     BRM_TRY(ensure_workspace(ctx, A->M));
+    BRM_TRY(ensure_ameta(ctx, A->nnz));
     brm::PlanDev P = ctx->plan;
     P.M = A->M;
     ctx->planned = false;

@@ -11,6 +11,10 @@ namespace brm {
 // (replaces compute_flop and the static load balance, spgemm.h:31-56, :496-503).
 void launch_analyze(const CsrDev &A, const CsrDev &B, const PlanDev &P, cudaStream_t s);
 
+// Mid-row batches: scan of the mid products in row order and the first row
+// of every batch (Counters::n_batch batches).
+void launch_batches(const PlanDev &P, int M, void *tmp, cudaStream_t s);
+
 // Exclusive scans with out[n] = total.  The int32 form ORs kErrOverflow into
 // cnt->err and stores the int64 total in cnt->cnnz (spgemm.h:564-578).
 void launch_scan_i32(const int *in, int *out, int n, Counters *cnt, void *tmp, cudaStream_t s);

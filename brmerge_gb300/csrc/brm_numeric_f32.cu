@@ -1,5 +1,7 @@
 // brm_numeric_f32.cu -- numeric phase launchers for float values.
 #include "brm_kernels.h"
+#include "brm_mid.cuh"
+#include "brm_seg.cuh"
 #include "brm_rows.cuh"
 
 namespace brm {
@@ -11,6 +13,15 @@ static void numeric_f32(const CsrDev &A, const CsrDev &B, const PlanDev &P, cons
 {
     k_copy_numeric<float, UPPER><<<num_sms * 8, 256, 0, s>>>(A, B, P, crpt, ccol, cval);
     k_warp_numeric<float, UPPER><<<num_sms * 8, 256, 0, s>>>(A, B, P, crpt, ccol, cval);
+    const size_t msm = MidNumLayout<float>::bytes;
+    cudaFuncSetAttribute(k_mid_numeric<float, UPPER>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)msm);
+    k_mid_numeric<float, UPPER><<<num_sms * 2, kMidThreads, msm, s>>>(A, B, P, crpt, ccol, cval);
+    k_split<0><<<num_sms * 8, 256, 0, s>>>(A, B, P);
+    const size_t ssm = SegLayout<float>::bytes;
+    cudaFuncSetAttribute(k_seg_numeric<float, UPPER>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)ssm);
+    k_seg_numeric<float, UPPER><<<num_sms * 2, kSegThreads, ssm, s>>>(A, B, P, crpt, ccol, cval);
     const size_t smem = NumLayout<float>::bytes;
     cudaFuncSetAttribute(k_rows_numeric<float, UPPER>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)smem);

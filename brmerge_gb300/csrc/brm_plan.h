@@ -19,6 +19,32 @@ constexpr int kWarpMaxFlop = 32;            // rows up to this many products go 
 constexpr int kHeavyFlop = 4 * kCap;        // rows above this are scheduled first
 constexpr int kRadixBits = 7;
 
+// Batched mid-row kernels: rows with more than kWarpMaxFlop products, weight
+// w = max(products, 2 * nonempty lists) <= kMidFlop and at most kMidMaxK A
+// entries are packed, in row order, into batches (a batch starts where the
+// row-order prefix of w crosses a multiple of kMidFlop, so a batch holds at
+// most kMidCap products and kMidMaxLists nonempty lists).
+constexpr int kMidThreads = 256;
+constexpr int kMidCap = 4096;
+constexpr int kMidFlop = kMidCap / 2;
+constexpr int kMidMaxLists = kMidCap / 2;
+constexpr int kMidMaxK = 255;
+constexpr int kMidMaxRows = kMidCap / (kWarpMaxFlop + 1) + 2;
+
+// Segmented heavy rows: a row that is not a mid row is cut, at 32-column word
+// boundaries, into column segments of at most kSegCap products spanning at
+// most kSegSpan columns.  The planning pass records, for every segment
+// boundary and every list of the row, where the list crosses the boundary
+// (the split table), so each segment is an independent unit of work.
+constexpr int kSegThreads = 256;
+constexpr int kSegCap = 3072;
+constexpr int kSegCut = kSegCap / 2;      // target products between cuts
+constexpr int kSegSpanBits = 16;
+constexpr int kSegSpan = 1 << kSegSpanBits;
+constexpr int kSegMaxK = 65535;           // leaf index stored in 16 bits
+constexpr int kPlanWords = 4096;          // bitmap words per planning chunk
+constexpr int kPlanBits = kPlanWords * 32;
+
 // Device error bits, OR-ed into Counters::err and read back by the host.
 enum DevErr : int {
     kErrNone = 0,
@@ -36,7 +62,8 @@ enum RowBin : int {
     kBinWarp = 2,   // <= kWarpMaxFlop products, >= 2 nonempty lists
     kBinHeavy = 3,  // row CTA, scheduled first
     kBinMid = 4,    // row CTA
-    kNumBins = 5,
+    kBinBatch = 5,  // batched mid-row kernels (no row list: row-order batches)
+    kNumBins = 6,
 };
 
 // Device counters (one struct in device memory, zeroed per phase).
@@ -50,7 +77,37 @@ struct Counters {
     unsigned long long total_flop;
     unsigned long long spill_bytes;  // scratch reserved for spill rows
     long long cnnz;    // total nnz of C (int64 before the int32 check)
-    int pad[4];
+    int n_batch;       // number of mid-row batches
+    int work_bsym;     // dynamic batch counter, symbolic
+    int work_bnum;     // dynamic batch counter, numeric
+    int work_seg;      // dynamic segment counter, numeric
+    unsigned long long seg_cap;    // descriptor slots reserved by the analysis
+    unsigned long long table_cap;  // split-table entries reserved by the planning
+    int n_seg;         // segments written by the planning
+    int work_plan;     // dynamic row counter of the heavy-row planning
+    int pad[2];
+};
+
+// Descriptor slots reserved for a heavy row with F products: the cut rule
+// makes at most F / kSegCut cuts at product thresholds, 2 per dense word
+// (a word with more than kSegCut products; at most F / kSegCut of them) and
+// at most 2 h / kSegCut + 1 inside a dense word of h products, plus the span
+// cuts and one chunk start per kPlanBits columns.
+__host__ __device__ inline unsigned long long seg_bound(long long F, int N)
+{
+    return 6ull * (unsigned long long)((F + kSegCut - 1) / kSegCut) +
+           3ull * ((unsigned)N >> kSegSpanBits) + 8ull;
+}
+
+// One column segment of a heavy row.
+struct SegDesc {
+    int row;
+    int c_lo;       // first column of the segment
+    int c_hi;       // one past the last column
+    int u_off;      // distinct columns of the row before c_lo
+    int bidx;       // boundary index of c_lo in the row's split table
+    int nprod;      // products in the segment
+    long long tab;  // split-table offset of the row (boundary-major, k entries each)
 };
 
 // Device arrays of a plan (all sized for M rows unless noted).
@@ -64,6 +121,16 @@ struct PlanDev {
     int *spill_rows;  // [M] spill row list
     unsigned long long *spill_off;  // [M] scratch byte offset per spill list entry
     long long *scan_flop;  // [M+1] exclusive scan of flop (Upper)
+    int *abs;              // [nnz(A)] start of B row acol[j] (list start of A entry j)
+    int *alen;             // [nnz(A)] length of B row acol[j] (0 if acol[j] is out of range)
+    int *mid_flop;         // [M] products of batched mid rows, 0 for other rows
+    long long *mid_pre;    // [M+1] exclusive scan of mid_flop
+    int *batch_start;      // [M+1] first row of each mid batch
+    unsigned long long *seg_base;  // [M] first descriptor slot of each heavy row
+    int *seg_n;            // [M] segments of each heavy row (0: not segmented)
+    SegDesc *seg;          // [Counters::seg_cap] segment descriptors (numbered per row)
+    int *seg_list;         // [Counters::seg_cap] descriptor slot of every written segment
+    int *split;            // [Counters::table_cap] split table (numeric phase)
     Counters *cnt;
 };
 

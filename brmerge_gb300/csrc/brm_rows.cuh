@@ -213,7 +213,7 @@ __global__ void __launch_bounds__(kRowThreads) k_rows_symbolic(CsrDev A, CsrDev 
     int *misc = (int *)(smem + SymLayout::o_misc);
     const int tid = threadIdx.x;
     const int M = A.M;
-    const int nheavy = P.cnt->bin_count[kBinHeavy];
+    const int nheavy = 0;  // heavy rows are segmented (brm_seg.cuh); this kernel takes kBinMid
     const int ntot = nheavy + P.cnt->bin_count[kBinMid];
     const int *heavy = P.rows + (size_t)kBinHeavy * M;
     const int *mid = P.rows + (size_t)kBinMid * M;
@@ -611,7 +611,7 @@ __global__ void __launch_bounds__(kRowThreads, 1)
     extern __shared__ __align__(16) unsigned char smem[];
     int *misc = (int *)(smem + NumLayout<T>::o_misc);
     const int M = A.M;
-    const int nheavy = P.cnt->bin_count[kBinHeavy];
+    const int nheavy = 0;  // heavy rows are segmented (brm_seg.cuh); this kernel takes kBinMid
     const int ntot = nheavy + P.cnt->bin_count[kBinMid];
     const int *heavy = P.rows + (size_t)kBinHeavy * M;
     const int *mid = P.rows + (size_t)kBinMid * M;

@@ -1,16 +1,35 @@
 // brm_symbolic.cu -- symbolic phase launchers (exact row nnz, spill routing).
 #include "brm_kernels.h"
+#include "brm_mid.cuh"
 #include "brm_rows.cuh"
+#include "brm_seg.cuh"
 
 namespace brm {
+
+void launch_batches(const PlanDev &P, int M, void *tmp, cudaStream_t s)
+{
+    if (M <= 0)
+        return;
+    launch_scan_i64(P.mid_flop, P.mid_pre, M, tmp, s);
+    k_batch_starts<0><<<(M + 1 + 255) / 256, 256, 0, s>>>(P, M);
+}
 
 void launch_symbolic(const CsrDev &A, const CsrDev &B, const PlanDev &P, int num_sms,
                      bool only_heavy, cudaStream_t s)
 {
     if (A.M <= 0)
         return;
-    if (!only_heavy)
+    if (!only_heavy) {
         k_warp_symbolic<0><<<num_sms * 8, 256, 0, s>>>(A, B, P);
+        const size_t msm = MidSymLayout::bytes;
+        cudaFuncSetAttribute(k_mid_symbolic<0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)msm);
+        k_mid_symbolic<0><<<num_sms * 2, kMidThreads, msm, s>>>(A, B, P);
+    }
+    // heavy rows: exact nnz and segment plan (both Precise and Upper)
+    const size_t psm = PlanLayout::bytes;
+    cudaFuncSetAttribute(k_heavy_plan<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)psm);
+    k_heavy_plan<0><<<num_sms * 3, kPlanThreads, psm, s>>>(A, B, P);
     const size_t smem = SymLayout::bytes;
     if (only_heavy) {
         cudaFuncSetAttribute(k_rows_symbolic<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,

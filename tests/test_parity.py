@@ -201,8 +201,22 @@ def test_spill_dense_word(ctx, oracle_mod):
     assert_same_csr(gpu_upper(ctx, A, B), R, "dense word upper")
 
 
+def test_spill_dense_column(ctx, oracle_mod):
+    # one column shared by more lists than a column segment holds (the
+    # global-memory spill path), next to ordinary segmented rows
+    rng = np.random.default_rng(23)
+    K, N = 4000, 3000
+    Brows = [sorted(set([7] + list(rng.choice(N, rng.integers(0, 5), replace=False))))
+             for _ in range(K)]
+    Arows = [list(range(K)), list(range(0, K, 7)), [1, 2, 3]]
+    A, B = _csr(Arows, K, 9), _csr(Brows, N, 10)
+    R = oracle_mod.precise(A, B)
+    assert_same_csr(gpu_precise(ctx, A, B), R, "dense column")
+    assert_same_csr(gpu_upper(ctx, A, B), R, "dense column upper")
+
+
 def test_invalid_input_rejected():
-    A = _csr([[0, 1], [2]], 3)
+    A = _csr([[0, 1], [2], [1]], 3)
     bad = A.copy()
     bad.col[0], bad.col[1] = bad.col[1], bad.col[0]  # unsorted row
     with pytest.raises(brm.BrmError) as ei:
@@ -214,7 +228,7 @@ def test_invalid_input_rejected():
         brm.brmerge_precise(A, oob)
     assert ei.value.status == 2
     with pytest.raises(ValueError):
-        brm.brmerge_precise(A, _csr([[0]], 1))
+        brm.brmerge_precise(A, _csr([[0]], 1))  # A.N != B.M
 
 
 def test_device_validate(ctx):
