@@ -166,6 +166,20 @@ int brm_compute_flop(brm_context ctx, const brm_csr *A, const brm_csr *B, long l
 int brm_upper_bound(brm_context ctx, brm_dtype dtype, const brm_csr *A, const brm_csr *B,
                     long long *products, long long *bytes);
 
+/* Per-row intermediate products of A*B (device A, B) without allocating any
+ * memory.  This entry point has no counterpart in the reference.  It is for
+ * callers that may not allocate when they need the count, for example an
+ * admission controller sizing a request before it reserves anything.
+ * row_flop: optional caller buffer of A->M ints (device) for the per-row
+ * counts; *products (host) receives the total.  Reduction scratch is a fixed
+ * 512 KB array in device memory shared by all calls: A->M may be at most
+ * 4,194,304 rows (BRM_ERR_CAPACITY beyond), and calls that overlap on the GPU
+ * race on the scratch.  The first call on each device looks up the scratch's
+ * device address, so make it before any stream capture.  The call
+ * synchronises `stream` (cudaStream_t as void*; NULL = legacy default). */
+int brm_compute_flop_noalloc(const brm_csr *A, const brm_csr *B, int *row_flop,
+                             long long *products, void *stream);
+
 /* Checks the CSR invariants of X on the device (columns must be < ncols).
  * *bad_row = -1 if valid, else the first offending row.  Returns
  * BRM_SUCCESS or BRM_ERR_INVALID_CSR. */
