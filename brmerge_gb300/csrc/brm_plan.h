@@ -32,18 +32,19 @@ constexpr int kMidMaxK = 255;
 constexpr int kMidMaxRows = kMidCap / (kWarpMaxFlop + 1) + 2;
 
 // Segmented heavy rows: a row that is not a mid row is cut, at 32-column word
-// boundaries, into column segments of at most kSegCap products spanning at
-// most kSegSpan columns.  The planning pass records, for every segment
-// boundary and every list of the row, where the list crosses the boundary
-// (the split table), so each segment is an independent unit of work.
+// (or, inside very dense words, column) boundaries, into column segments of at
+// most kSegCap products within one planning chunk of kPlanBits columns.  The
+// planning pass records, for every segment boundary and every list of the
+// row, where the list crosses the boundary (the split table), so each segment
+// is an independent unit of work.
 constexpr int kSegThreads = 256;
 constexpr int kSegCap = 3072;
 constexpr int kSegCut = kSegCap / 2;      // target products between cuts
-constexpr int kSegSpanBits = 16;
-constexpr int kSegSpan = 1 << kSegSpanBits;
 constexpr int kSegMaxK = 65535;           // leaf index stored in 16 bits
-constexpr int kPlanWords = 4096;          // bitmap words per planning chunk
-constexpr int kPlanBits = kPlanWords * 32;
+constexpr int kPlanWordsLog2 = 13;
+constexpr int kPlanWords = 1 << kPlanWordsLog2;  // bitmap words per planning chunk
+constexpr int kPlanBits = kPlanWords * 32;       // 2^18 columns
+constexpr int kSumWords = kPlanBits / 1024;      // summary words of a segment bitmap
 
 // Device error bits, OR-ed into Counters::err and read back by the host.
 enum DevErr : int {
@@ -89,14 +90,14 @@ struct Counters {
 };
 
 // Descriptor slots reserved for a heavy row with F products: the cut rule
-// makes at most F / kSegCut cuts at product thresholds, 2 per dense word
-// (a word with more than kSegCut products; at most F / kSegCut of them) and
-// at most 2 h / kSegCut + 1 inside a dense word of h products, plus the span
-// cuts and one chunk start per kPlanBits columns.
+// makes at most F / kSegCut cuts at product thresholds (plus one per chunk),
+// 2 per dense word (a word with more than kSegCut products; at most
+// F / kSegCut of them) and at most 2 h / kSegCut + 1 inside a dense word of h
+// products, plus one chunk start per kPlanBits columns.
 __host__ __device__ inline unsigned long long seg_bound(long long F, int N)
 {
     return 6ull * (unsigned long long)((F + kSegCut - 1) / kSegCut) +
-           3ull * ((unsigned)N >> kSegSpanBits) + 8ull;
+           2ull * ((unsigned)N / (unsigned)kPlanBits) + 8ull;
 }
 
 // One column segment of a heavy row.

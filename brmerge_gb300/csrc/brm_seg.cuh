@@ -11,17 +11,20 @@
 //      row's columns and a product count per 32-column word over chunks of
 //      kPlanBits columns give the row's exact nnz and the cut points: a cut
 //      before word w when the running product count crosses a multiple of
-//      kSegCut, around words holding more than kSegCut products, and every
-//      kSegSpan columns; each segment then holds <= kSegCap products.  The
-//      segment's output offset within the row (distinct columns before c_lo)
-//      comes from the same bitmap.
+//      kSegCut and around words holding more than kSegCut products (inside
+//      such a word the cuts are per column); a segment then holds <= kSegCap
+//      products.  Its output offset within the row (distinct columns before
+//      c_lo) comes from the same bitmap.
 //   2. split table (numeric phase): for every segment boundary and every list
 //      of the row, the first list position at or after the boundary column
-//      (one independent binary search per entry).
+//      (one block per boundary, one binary search per list).
 //   3. segment kernel (numeric phase, one CTA pass per segment): stage the
-//      segment's products in list-major order, stable LSD radix sort on the
-//      column offset c - c_lo (< 2^kSegSpanBits, two 8-bit passes), then one
-//      thread per output column evaluates the merge tree with ShiftReduce.
+//      segment's products in list-major order; the rank u of every product's
+//      column among the segment's distinct columns comes from a two-level
+//      bitmap (a summary bit per nonempty 32-column word, then the compressed
+//      words); a stable radix sort on u puts each column's contributions in
+//      leaf order; one thread per output column evaluates the merge tree with
+//      ShiftReduce and stores column u at position u (coalesced).
 #pragma once
 
 #include <climits>
@@ -33,7 +36,6 @@
 namespace brm {
 
 constexpr int kPlanThreads = 512;
-
 constexpr int kDenseMax = 128;  // dense words per planning chunk with per-column counts
 
 struct PlanLayout {
@@ -41,10 +43,79 @@ struct PlanLayout {
     static constexpr size_t o_hist = o_bm + kPlanWords * 4;
     static constexpr size_t o_dix = o_hist + kPlanWords * 4;
     static constexpr size_t o_ccnt = o_dix + kPlanWords * 2;
-    static constexpr size_t o_ws = o_ccnt + kDenseMax * 32 * 4;
+    static constexpr size_t o_lst = o_ccnt + kDenseMax * 32 * 4;
+    static constexpr size_t o_loffs = o_lst + (kPlanThreads + 1) * 4;
+    static constexpr size_t o_ws = o_loffs + (kPlanThreads + 1) * 4 + 8;
     static constexpr size_t o_misc = o_ws + (kPlanThreads / 32 + 1) * 8;
     static constexpr size_t bytes = o_misc + 64;
 };
+
+// Calls f(rc) for every product of the row whose column lies in [lo, chi),
+// rc = column - lo, with the products split evenly over the block: the lists
+// are taken NT at a time, their lengths scanned, and every thread walks a
+// contiguous share of the chunk's products (a single very long list of a
+// power-law row is shared by all threads instead of one group).  A thread
+// sees its products in list order, column-sorted within each list.
+// lst/loffs are NT+1 ints of shared scratch.
+template <int NT, typename Fn>
+__device__ __forceinline__ void plan_products(const PlanDev &P, const int *__restrict__ bcol,
+                                              int a0, int k, bool multi, int lo, int chi,
+                                              int *lst, int *loffs, long long *ws, Fn f)
+{
+    const int tid = threadIdx.x;
+    for (int lb = 0; lb < k; lb += NT) {
+        const int l = lb + tid;
+        int s = 0, len = 0;
+        if (l < k) {
+            len = P.alen[a0 + l];
+            s = P.abs[a0 + l];
+            if (multi && len > 0) {
+                int e = s + len;
+                s = lower_bound_idx(bcol, s, e, lo);
+                e = lower_bound_idx(bcol, s, e, chi);
+                len = e - s;
+            }
+        }
+        long long tot;
+        const int off = (int)block_excl_scan<NT, long long>(len, ws, &tot);
+        lst[tid] = s;
+        loffs[tid] = off;
+        if (tid == 0)
+            loffs[NT] = (int)tot;
+        __syncthreads();
+        const int n = (int)tot;
+        const int ipt = (n + NT - 1) / NT;
+        const int p0 = min(tid * ipt, n), p1 = min(p0 + ipt, n);
+        if (p0 < p1) {
+            int j = last_le(loffs, NT, p0);
+            int lbeg = loffs[j], lend = loffs[j + 1], bsj = lst[j];
+            for (int p = p0; p < p1; p += kGatherBatch) {
+                const int m = min(kGatherBatch, p1 - p);
+                int addr[kGatherBatch], c[kGatherBatch];
+#pragma unroll
+                for (int i = 0; i < kGatherBatch; i++) {
+                    if (i < m) {
+                        while (p + i >= lend) {
+                            j++;
+                            lbeg = lend;
+                            lend = loffs[j + 1];
+                            bsj = lst[j];
+                        }
+                        addr[i] = bsj + (p + i - lbeg);
+                    }
+                }
+#pragma unroll
+                for (int i = 0; i < kGatherBatch; i++)
+                    c[i] = i < m ? bcol[addr[i]] : 0;
+#pragma unroll
+                for (int i = 0; i < kGatherBatch; i++)
+                    if (i < m)
+                        f(c[i] - lo);
+            }
+        }
+        __syncthreads();
+    }
+}
 
 // Walks the segment starts of planning word w (chunk-relative) in column
 // order and calls f(column_in_word, product_prefix, distinct_prefix) for
@@ -75,8 +146,7 @@ __device__ __forceinline__ void plan_word_starts(int w, unsigned h, unsigned ph,
         }
         return;
     }
-    const bool start = (w == 0) || ph > (unsigned)kSegCut || (pe / kSegCut) != ((pe - ph) / kSegCut) ||
-                       ((w & (kSegSpan / 32 - 1)) == 0);
+    const bool start = (w == 0) || ph > (unsigned)kSegCut || (pe / kSegCut) != ((pe - ph) / kSegCut);
     if (start)
         f(0, pe, ue);
 }
@@ -93,6 +163,8 @@ __global__ void __launch_bounds__(kPlanThreads) k_heavy_plan(CsrDev A, CsrDev B,
     unsigned *hist = (unsigned *)(smem + PlanLayout::o_hist);
     unsigned short *dix = (unsigned short *)(smem + PlanLayout::o_dix);
     unsigned *ccnt = (unsigned *)(smem + PlanLayout::o_ccnt);
+    int *lst = (int *)(smem + PlanLayout::o_lst);
+    int *loffs = (int *)(smem + PlanLayout::o_loffs);
     long long *ws = (long long *)(smem + PlanLayout::o_ws);
     int *misc = (int *)(smem + PlanLayout::o_misc);
     const int tid = threadIdx.x;
@@ -134,9 +206,7 @@ __global__ void __launch_bounds__(kPlanThreads) k_heavy_plan(CsrDev A, CsrDev B,
             }
             continue;
         }
-        // lanes per list: about avg / kGatherBatch, a power of two in [1, 32]
-        const int G = group_size(F / kGatherBatch, k);
-        const int lg = tid & (G - 1);
+        const bool multi = (long long)mx + 1 - mn > kPlanBits;
         long long u_run = 0;
         int nseg = 0;
         bool fail = false;
@@ -145,41 +215,40 @@ __global__ void __launch_bounds__(kPlanThreads) k_heavy_plan(CsrDev A, CsrDev B,
             const int chi = (int)min((long long)mx + 1, clo + kPlanBits);
             const int span = chi - lo;
             const int nw = (span + 31) >> 5;
-            const bool multi = (long long)mx + 1 - mn > kPlanBits;
             for (int i = tid; i < nw; i += NT) {
                 bm[i] = 0;
                 hist[i] = 0;
             }
             __syncthreads();
-            // pass over the chunk's products: column bitmap and products per word
-            for (int l = tid / G; l < k; l += NT / G) {
-                const int len = P.alen[a0 + l];
-                if (len == 0)
-                    continue;
-                int s = P.abs[a0 + l], e = s + len;
-                if (multi) {
-                    s = lower_bound_idx(bcol, s, e, lo);
-                    e = lower_bound_idx(bcol, s, e, chi);
+            // pass over the chunk's products: column bitmap and products per
+            // word.  A thread's products are column-sorted within each list,
+            // so runs in one word are gathered in registers and flushed once.
+            bool bad = false;
+            unsigned run_w = 0, run_b = 0, run_n = 0;
+            plan_products<NT>(P, bcol, a0, k, multi, lo, chi, lst, loffs, ws, [&](int rc) {
+                if ((unsigned)rc >= (unsigned)span) {
+                    bad = true;
+                    return;
                 }
-                for (int idx = s + lg; idx < e; idx += G * kGatherBatch) {
-                    int c[kGatherBatch];
-#pragma unroll
-                    for (int i = 0; i < kGatherBatch; i++)
-                        c[i] = (idx + i * G < e) ? bcol[idx + i * G] : -1;
-#pragma unroll
-                    for (int i = 0; i < kGatherBatch; i++) {
-                        if (idx + i * G < e) {
-                            const int rc = c[i] - lo;
-                            if ((unsigned)rc < (unsigned)span) {
-                                atomicOr(&bm[rc >> 5], 1u << (rc & 31));
-                                atomicAdd(&hist[rc >> 5], 1u);
-                            } else {
-                                atomicOr(&P.cnt->err, kErrBadInput);
-                            }
-                        }
+                const unsigned w = (unsigned)rc >> 5;
+                if (w != run_w) {
+                    if (run_n) {
+                        atomicOr(&bm[run_w], run_b);
+                        atomicAdd(&hist[run_w], run_n);
                     }
+                    run_w = w;
+                    run_b = 0;
+                    run_n = 0;
                 }
+                run_b |= 1u << (rc & 31);
+                run_n++;
+            });
+            if (run_n) {
+                atomicOr(&bm[run_w], run_b);
+                atomicAdd(&hist[run_w], run_n);
             }
+            if (bad)
+                atomicOr(&P.cnt->err, kErrBadInput);
             __syncthreads();
             const int wpt = (nw + NT - 1) / NT;
             const int w0 = min(tid * wpt, nw), w1 = min(w0 + wpt, nw);
@@ -203,31 +272,10 @@ __global__ void __launch_bounds__(kPlanThreads) k_heavy_plan(CsrDev A, CsrDev B,
                 for (int i = tid; i < nd * 32; i += NT)
                     ccnt[i] = 0;
                 __syncthreads();
-                for (int l = tid / G; l < k; l += NT / G) {
-                    const int len = P.alen[a0 + l];
-                    if (len == 0)
-                        continue;
-                    int s = P.abs[a0 + l], e = s + len;
-                    if (multi) {
-                        s = lower_bound_idx(bcol, s, e, lo);
-                        e = lower_bound_idx(bcol, s, e, chi);
-                    }
-                    for (int idx = s + lg; idx < e; idx += G * kGatherBatch) {
-                        int c[kGatherBatch];
-#pragma unroll
-                        for (int i = 0; i < kGatherBatch; i++)
-                            c[i] = (idx + i * G < e) ? bcol[idx + i * G] : -1;
-#pragma unroll
-                        for (int i = 0; i < kGatherBatch; i++) {
-                            if (idx + i * G < e) {
-                                const int rc = c[i] - lo;
-                                if ((unsigned)rc < (unsigned)span && hist[rc >> 5] > (unsigned)kSegCut)
-                                    atomicAdd(&ccnt[dix[rc >> 5] * 32 + (rc & 31)], 1u);
-                            }
-                        }
-                    }
-                }
-                __syncthreads();
+                plan_products<NT>(P, bcol, a0, k, multi, lo, chi, lst, loffs, ws, [&](int rc) {
+                    if ((unsigned)rc < (unsigned)span && hist[rc >> 5] > (unsigned)kSegCut)
+                        atomicAdd(&ccnt[dix[rc >> 5] * 32 + (rc & 31)], 1u);
+                });
                 bool big = false;
                 for (int i = tid; i < nd * 32; i += NT)
                     big |= ccnt[i] > (unsigned)kSegCap;
@@ -371,81 +419,30 @@ __global__ void __launch_bounds__(256) k_split(CsrDev A, CsrDev B, PlanDev P)
 // ---------------------------------------------------------------------------
 // 3. segment kernel
 // ---------------------------------------------------------------------------
+constexpr int kLongRun = 32;  // runs longer than this are reduced in a separate pass
+constexpr int kLongMax = kSegCap / (kLongRun + 1) + 1;
+
 template <typename T>
 struct SegLayout {
     static constexpr int NW = kSegThreads / 32;
-    static constexpr size_t o_col = 0;
-    static constexpr size_t o_val = o_col + mid_a16(kSegCap * 4);
-    static constexpr size_t o_ia = o_val + mid_a16(kSegCap * sizeof(T));
-    static constexpr size_t o_ib = o_ia + mid_a16(kSegCap * 2);
-    static constexpr size_t o_leaf = o_ib + mid_a16(kSegCap * 2);
-    static constexpr size_t o_loff = o_leaf + mid_a16(kSegCap * 2);
+    static constexpr size_t o_loff = 0;
     static constexpr size_t o_lbs = o_loff + mid_a16((kSegCap + 1) * 4);
     static constexpr size_t o_lleaf = o_lbs + mid_a16(kSegCap * 4);
-    static constexpr size_t o_rcnt = o_lleaf + mid_a16(kSegCap * 2);
-    static constexpr size_t o_head = o_rcnt + mid_a16(256 * NW * 2);
-    static constexpr size_t o_ws = o_head + mid_a16(kSegCap / 8 + 4);
+    static constexpr size_t o_prc = o_lleaf + mid_a16(kSegCap * 2);
+    static constexpr size_t o_pval = o_prc + mid_a16(kSegCap * 4);
+    static constexpr size_t o_pleaf = o_pval + mid_a16(kSegCap * sizeof(T));
+    static constexpr size_t o_pu = o_pleaf + mid_a16(kSegCap * 2);
+    static constexpr size_t o_ia = o_pu + mid_a16(kSegCap * 2);
+    static constexpr size_t o_ib = o_ia + mid_a16(kSegCap * 2);
+    static constexpr size_t o_summ = o_ib + mid_a16(kSegCap * 2);
+    static constexpr size_t o_srank = o_summ + mid_a16(kSumWords * 4);
+    static constexpr size_t o_cw = o_srank + mid_a16(kSumWords * 2);
+    static constexpr size_t o_cwr = o_cw + mid_a16(kSegCap * 4);
+    static constexpr size_t o_long = o_cwr + mid_a16((kSegCap + 1) * 2);
+    static constexpr size_t o_ws = o_long + mid_a16(kLongMax * 2);
     static constexpr size_t o_misc = o_ws + mid_a16((NW + 1) * 8);
     static constexpr size_t bytes = o_misc + 64;
 };
-
-// One stable LSD pass with 8-bit digits over u16 indices; the digit of index
-// e is ((col[e] - c_lo) >> shift) & 255.  Same ownership scheme as radix_pass.
-template <int NT>
-__device__ __forceinline__ void radix_pass_idx(const unsigned short *__restrict__ src,
-                                               unsigned short *__restrict__ dst,
-                                               const int *__restrict__ col, int c_lo, int n,
-                                               int shift, unsigned short *cnt, int *ws)
-{
-    constexpr int NW = NT / 32;
-    constexpr int RADIX = 256;
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const int per = ((n + NW - 1) / NW + 31) & ~31;
-    const int beg = min(w * per, n), end = min(beg + per, n);
-    for (int d = lane; d < RADIX; d += 32)
-        cnt[d * NW + w] = 0;
-    __syncwarp();
-    for (int base = beg; base < end; base += 32) {
-        const int i = base + lane;
-        const bool valid = i < end;
-        const unsigned d = valid ? ((unsigned)(col[src[i]] - c_lo) >> shift) & 255u : 0xffffffffu;
-        const unsigned peers = __match_any_sync(kFull, d);
-        if (valid && lane == __ffs(peers) - 1)
-            cnt[d * NW + w] += (unsigned short)__popc(peers);
-        __syncwarp();
-    }
-    __syncthreads();
-    constexpr int PER = RADIX * NW / NT;
-    int local[PER];
-    int s = 0;
-#pragma unroll
-    for (int j = 0; j < PER; j++) {
-        local[j] = cnt[threadIdx.x * PER + j];
-        s += local[j];
-    }
-    int tot;
-    int ex = block_excl_scan<NT>(s, ws, &tot);
-#pragma unroll
-    for (int j = 0; j < PER; j++) {
-        cnt[threadIdx.x * PER + j] = (unsigned short)ex;
-        ex += local[j];
-    }
-    __syncthreads();
-    for (int base = beg; base < end; base += 32) {
-        const int i = base + lane;
-        const bool valid = i < end;
-        const unsigned short e = valid ? src[i] : 0;
-        const unsigned d = valid ? ((unsigned)(col[e] - c_lo) >> shift) & 255u : 0xffffffffu;
-        const unsigned peers = __match_any_sync(kFull, d);
-        if (valid)
-            dst[cnt[d * NW + w] + __popc(peers & lanemask_lt())] = e;
-        __syncwarp();
-        if (valid && lane == __ffs(peers) - 1)
-            cnt[d * NW + w] += (unsigned short)__popc(peers);
-        __syncwarp();
-    }
-    __syncthreads();
-}
 
 template <typename T, bool UPPER>
 __global__ void __launch_bounds__(kSegThreads) k_seg_numeric(CsrDev A, CsrDev B, PlanDev P,
@@ -454,16 +451,21 @@ __global__ void __launch_bounds__(kSegThreads) k_seg_numeric(CsrDev A, CsrDev B,
     constexpr int NT = kSegThreads;
     using L = SegLayout<T>;
     extern __shared__ __align__(16) unsigned char smem[];
-    int *col = (int *)(smem + L::o_col);
-    T *val = (T *)(smem + L::o_val);
-    unsigned short *ia = (unsigned short *)(smem + L::o_ia);
-    unsigned short *ib = (unsigned short *)(smem + L::o_ib);
-    unsigned short *leafp = (unsigned short *)(smem + L::o_leaf);
     int *loff = (int *)(smem + L::o_loff);
+    int *ucnt = loff;  // per-column counts, then column starts (after staging)
     int *lbs = (int *)(smem + L::o_lbs);
     unsigned short *lleaf = (unsigned short *)(smem + L::o_lleaf);
-    unsigned short *rcnt = (unsigned short *)(smem + L::o_rcnt);
-    unsigned *head = (unsigned *)(smem + L::o_head);
+    int *prc = (int *)(smem + L::o_prc);
+    T *pval = (T *)(smem + L::o_pval);
+    unsigned short *pleaf = (unsigned short *)(smem + L::o_pleaf);
+    unsigned short *pu = (unsigned short *)(smem + L::o_pu);
+    unsigned short *ia = (unsigned short *)(smem + L::o_ia);
+    unsigned short *ib = (unsigned short *)(smem + L::o_ib);
+    unsigned *summ = (unsigned *)(smem + L::o_summ);
+    unsigned short *srank = (unsigned short *)(smem + L::o_srank);
+    unsigned *cw = (unsigned *)(smem + L::o_cw);
+    unsigned short *cwr = (unsigned short *)(smem + L::o_cwr);
+    unsigned short *longu = (unsigned short *)(smem + L::o_long);
     long long *ws = (long long *)(smem + L::o_ws);
     int *wsi = (int *)(smem + L::o_ws);
     int *misc = (int *)(smem + L::o_misc);
@@ -485,6 +487,8 @@ __global__ void __launch_bounds__(kSegThreads) k_seg_numeric(CsrDev A, CsrDev B,
         const int row = d.row;
         const int a0 = A.rpt[row];
         const int k = A.rpt[row + 1] - a0;
+        const int span = d.c_hi - d.c_lo;
+        const int nsum = (span + 1023) >> 10;
         const int *sp0 = P.split + d.tab + (long long)d.bidx * k;
         const int *sp1 = sp0 + k;
         // nonempty sub-lists of the segment, in leaf order
@@ -511,18 +515,25 @@ __global__ void __launch_bounds__(kSegThreads) k_seg_numeric(CsrDev A, CsrDev B,
             pcarry += (int)(tot & 0xffffffffLL);
         }
         const int nlists = lcarry, nprod = pcarry;
-        if (nprod > kSegCap || nprod != d.nprod) {
+        if (nprod > kSegCap || nprod != d.nprod || nsum > kSumWords || span <= 0) {
             if (tid == 0)
                 atomicOr(&P.cnt->err, kErrWindowOverflow);
             continue;
         }
-        if (tid == 0)
+        if (tid == 0) {
             loff[nlists] = nprod;
-        for (int i = tid; i < (nprod + 31) / 32 + 1; i += NT)
-            head[i] = 0;
+            misc[1] = 0;  // long runs
+            misc[2] = 0;  // staged column out of range
+        }
+        if (tid < nsum)
+            summ[tid] = 0;
         __syncthreads();
+        // stage products in list-major (= leaf) order; mark their words in the summary
         const int ipt = (nprod + NT - 1) / NT;
         const int p0 = min(tid * ipt, nprod), p1 = min(p0 + ipt, nprod);
+        // a thread's products are column-sorted within each list, so runs of
+        // equal summary words are OR-ed in a register and flushed once
+        unsigned run_w = 0xffffffffu, run_b = 0;
         if (p0 < p1) {
             int j = last_le(loff, nlists, p0);
             int lbeg = loff[j], lend = loff[j + 1], bsj = lbs[j];
@@ -555,69 +566,196 @@ __global__ void __launch_bounds__(kSegThreads) k_seg_numeric(CsrDev A, CsrDev B,
                 for (int i = 0; i < kGatherBatch; i++) {
                     if (i < n) {
                         const int e = p + i;
-                        col[e] = c[i];
-                        val[e] = vmul(av[i], bv[i]);
-                        leafp[e] = lleaf[lid[i]];
-                        ia[e] = (unsigned short)e;
+                        int rc = c[i] - d.c_lo;
+                        if ((unsigned)rc >= (unsigned)span) {
+                            misc[2] = 1;
+                            rc = 0;
+                        }
+                        prc[e] = rc;
+                        pval[e] = vmul(av[i], bv[i]);
+                        pleaf[e] = lleaf[lid[i]];
+                        const unsigned sw = (unsigned)rc >> 10;
+                        if (sw != run_w) {
+                            if (run_b)
+                                atomicOr(&summ[run_w], run_b);
+                            run_w = sw;
+                            run_b = 0;
+                        }
+                        run_b |= 1u << ((rc >> 5) & 31);
                     }
                 }
             }
+            if (run_b)
+                atomicOr(&summ[run_w], run_b);
         }
         __syncthreads();
-        // stable sort by column offset (list-major input order = leaf order)
-        const int span = d.c_hi - d.c_lo;
-        unsigned short *src = ia, *dst = ib;
-        for (int sh = 0; sh < kSegSpanBits && (span - 1) >> sh; sh += 8) {
-            radix_pass_idx<NT>(src, dst, col, d.c_lo, nprod, sh, rcnt, wsi);
-            unsigned short *x = src;
-            src = dst;
-            dst = x;
+        if (misc[2]) {  // a column outside the segment: the plan does not match the input
+            if (tid == 0)
+                atomicOr(&P.cnt->err, kErrBadInput);
+            continue;
         }
-        // heads and their ranks
-        int nh = 0;
+        // compressed words: one per nonempty 32-column word
+        long long ncw_t;
         {
-            int prev = p0 > 0 && p0 < p1 ? col[src[p0 - 1]] : -1;
+            const unsigned sv = tid < nsum ? summ[tid] : 0u;
+            const int sx = (int)block_excl_scan<NT, long long>(__popc(sv), ws, &ncw_t);
+            if (tid < nsum)
+                srank[tid] = (unsigned short)sx;
+        }
+        const int ncw = (int)ncw_t;
+        for (int i = tid; i < ncw; i += NT)
+            cw[i] = 0;
+        for (int i = tid; i <= nprod; i += NT)  // the sub-list table is dead now
+            ucnt[i] = 0;
+        __syncthreads();
+        // mark the compressed words; keep each product's word index in pu
+        {
+            int run_ci = -1;
+            unsigned bits = 0;
             for (int p = p0; p < p1; p++) {
-                const int c = col[src[p]];
-                if (c != prev) {
-                    atomicOr(&head[p >> 5], 1u << (p & 31));
-                    nh++;
+                const int rc = prc[p];
+                const int w = rc >> 5;
+                const int ci = srank[w >> 5] + __popc(summ[w >> 5] & ((1u << (w & 31)) - 1u));
+                pu[p] = (unsigned short)ci;
+                if (ci != run_ci) {
+                    if (bits)
+                        atomicOr(&cw[run_ci], bits);
+                    run_ci = ci;
+                    bits = 0;
                 }
-                prev = c;
+                bits |= 1u << (rc & 31);
+            }
+            if (bits)
+                atomicOr(&cw[run_ci], bits);
+        }
+        __syncthreads();
+        // ranks of the compressed words -> distinct columns before each word
+        long long U_t;
+        {
+            const int cpt = (ncw + NT - 1) / NT;
+            const int c0 = min(tid * cpt, ncw), c1 = min(c0 + cpt, ncw);
+            int cs = 0;
+            for (int i = c0; i < c1; i++)
+                cs += __popc(cw[i]);
+            int r = (int)block_excl_scan<NT, long long>(cs, ws, &U_t);
+            for (int i = c0; i < c1; i++) {
+                cwr[i] = (unsigned short)r;
+                r += __popc(cw[i]);
             }
         }
-        long long htot;
-        const int hx = (int)block_excl_scan<NT, long long>(nh, ws, &htot);
+        const int U = (int)U_t;
+        const bool nodup = (U == nprod);
+        __syncthreads();
+        // u = distinct-column rank of each product; count the products of
+        // every column (the rank within a column, from the atomic, is in
+        // arbitrary order and is put in leaf order when the column is reduced)
+        for (int p = p0; p < p1; p++) {
+            const int ci = pu[p];
+            const int u = cwr[ci] + __popc(cw[ci] & ((1u << (prc[p] & 31)) - 1u));
+            pu[p] = (unsigned short)u;
+            if (!nodup)
+                ia[p] = (unsigned short)atomicAdd(&ucnt[u], 1);
+        }
+        __syncthreads();
         const long long obase = (UPPER ? P.scan_flop[row] : (long long)crpt[row]) + d.u_off;
-        {
-            int h = hx;
-            for (int p = p0; p < p1; p++) {
-                if (!((head[p >> 5] >> (p & 31)) & 1u))
-                    continue;
-                const int e = src[p];
-                int q = p + 1;
-                T v;
-                if (q >= nprod || ((head[q >> 5] >> (q & 31)) & 1u)) {
-                    v = val[e];
-                } else {
-                    ShiftReduce<T> sr;
-                    sr.init(leafp[e], val[e]);
-                    for (; q < nprod && !((head[q >> 5] >> (q & 31)) & 1u); q++) {
-                        const int e2 = src[q];
-                        sr.push(leafp[e2], val[e2]);
-                    }
-                    v = sr.finish();
-                }
-                ccol[obase + h] = col[e];
-                cval[obase + h] = v;
-                h++;
+        unsigned short *S = ib;
+        if (nodup) {
+            // every column has one contribution: position u holds product e
+            for (int p = p0; p < p1; p++)
+                S[pu[p]] = (unsigned short)p;
+        } else {
+            // exclusive scan of the column counts (in place), then scatter
+            const int cpt = (U + NT - 1) / NT;
+            const int c0 = min(tid * cpt, U), c1 = min(c0 + cpt, U);
+            int cs = 0;
+            for (int i = c0; i < c1; i++)
+                cs += ucnt[i];
+            long long tot;
+            int r = (int)block_excl_scan<NT, long long>(cs, ws, &tot);
+            for (int i = c0; i < c1; i++) {
+                const int c = ucnt[i];
+                ucnt[i] = r;
+                r += c;
             }
+            if (tid == 0)
+                ucnt[U] = nprod;
+            __syncthreads();
+            for (int p = p0; p < p1; p++)
+                S[ucnt[pu[p]] + ia[p]] = (unsigned short)p;
+        }
+        __syncthreads();
+        // one thread per output column (consecutive columns -> coalesced stores)
+        for (int u = tid; u < U; u += NT) {
+            int i0 = u, len = 1;
+            if (!nodup) {
+                i0 = ucnt[u];
+                len = ucnt[u + 1] - i0;
+            }
+            const int e0 = S[i0];
+            T v;
+            if (len == 1) {
+                v = pval[e0];
+            } else if (len == 2) {
+                const int e1 = S[i0 + 1];
+                v = pleaf[e0] < pleaf[e1] ? vadd(pval[e0], pval[e1])   // left + right
+                                          : vadd(pval[e1], pval[e0]);
+            } else if (len <= kLongRun) {
+                // insertion sort of the column's products by leaf, then the trie
+                for (int i = i0 + 1; i < i0 + len; i++) {
+                    const unsigned short e = S[i];
+                    const int key = pleaf[e];
+                    int j = i - 1;
+                    while (j >= i0 && pleaf[S[j]] > key) {
+                        S[j + 1] = S[j];
+                        j--;
+                    }
+                    S[j + 1] = e;
+                }
+                ShiftReduce<T, 17> sr;
+                sr.init(pleaf[S[i0]], pval[S[i0]]);
+                for (int i = i0 + 1; i < i0 + len; i++)
+                    sr.push(pleaf[S[i]], pval[S[i]]);
+                v = sr.finish();
+            } else {
+                const int li = atomicAdd(&misc[1], 1);
+                if (li < kLongMax)
+                    longu[li] = (unsigned short)u;
+                continue;
+            }
+            ccol[obase + u] = d.c_lo + prc[e0];
+            cval[obase + u] = v;
+        }
+        __syncthreads();
+        // long columns: one warp each ranks the products by leaf (leaves of
+        // one column are distinct) into ia, then its first lane reduces
+        const int nlong = min(misc[1], kLongMax);
+        for (int li = tid >> 5; li < nlong; li += NT / 32) {
+            const int lane = tid & 31;
+            const int u = longu[li];
+            const int i0 = ucnt[u], i1 = ucnt[u + 1];
+            for (int i = i0 + lane; i < i1; i += 32) {
+                const int key = pleaf[S[i]];
+                int r = 0;
+                for (int j = i0; j < i1; j++)
+                    r += pleaf[S[j]] < key ? 1 : 0;
+                ia[i0 + r] = S[i];
+            }
+            __syncwarp();
+            if (lane == 0) {
+                ShiftReduce<T, 17> sr;
+                sr.init(pleaf[ia[i0]], pval[ia[i0]]);
+                for (int i = i0 + 1; i < i1; i++)
+                    sr.push(pleaf[ia[i]], pval[ia[i]]);
+                ccol[obase + u] = d.c_lo + prc[ia[i0]];
+                cval[obase + u] = sr.finish();
+            }
+            __syncwarp();
         }
         if (tid == 0) {
             // the segment must produce exactly its share of the row's columns
             const int nseg = P.seg_n[row];
             const int next_u = (d.bidx + 1 < nseg) ? P.seg[slot + 1].u_off : P.nnz[row];
-            if ((int)htot != next_u - d.u_off)
+            if (U != next_u - d.u_off)
                 atomicOr(&P.cnt->err, kErrNnzMismatch);
         }
         __syncthreads();
