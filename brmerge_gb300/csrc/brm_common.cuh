@@ -193,4 +193,72 @@ struct ShiftReduce {
     }
 };
 
+// Closed forms of the trie for three and four leaves in increasing order.
+// Adjacent leaves a < b join at split_level(a, b); the highest adjacent split
+// is the root, and two adjacent pairs never share a split level when every
+// split between them is lower, so the maximum is unique.
+template <typename T>
+__device__ __forceinline__ T trie3(int l0, int l1, int l2, T v0, T v1, T v2)
+{
+    return split_level(l0, l1) < split_level(l1, l2) ? vadd(vadd(v0, v1), v2)
+                                                     : vadd(v0, vadd(v1, v2));
+}
+
+template <typename T>
+__device__ __forceinline__ T trie4(int l0, int l1, int l2, int l3, T v0, T v1, T v2, T v3)
+{
+    const int s01 = split_level(l0, l1), s12 = split_level(l1, l2), s23 = split_level(l2, l3);
+    if (s12 > s01 && s12 > s23)
+        return vadd(vadd(v0, v1), vadd(v2, v3));
+    if (s01 > s23)
+        return vadd(v0, s12 < s23 ? vadd(vadd(v1, v2), v3) : vadd(v1, vadd(v2, v3)));
+    return vadd(s01 < s12 ? vadd(vadd(v0, v1), v2) : vadd(v0, vadd(v1, v2)), v3);
+}
+
+// Orders two (leaf, value) pairs by leaf.
+template <typename T>
+__device__ __forceinline__ void leaf_cas(int &la, T &va, int &lb, T &vb)
+{
+    if (la > lb) {
+        const int l = la;
+        la = lb;
+        lb = l;
+        const T v = va;
+        va = vb;
+        vb = v;
+    }
+}
+
+// Trie value of n <= 32 leaves held one per lane (lane j < n holds the j-th
+// smallest leaf and its value); called by a full warp, result in lane 0.
+// Each round joins every adjacent pair of surviving subtrees whose split
+// level is the lowest present: such pairs are disjoint siblings, and a
+// subtree is represented by any of its leaves.
+template <typename T>
+__device__ __forceinline__ T warp_trie(int leaf, T v, int n)
+{
+    const int lane = threadIdx.x & 31;
+    bool alive = lane < n;
+    for (;;) {
+        const unsigned am = __ballot_sync(kFull, alive);
+        if ((am & (am - 1u)) == 0)
+            break;
+        const unsigned after = am & ~((2u << lane) - 1u);
+        const int nl = after ? __ffs(after) - 1 : lane;
+        const int kn = __shfl_sync(kFull, leaf, nl);
+        const T vn = __shfl_sync(kFull, v, nl);
+        const bool has = alive && after != 0u;
+        const int s = has ? split_level(leaf, kn) : 64;
+        const int smin = __reduce_min_sync(kFull, s);
+        const bool comb = has && s == smin;
+        if (comb)
+            v = vadd(v, vn);
+        const unsigned cm = __ballot_sync(kFull, comb);
+        const unsigned before = am & ((1u << lane) - 1u);
+        if (alive && before && ((cm >> (31 - __clz(before))) & 1u))
+            alive = false;
+    }
+    return v;
+}
+
 }  // namespace brm

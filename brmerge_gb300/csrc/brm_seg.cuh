@@ -419,8 +419,10 @@ __global__ void __launch_bounds__(256) k_split(CsrDev A, CsrDev B, PlanDev P)
 // ---------------------------------------------------------------------------
 // 3. segment kernel
 // ---------------------------------------------------------------------------
-constexpr int kLongRun = 32;  // runs longer than this are reduced in a separate pass
-constexpr int kLongMax = kSegCap / (kLongRun + 1) + 1;
+constexpr int kLongMin = 5;  // columns with this many products are reduced by warps
+constexpr int kLongMax = kSegCap / kLongMin + 1;
+constexpr int kSegPWords = kSegCap / 32;  // words of a bitmap over a segment's products
+static_assert(kSegCap % 32 == 0 && kSegPWords <= 96, "p-bitmap prefix: three words per lane");
 
 template <typename T>
 struct SegLayout {
@@ -442,6 +444,8 @@ struct SegLayout {
     static constexpr size_t o_ws = o_long + mid_a16(kLongMax * 2);
     static constexpr size_t o_misc = o_ws + mid_a16((NW + 1) * 8);
     static constexpr size_t bytes = o_misc + 64;
+    // per-warp p-bitmaps and their word prefixes live in cw once u is known
+    static_assert(NW * kSegPWords * 6 <= kSegCap * 4, "cw region holds the warp bitmaps");
 };
 
 template <typename T, bool UPPER>
@@ -699,23 +703,27 @@ __global__ void __launch_bounds__(kSegThreads) k_seg_numeric(CsrDev A, CsrDev B,
                 const int e1 = S[i0 + 1];
                 v = pleaf[e0] < pleaf[e1] ? vadd(pval[e0], pval[e1])   // left + right
                                           : vadd(pval[e1], pval[e0]);
-            } else if (len <= kLongRun) {
-                // insertion sort of the column's products by leaf, then the trie
-                for (int i = i0 + 1; i < i0 + len; i++) {
-                    const unsigned short e = S[i];
-                    const int key = pleaf[e];
-                    int j = i - 1;
-                    while (j >= i0 && pleaf[S[j]] > key) {
-                        S[j + 1] = S[j];
-                        j--;
-                    }
-                    S[j + 1] = e;
+            } else if (len <= 4) {
+                // sort the (leaf, value) pairs in registers, then the closed form
+                const int e1 = S[i0 + 1], e2 = S[i0 + 2];
+                int l0 = pleaf[e0], l1 = pleaf[e1], l2 = pleaf[e2];
+                T v0 = pval[e0], v1 = pval[e1], v2 = pval[e2];
+                if (len == 3) {
+                    leaf_cas(l0, v0, l1, v1);
+                    leaf_cas(l1, v1, l2, v2);
+                    leaf_cas(l0, v0, l1, v1);
+                    v = trie3(l0, l1, l2, v0, v1, v2);
+                } else {
+                    const int e3 = S[i0 + 3];
+                    int l3 = pleaf[e3];
+                    T v3 = pval[e3];
+                    leaf_cas(l0, v0, l1, v1);
+                    leaf_cas(l2, v2, l3, v3);
+                    leaf_cas(l0, v0, l2, v2);
+                    leaf_cas(l1, v1, l3, v3);
+                    leaf_cas(l1, v1, l2, v2);
+                    v = trie4(l0, l1, l2, l3, v0, v1, v2, v3);
                 }
-                ShiftReduce<T, 17> sr;
-                sr.init(pleaf[S[i0]], pval[S[i0]]);
-                for (int i = i0 + 1; i < i0 + len; i++)
-                    sr.push(pleaf[S[i]], pval[S[i]]);
-                v = sr.finish();
             } else {
                 const int li = atomicAdd(&misc[1], 1);
                 if (li < kLongMax)
@@ -726,30 +734,64 @@ __global__ void __launch_bounds__(kSegThreads) k_seg_numeric(CsrDev A, CsrDev B,
             cval[obase + u] = v;
         }
         __syncthreads();
-        // long columns: one warp each ranks the products by leaf (leaves of
-        // one column are distinct) into ia, then its first lane reduces
+        // columns with more than four products: one warp each puts them in
+        // leaf order (= staging order p, which it ranks with a bitmap over p)
+        // into ia, then reduces them across its lanes (or, beyond 32, in its
+        // first lane)
         const int nlong = min(misc[1], kLongMax);
-        for (int li = tid >> 5; li < nlong; li += NT / 32) {
-            const int lane = tid & 31;
-            const int u = longu[li];
-            const int i0 = ucnt[u], i1 = ucnt[u + 1];
-            for (int i = i0 + lane; i < i1; i += 32) {
-                const int key = pleaf[S[i]];
-                int r = 0;
-                for (int j = i0; j < i1; j++)
-                    r += pleaf[S[j]] < key ? 1 : 0;
-                ia[i0 + r] = S[i];
+        {
+            const int lane = tid & 31, wid = tid >> 5;
+            unsigned *bmp = cw + wid * kSegPWords;
+            unsigned short *wpre = (unsigned short *)(cw + L::NW * kSegPWords) + wid * kSegPWords;
+            const int nwp = (nprod + 31) >> 5;
+            for (int li = wid; li < nlong; li += L::NW) {
+                const int u = longu[li];
+                const int i0 = ucnt[u], i1 = ucnt[u + 1], len = i1 - i0;
+                for (int w = lane; w < nwp; w += 32)
+                    bmp[w] = 0;
+                __syncwarp();
+                for (int i = i0 + lane; i < i1; i += 32) {
+                    const int p = S[i];
+                    atomicOr(&bmp[p >> 5], 1u << (p & 31));
+                }
+                __syncwarp();
+                {
+                    const int w0 = lane * 3;
+                    const int c0 = w0 < nwp ? __popc(bmp[w0]) : 0;
+                    const int c1 = w0 + 1 < nwp ? __popc(bmp[w0 + 1]) : 0;
+                    const int c2 = w0 + 2 < nwp ? __popc(bmp[w0 + 2]) : 0;
+                    const int ex = warp_incl_scan(c0 + c1 + c2) - (c0 + c1 + c2);
+                    if (w0 < nwp)
+                        wpre[w0] = (unsigned short)ex;
+                    if (w0 + 1 < nwp)
+                        wpre[w0 + 1] = (unsigned short)(ex + c0);
+                    if (w0 + 2 < nwp)
+                        wpre[w0 + 2] = (unsigned short)(ex + c0 + c1);
+                }
+                __syncwarp();
+                for (int i = i0 + lane; i < i1; i += 32) {
+                    const int p = S[i];
+                    const int r = wpre[p >> 5] + __popc(bmp[p >> 5] & ((1u << (p & 31)) - 1u));
+                    ia[i0 + r] = (unsigned short)p;
+                }
+                __syncwarp();
+                if (len <= 32) {
+                    const int e = ia[i0 + (lane < len ? lane : 0)];
+                    const T r = warp_trie<T>(pleaf[e], pval[e], len);
+                    if (lane == 0) {
+                        ccol[obase + u] = d.c_lo + prc[e];
+                        cval[obase + u] = r;
+                    }
+                } else if (lane == 0) {
+                    ShiftReduce<T, 17> sr;
+                    sr.init(pleaf[ia[i0]], pval[ia[i0]]);
+                    for (int i = i0 + 1; i < i1; i++)
+                        sr.push(pleaf[ia[i]], pval[ia[i]]);
+                    ccol[obase + u] = d.c_lo + prc[ia[i0]];
+                    cval[obase + u] = sr.finish();
+                }
+                __syncwarp();
             }
-            __syncwarp();
-            if (lane == 0) {
-                ShiftReduce<T, 17> sr;
-                sr.init(pleaf[ia[i0]], pval[ia[i0]]);
-                for (int i = i0 + 1; i < i1; i++)
-                    sr.push(pleaf[ia[i]], pval[ia[i]]);
-                ccol[obase + u] = d.c_lo + prc[ia[i0]];
-                cval[obase + u] = sr.finish();
-            }
-            __syncwarp();
         }
         if (tid == 0) {
             // the segment must produce exactly its share of the row's columns
