@@ -11,6 +11,7 @@
 #include <cstring>
 #include <mutex>
 
+#include "brm_hostpool.h"
 #include "brm_kernels.h"
 #include "brmerge.h"
 
@@ -455,13 +456,14 @@ int host_call(bool upper, const int *arpt, const int *acol, const T *aval, const
         BRM_TRY(read_err(ctx));
         t_num1 = now_sec();
     }
-    int *crpt = (int *)std::malloc(4 * ((size_t)M + 1));
-    int *ccol = (int *)std::malloc(4 * (size_t)(cnnz > 0 ? cnnz : 1));
-    T *cval = (T *)std::malloc(sizeof(T) * (size_t)(cnnz > 0 ? cnnz : 1));
+    // result arrays: page-locked blocks from the host cache (released by brm_free)
+    int *crpt = (int *)brm::host_alloc(4 * ((size_t)M + 1));
+    int *ccol = (int *)brm::host_alloc(4 * (size_t)(cnnz > 0 ? cnnz : 1));
+    T *cval = (T *)brm::host_alloc(sizeof(T) * (size_t)(cnnz > 0 ? cnnz : 1));
     if (!crpt || !ccol || !cval) {
-        std::free(crpt);
-        std::free(ccol);
-        std::free(cval);
+        brm_free(crpt);
+        brm_free(ccol);
+        brm_free(cval);
         return BRM_ERR_ALLOC;
     }
     cudaError_t e1 = cudaMemcpyAsync(crpt, ctx->io_crpt.p, 4 * ((size_t)M + 1), cudaMemcpyDeviceToHost, s);
@@ -469,9 +471,9 @@ int host_call(bool upper, const int *arpt, const int *acol, const T *aval, const
     cudaError_t e3 = cudaMemcpyAsync(cval, ctx->io_cval.p, sizeof(T) * (size_t)cnnz, cudaMemcpyDeviceToHost, s);
     cudaError_t e4 = cudaStreamSynchronize(s);
     if (e1 != cudaSuccess || e2 != cudaSuccess || e3 != cudaSuccess || e4 != cudaSuccess) {
-        std::free(crpt);
-        std::free(ccol);
-        std::free(cval);
+        brm_free(crpt);
+        brm_free(ccol);
+        brm_free(cval);
         (void)cudaGetLastError();
         return BRM_ERR_CUDA;
     }
@@ -828,7 +830,13 @@ int brm_upper_f32(const int *arpt, const int *acol, const float *aval, const int
                             cnnz, nullptr, timing);
 }
 
-void brm_free(void *p) { std::free(p); }
+void brm_free(void *p)
+{
+    if (p && !brm::host_release(p))
+        std::free(p);
+}
+
+void brm_host_cache_release(void) { brm::host_trim(); }
 
 int brm_compute_flop(brm_context ctx, const brm_csr *A, const brm_csr *B, long long *products)
 {

@@ -78,6 +78,32 @@ def _ptr(a: np.ndarray):
     return a.ctypes.data_as(C.c_void_p)
 
 
+class _HostBlock:
+    """Owner of one array returned by a host drop-in; releases it with brm_free."""
+    __slots__ = ("_L", "_p")
+
+    def __init__(self, L, p):
+        self._L, self._p = L, p
+
+    def __del__(self):
+        if self._p:
+            self._L.brm_free(self._p)
+            self._p = None
+
+
+def _owned(L, ptr, n: int, ctype, dtype) -> np.ndarray:
+    """A numpy view of n elements at ptr that frees the block when collected."""
+    addr = C.cast(ptr, C.c_void_p).value
+    if not addr:
+        return np.zeros(n, dtype)
+    if n == 0:
+        L.brm_free(addr)
+        return np.zeros(0, dtype)
+    buf = (ctype * n).from_address(addr)
+    buf._owner = _HostBlock(L, addr)
+    return np.frombuffer(buf, dtype=dtype, count=n)
+
+
 def _host_call(name_f64: str, name_f32: str, A: CSR, B: CSR, C_out: CSR | None, timing, tcls):
     if A.N != B.M:
         raise ValueError(f"A.N ({A.N}) != B.M ({B.M})")
@@ -99,16 +125,12 @@ def _host_call(name_f64: str, name_f32: str, A: CSR, B: CSR, C_out: CSR | None, 
     st = fn(*[_ptr(a) for a in arrs], C.byref(crpt), C.byref(ccol), C.byref(cval),
             A.M, A.N, B.N, C.byref(cnnz), C.byref(tc))
     _native.check(st, name_f64)
-    try:
-        n = cnnz.value
-        rpt = np.ctypeslib.as_array(crpt, shape=(A.M + 1,)).copy()
-        col = np.ctypeslib.as_array(ccol, shape=(n,)).copy() if n else np.zeros(0, np.int32)
-        val = (np.ctypeslib.as_array(cval, shape=(n,)).copy() if n
-               else np.zeros(0, np.float64 if code == F64 else np.float32))
-    finally:
-        L.brm_free(C.cast(crpt, C.c_void_p))
-        L.brm_free(C.cast(ccol, C.c_void_p))
-        L.brm_free(C.cast(cval, C.c_void_p))
+    n = cnnz.value
+    # the result arrays stay where the library put them (page-locked host
+    # blocks); numpy views own them and hand them back through brm_free
+    rpt = _owned(L, crpt, A.M + 1, C.c_int, np.int32)
+    col = _owned(L, ccol, n, C.c_int, np.int32)
+    val = _owned(L, cval, n, vt, np.float64 if code == F64 else np.float32)
     if timing is not None:
         timing._load(tc)
     out = C_out if C_out is not None else CSR(0, 0, np.zeros(1, np.int32), np.zeros(0, np.int32),

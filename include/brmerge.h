@@ -138,9 +138,11 @@ int brm_device_free(brm_context ctx, void *p);
 /* ---- host drop-ins: the reference's argument order ------------------------ */
 
 /* brmerge_precise with host arrays (spgemm.h:468-471): A is M x K, B is
- * K x N.  *crpt (M+1), *ccol and *cval (cnnz) are malloc'ed by the callee;
- * release each with brm_free.  timing may be NULL.  Uses a process-wide
- * context on the current device. */
+ * K x N.  *crpt (M+1), *ccol and *cval (cnnz) are allocated by the callee
+ * (the reference allocates them with new[], spgemm.h:575-578) from a cache
+ * of page-locked host blocks, so the device-to-host copy runs at the link's
+ * bandwidth; release each with brm_free (never free()).  timing may be NULL.
+ * Uses a process-wide context on the current device. */
 int brm_precise(const int *arpt, const int *acol, const double *aval, const int *brpt,
                 const int *bcol, const double *bval, int **crpt, int **ccol, double **cval,
                 int M, int K, int N, int *cnnz, brm_precise_timing *timing);
@@ -153,7 +155,15 @@ int brm_precise_f32(const int *arpt, const int *acol, const float *aval, const i
 int brm_upper_f32(const int *arpt, const int *acol, const float *aval, const int *brpt,
                   const int *bcol, const float *bval, int **crpt, int **ccol, float **cval,
                   int M, int K, int N, int *cnnz, brm_upper_timing *timing);
+/* Releases an array returned by a host drop-in (its block goes back to the
+ * page-locked cache).  NULL is ignored. */
 void brm_free(void *p);
+
+/* Returns the cached page-locked blocks that no result holds to the driver.
+ * No counterpart in the reference (whose results are plain new[] arrays).
+ * The cache keeps at most BRM_HOST_CACHE_MB (environment, default 16384)
+ * MiB of unused blocks. */
+void brm_host_cache_release(void);
 
 /* ---- helpers ---------------------------------------------------------------- */
 

@@ -114,6 +114,34 @@ def test_host_drop_in_matches_device(ctx):
     assert_same_csr(C1, gpu_precise(ctx, A, A), "host vs device")
 
 
+def test_host_results_are_independent_blocks(oracle_mod):
+    """Results held at the same time never share a cached host block, and a
+    released block is reused only after its result is gone."""
+    import gc
+    from brmerge_gb300 import _native
+    A = brm.gen_rmat(12, int(2.35 * 4096), seed=21)
+    B = brm.gen_lognormal(4096, 4096, seed=22)
+    R1, R2 = oracle_mod.precise(A, A), oracle_mod.precise(A, B)
+    held = [brm.brmerge_precise(A, A), brm.brmerge_precise(A, B), brm.brmerge_precise(A, A)]
+    ptrs = {a.ctypes.data for C in held for a in (C.rpt, C.col, C.val)}
+    assert len(ptrs) == 9
+    assert_same_csr(held[0], R1, "held 0")
+    assert_same_csr(held[1], R2, "held 1")
+    assert_same_csr(held[2], R1, "held 2")
+    view = held[1].val[5:50]  # a slice keeps its block alive
+    expect = view.copy()
+    del held
+    gc.collect()
+    again = [brm.brmerge_precise(A, B) for _ in range(2)]
+    assert np.array_equal(view, expect)
+    for C in again:
+        assert_same_csr(C, R2, "after release")
+    del again, view
+    gc.collect()
+    _native.lib().brm_host_cache_release()
+    assert_same_csr(brm.brmerge_precise(A, A), R1, "after cache release")
+
+
 # ---------------------------------------------------------------------------
 # edge cases
 # ---------------------------------------------------------------------------
