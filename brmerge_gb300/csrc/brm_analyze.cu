@@ -72,26 +72,45 @@ __global__ void __launch_bounds__(kAnaThreads) k_analyze(CsrDev A, CsrDev B, Pla
         nl = warp_sum(nl);
         leaf = warp_max(leaf);
         bad = __any_sync(kFull, bad);
+        const bool ovf = f > INT_MAX;
+        if (ovf)
+            f = INT_MAX;
+        // row class (f, nl, a0, a1 are warp-uniform)
+        int bin;
+        if (f == 0)
+            bin = kBinEmpty;
+        else if (nl == 1)
+            bin = kBinCopy;
+        else if (f <= kWarpMaxFlop)
+            bin = kBinWarp;
+        else if (f <= kMidFlop && 2 * nl <= kMidFlop && a1 - a0 <= kMidMaxK)
+            bin = kBinBatch;
+        else if (a1 - a0 <= kSegMaxK)
+            bin = kBinHeavy;  // segmented (brm_seg.cuh)
+        else
+            bin = kBinMid;    // row CTA / spill path
+        if (bin == kBinHeavy) {
+            // column range of the row for the segment planning: the first and
+            // last column of every nonempty list
+            int mn = INT_MAX, mx = -1;
+            for (int j = a0 + lane; j < a1; j += 32) {
+                const int len = P.alen[j];
+                if (len > 0) {
+                    const int bs = P.abs[j];
+                    mn = min(mn, B.col[bs]);
+                    mx = max(mx, B.col[bs + len - 1]);
+                }
+            }
+            mn = warp_min(mn);
+            mx = warp_max(mx);
+            if (lane == 0)
+                P.crange[row] = make_int2(mn, mx);
+        }
         if (lane == 0) {
             if (bad)
                 atomicOr(&P.cnt->err, kErrBadInput);
-            if (f > INT_MAX) {
+            if (ovf)
                 atomicOr(&P.cnt->err, kErrOverflow);
-                f = INT_MAX;
-            }
-            int bin;
-            if (f == 0)
-                bin = kBinEmpty;
-            else if (nl == 1)
-                bin = kBinCopy;
-            else if (f <= kWarpMaxFlop)
-                bin = kBinWarp;
-            else if (f <= kMidFlop && 2 * nl <= kMidFlop && a1 - a0 <= kMidMaxK)
-                bin = kBinBatch;
-            else if (a1 - a0 <= kSegMaxK)
-                bin = kBinHeavy;  // segmented (brm_seg.cuh)
-            else
-                bin = kBinMid;    // row CTA / spill path
             P.flop[row] = (int)f;
             if (bin == kBinHeavy)
                 P.seg_base[row] = atomicAdd(&P.cnt->seg_cap, seg_bound(f, B.N));
@@ -103,8 +122,15 @@ __global__ void __launch_bounds__(kAnaThreads) k_analyze(CsrDev A, CsrDev B, Pla
                 P.nnz[row] = (int)f;
                 P.copy_leaf[row] = leaf;
             }
+            if (bin == kBinHeavy && f > kHugeFlop) {
+                // the planning takes these first, so the longest rows do not
+                // start last and finish after every other block
+                const int h = atomicAdd(&P.cnt->n_huge, 1);
+                P.rows[(size_t)kBinHeavy * M + (M - 1 - h)] = row;
+                bin = -2;
+            }
             s_bin[slot] = bin;
-            s_idx[slot] = (bin == kBinEmpty || bin == kBinBatch) ? 0 : atomicAdd(&s_cnt[bin], 1);
+            s_idx[slot] = (bin < 0 || bin == kBinEmpty || bin == kBinBatch) ? 0 : atomicAdd(&s_cnt[bin], 1);
             wflop += (unsigned long long)f;
             wmaxk = max(wmaxk, a1 - a0);
         }

@@ -130,6 +130,7 @@ size_t workspace_bytes(int M)
     b += a256(4 * (m + 1));                 // batch_start
     b += a256(8 * m);                       // seg_base
     b += a256(4 * m);                       // seg_n
+    b += a256(8 * m);                       // crange
     b += a256(sizeof(brm::Counters));
     b += a256(brm::scan_tmp_bytes((int)m + 1));
     b += a256(4);                           // bad row
@@ -170,6 +171,7 @@ int ensure_workspace(brm_context ctx, int M)
     P.batch_start = (int *)take(4 * (m + 1));
     P.seg_base = (unsigned long long *)take(8 * m);
     P.seg_n = (int *)take(4 * m);
+    P.crange = (int2 *)take(8 * m);
     P.cnt = (brm::Counters *)take(sizeof(brm::Counters));
     ctx->scan_tmp = take(brm::scan_tmp_bytes((int)m + 1));
     ctx->d_bad = (int *)take(4);

@@ -229,6 +229,82 @@ __device__ __forceinline__ void leaf_cas(int &la, T &va, int &lb, T &vb)
     }
 }
 
+// Sorts eight (leaf, value) pairs by leaf in registers (Batcher's odd-even
+// merge network, 19 comparators).
+template <typename T>
+__device__ __forceinline__ void leaf_sort8(int (&l)[8], T (&v)[8])
+{
+    leaf_cas(l[0], v[0], l[1], v[1]);
+    leaf_cas(l[2], v[2], l[3], v[3]);
+    leaf_cas(l[4], v[4], l[5], v[5]);
+    leaf_cas(l[6], v[6], l[7], v[7]);
+    leaf_cas(l[0], v[0], l[2], v[2]);
+    leaf_cas(l[1], v[1], l[3], v[3]);
+    leaf_cas(l[4], v[4], l[6], v[6]);
+    leaf_cas(l[5], v[5], l[7], v[7]);
+    leaf_cas(l[1], v[1], l[2], v[2]);
+    leaf_cas(l[5], v[5], l[6], v[6]);
+    leaf_cas(l[0], v[0], l[4], v[4]);
+    leaf_cas(l[1], v[1], l[5], v[5]);
+    leaf_cas(l[2], v[2], l[6], v[6]);
+    leaf_cas(l[3], v[3], l[7], v[7]);
+    leaf_cas(l[2], v[2], l[4], v[4]);
+    leaf_cas(l[3], v[3], l[5], v[5]);
+    leaf_cas(l[1], v[1], l[2], v[2]);
+    leaf_cas(l[3], v[3], l[4], v[4]);
+    leaf_cas(l[5], v[5], l[6], v[6]);
+}
+
+// ShiftReduce with its stack in registers for at most D leaves: the entry
+// below the top is always st[0], so every access uses a fixed index (a push
+// shifts the stack down, a reduction shifts it up).
+template <typename T, int D>
+struct RegShiftReduce {
+    T st[D - 1];
+    int op[D - 1];  // op[i]: split level between st[i] and the entry above it
+    int nb;         // entries below the top
+    T cur;          // top of the stack
+    int last;
+    __device__ __forceinline__ void init(int leaf, T v)
+    {
+        nb = 0;
+        cur = v;
+        last = leaf;
+    }
+    __device__ __forceinline__ void pop()
+    {
+        cur = vadd(st[0], cur);
+#pragma unroll
+        for (int i = 0; i < D - 2; i++) {
+            st[i] = st[i + 1];
+            op[i] = op[i + 1];
+        }
+        nb--;
+    }
+    __device__ __forceinline__ void push(int leaf, T v)
+    {
+        const int s = split_level(last, leaf);
+        while (nb > 0 && op[0] < s)
+            pop();
+#pragma unroll
+        for (int i = D - 2; i > 0; i--) {
+            st[i] = st[i - 1];
+            op[i] = op[i - 1];
+        }
+        st[0] = cur;
+        op[0] = s;
+        nb++;
+        cur = v;
+        last = leaf;
+    }
+    __device__ __forceinline__ T finish()
+    {
+        while (nb > 0)
+            pop();
+        return cur;
+    }
+};
+
 // Trie value of n <= 32 leaves held one per lane (lane j < n holds the j-th
 // smallest leaf and its value); called by a full warp, result in lane 0.
 // Each round joins every adjacent pair of surviving subtrees whose split

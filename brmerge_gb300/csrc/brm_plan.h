@@ -7,6 +7,8 @@
 
 #include <cstdint>
 
+#include <vector_types.h>
+
 namespace brm {
 
 // Tuning constants of the row kernels.
@@ -41,6 +43,7 @@ constexpr int kSegThreads = 256;
 constexpr int kSegCap = 3072;
 constexpr int kSegCut = kSegCap / 2;      // target products between cuts
 constexpr int kSegMaxK = 65535;           // leaf index stored in 16 bits
+constexpr int kHugeFlop = 16 * kSegCap;   // heavy rows planned first (longest first)
 constexpr int kPlanWordsLog2 = 13;
 constexpr int kPlanWords = 1 << kPlanWordsLog2;  // bitmap words per planning chunk
 constexpr int kPlanBits = kPlanWords * 32;       // 2^18 columns
@@ -86,7 +89,8 @@ struct Counters {
     unsigned long long table_cap;  // split-table entries reserved by the planning
     int n_seg;         // segments written by the planning
     int work_plan;     // dynamic row counter of the heavy-row planning
-    int pad[2];
+    int n_huge;        // heavy rows above kHugeFlop products (listed from the end)
+    int pad;
 };
 
 // Descriptor slots reserved for a heavy row with F products: the cut rule
@@ -129,6 +133,7 @@ struct PlanDev {
     int *batch_start;      // [M+1] first row of each mid batch
     unsigned long long *seg_base;  // [M] first descriptor slot of each heavy row
     int *seg_n;            // [M] segments of each heavy row (0: not segmented)
+    int2 *crange;          // [M] smallest and largest column of each heavy row (x > y: none)
     SegDesc *seg;          // [Counters::seg_cap] segment descriptors (numbered per row)
     int *seg_list;         // [Counters::seg_cap] descriptor slot of every written segment
     int *split;            // [Counters::table_cap] split table (numeric phase)

@@ -36,22 +36,31 @@
 namespace brm {
 
 constexpr int kPlanThreads = 512;
-constexpr int kDenseMax = 128;  // dense words per planning chunk with per-column counts
+// Segment cuts are placed at planning-group boundaries (kPlanGroupBits
+// columns); a group with more than kSegCut products gets per-column counts
+// (at most kDenseGroups such groups per chunk).
+constexpr int kPlanGroupLog2 = 7;
+constexpr int kPlanGroupBits = 1 << kPlanGroupLog2;      // 128 columns
+constexpr int kPlanGroupWords = kPlanGroupBits / 32;     // 4 bitmap words
+constexpr int kPlanGroups = kPlanBits / kPlanGroupBits;  // 2048 per chunk
+constexpr int kDenseGroups = 32;
 
 struct PlanLayout {
     static constexpr size_t o_bm = 0;
     static constexpr size_t o_hist = o_bm + kPlanWords * 4;
-    static constexpr size_t o_dix = o_hist + kPlanWords * 4;
-    static constexpr size_t o_ccnt = o_dix + kPlanWords * 2;
-    static constexpr size_t o_lst = o_ccnt + kDenseMax * 32 * 4;
+    static constexpr size_t o_gpop = o_hist + kPlanGroups * 4;
+    static constexpr size_t o_dix = o_gpop + kPlanGroups * 2;
+    static constexpr size_t o_ccnt = o_dix + kPlanGroups * 2;
+    static constexpr size_t o_lst = o_ccnt + kDenseGroups * kPlanGroupBits * 4;
     static constexpr size_t o_loffs = o_lst + (kPlanThreads + 1) * 4;
     static constexpr size_t o_ws = o_loffs + (kPlanThreads + 1) * 4 + 8;
     static constexpr size_t o_misc = o_ws + (kPlanThreads / 32 + 1) * 8;
     static constexpr size_t bytes = o_misc + 64;
 };
 
-// Calls f(rc) for every product of the row whose column lies in [lo, chi),
-// rc = column - lo, with the products split evenly over the block: the lists
+// Calls f(rc) for every product of the row, rc = column - base; with clip,
+// only for the products whose column lies in [lo, chi) (each list is cut by
+// binary search).  The products are split evenly over the block: the lists
 // are taken NT at a time, their lengths scanned, and every thread walks a
 // contiguous share of the chunk's products (a single very long list of a
 // power-law row is shared by all threads instead of one group).  A thread
@@ -59,7 +68,7 @@ struct PlanLayout {
 // lst/loffs are NT+1 ints of shared scratch.
 template <int NT, typename Fn>
 __device__ __forceinline__ void plan_products(const PlanDev &P, const int *__restrict__ bcol,
-                                              int a0, int k, bool multi, int lo, int chi,
+                                              int a0, int k, bool clip, int lo, int chi, int base,
                                               int *lst, int *loffs, long long *ws, Fn f)
 {
     const int tid = threadIdx.x;
@@ -69,7 +78,7 @@ __device__ __forceinline__ void plan_products(const PlanDev &P, const int *__res
         if (l < k) {
             len = P.alen[a0 + l];
             s = P.abs[a0 + l];
-            if (multi && len > 0) {
+            if (clip && len > 0) {
                 int e = s + len;
                 s = lower_bound_idx(bcol, s, e, lo);
                 e = lower_bound_idx(bcol, s, e, chi);
@@ -110,43 +119,46 @@ __device__ __forceinline__ void plan_products(const PlanDev &P, const int *__res
 #pragma unroll
                 for (int i = 0; i < kGatherBatch; i++)
                     if (i < m)
-                        f(c[i] - lo);
+                        f(c[i] - base);
             }
         }
         __syncthreads();
     }
 }
 
-// Walks the segment starts of planning word w (chunk-relative) in column
-// order and calls f(column_in_word, product_prefix, distinct_prefix) for
-// each.  `run` packs (products << 32 | distinct columns) before word w and
-// ph is the product count of word w-1.  A word with more than kSegCut
+// Walks the segment starts of planning group g (chunk-relative) in column
+// order and calls f(column_in_group, product_prefix, distinct_prefix) for
+// each.  `run` packs (products << 32 | distinct columns) before group g and
+// ph is the product count of group g-1.  A group with more than kSegCut
 // products is always cut before and after; inside it, a new segment starts
-// at a column when the running product count would exceed kSegCut.
+// at a column when the running product count would exceed kSegCut.  Any
+// other group starts a segment when the group before it crossed a multiple
+// of kSegCut, so a segment holds less than 2 * kSegCut = kSegCap products.
 template <typename Fn>
-__device__ __forceinline__ void plan_word_starts(int w, unsigned h, unsigned ph,
-                                                 unsigned long long run, unsigned bits,
-                                                 const unsigned *ccnt, Fn f)
+__device__ __forceinline__ void plan_group_starts(int g, unsigned h, unsigned ph,
+                                                  unsigned long long run, const unsigned *ccnt,
+                                                  Fn f)
 {
     const unsigned pe = (unsigned)(run >> 32);
     const unsigned ue = (unsigned)(run & 0xffffffffu);
     if (h > (unsigned)kSegCut) {
         f(0, pe, ue);
-        unsigned acc = 0, pp = pe;
-        for (int c = 0; c < 32; c++) {
+        unsigned acc = 0, pp = pe, uu = ue;
+        for (int c = 0; c < kPlanGroupBits; c++) {
             const unsigned cc = ccnt[c];
             if (cc == 0)
                 continue;
             if (acc > 0 && acc + cc > (unsigned)kSegCut) {
-                f(c, pp, ue + __popc(bits & ((1u << c) - 1u)));
+                f(c, pp, uu);
                 acc = 0;
             }
             acc += cc;
             pp += cc;
+            uu++;  // a column with products is one distinct column
         }
         return;
     }
-    const bool start = (w == 0) || ph > (unsigned)kSegCut || (pe / kSegCut) != ((pe - ph) / kSegCut);
+    const bool start = (g == 0) || ph > (unsigned)kSegCut || (pe / kSegCut) != ((pe - ph) / kSegCut);
     if (start)
         f(0, pe, ue);
 }
@@ -161,6 +173,7 @@ __global__ void __launch_bounds__(kPlanThreads) k_heavy_plan(CsrDev A, CsrDev B,
     extern __shared__ __align__(16) unsigned char smem[];
     unsigned *bm = (unsigned *)(smem + PlanLayout::o_bm);
     unsigned *hist = (unsigned *)(smem + PlanLayout::o_hist);
+    unsigned short *gpop = (unsigned short *)(smem + PlanLayout::o_gpop);
     unsigned short *dix = (unsigned short *)(smem + PlanLayout::o_dix);
     unsigned *ccnt = (unsigned *)(smem + PlanLayout::o_ccnt);
     int *lst = (int *)(smem + PlanLayout::o_lst);
@@ -169,9 +182,15 @@ __global__ void __launch_bounds__(kPlanThreads) k_heavy_plan(CsrDev A, CsrDev B,
     int *misc = (int *)(smem + PlanLayout::o_misc);
     const int tid = threadIdx.x;
     const int M = A.M;
-    const int nrows = P.cnt->bin_count[kBinHeavy];
+    // rows above kHugeFlop products sit at the end of the list; take them first
+    const int nhuge = P.cnt->n_huge;
+    const int nrows = P.cnt->bin_count[kBinHeavy] + nhuge;
     const int *rows = P.rows + (size_t)kBinHeavy * M;
     const int *__restrict__ bcol = B.col;
+    for (int i = tid; i < kPlanWords; i += NT)
+        bm[i] = 0;
+    for (int i = tid; i < kPlanGroups; i += NT)
+        hist[i] = 0;
     for (;;) {
         if (tid == 0)
             misc[0] = atomicAdd(&P.cnt->work_plan, 1);
@@ -180,23 +199,14 @@ __global__ void __launch_bounds__(kPlanThreads) k_heavy_plan(CsrDev A, CsrDev B,
         __syncthreads();
         if (item >= nrows)
             break;
-        const int row = rows[item];
+        const int row = item < nhuge ? rows[M - 1 - item] : rows[item - nhuge];
         const int a0 = A.rpt[row];
         const int k = A.rpt[row + 1] - a0;
         const long long F = P.flop[row];
         const unsigned long long base = P.seg_base[row];
         const unsigned long long bound = seg_bound(F, B.N);
-        int mn = INT_MAX, mx = -1;
-        for (int l = tid; l < k; l += NT) {
-            const int len = P.alen[a0 + l];
-            if (len > 0) {
-                const int s = P.abs[a0 + l];
-                mn = min(mn, bcol[s]);
-                mx = max(mx, bcol[s + len - 1]);
-            }
-        }
-        mn = (int)block_min<NT, long long>(mn, ws);
-        mx = (int)block_max<NT, long long>(mx, ws);
+        const int2 cr = P.crange[row];  // written by the analysis
+        const int mn = cr.x, mx = cr.y;
         if (mx < 0 || mn < 0 || mx >= B.N) {
             if (tid == 0) {
                 if (mx >= 0)
@@ -214,70 +224,96 @@ __global__ void __launch_bounds__(kPlanThreads) k_heavy_plan(CsrDev A, CsrDev B,
             const int lo = (int)clo;
             const int chi = (int)min((long long)mx + 1, clo + kPlanBits);
             const int span = chi - lo;
-            const int nw = (span + 31) >> 5;
-            for (int i = tid; i < nw; i += NT) {
-                bm[i] = 0;
-                hist[i] = 0;
+            const int ng = (span + kPlanGroupBits - 1) >> kPlanGroupLog2;
+            // bm and hist are zero here: cleared at the start and after every chunk
+            if (tid == 0) {
+                misc[4] = INT_MAX;  // first dense group
+                misc[5] = -1;       // last dense group
             }
             __syncthreads();
             // pass over the chunk's products: column bitmap and products per
-            // word.  A thread's products are column-sorted within each list,
-            // so runs in one word are gathered in registers and flushed once.
+            // group.  A thread's products are column-sorted within each list,
+            // so runs in one word (group) are gathered in registers and
+            // flushed once.
             bool bad = false;
-            unsigned run_w = 0, run_b = 0, run_n = 0;
-            plan_products<NT>(P, bcol, a0, k, multi, lo, chi, lst, loffs, ws, [&](int rc) {
+            unsigned run_w = 0xffffffffu, run_b = 0, run_g = 0xffffffffu, run_n = 0;
+            plan_products<NT>(P, bcol, a0, k, multi, lo, chi, lo, lst, loffs, ws, [&](int rc) {
                 if ((unsigned)rc >= (unsigned)span) {
                     bad = true;
                     return;
                 }
                 const unsigned w = (unsigned)rc >> 5;
                 if (w != run_w) {
-                    if (run_n) {
+                    if (run_b)
                         atomicOr(&bm[run_w], run_b);
-                        atomicAdd(&hist[run_w], run_n);
-                    }
                     run_w = w;
                     run_b = 0;
-                    run_n = 0;
                 }
                 run_b |= 1u << (rc & 31);
+                const unsigned g = (unsigned)rc >> kPlanGroupLog2;
+                if (g != run_g) {
+                    if (run_n)
+                        atomicAdd(&hist[run_g], run_n);
+                    run_g = g;
+                    run_n = 0;
+                }
                 run_n++;
             });
-            if (run_n) {
+            if (run_b)
                 atomicOr(&bm[run_w], run_b);
-                atomicAdd(&hist[run_w], run_n);
-            }
+            if (run_n)
+                atomicAdd(&hist[run_g], run_n);
             if (bad)
                 atomicOr(&P.cnt->err, kErrBadInput);
             __syncthreads();
-            const int wpt = (nw + NT - 1) / NT;
-            const int w0 = min(tid * wpt, nw), w1 = min(w0 + wpt, nw);
-            // dense words get per-column product counts (second pass)
-            int nd_local = 0;
+            const int gpt = (ng + NT - 1) / NT;
+            const int g0 = min(tid * gpt, ng), g1 = min(g0 + gpt, ng);
+            // distinct columns per group; dense groups get per-column counts
+            int nd_local = 0, dlo = INT_MAX, dhi = -1;
             unsigned long long sp = 0;
-            for (int w = w0; w < w1; w++) {
-                const unsigned h = hist[w];
-                nd_local += h > (unsigned)kSegCut ? 1 : 0;
-                sp += ((unsigned long long)h << 32) | (unsigned)__popc(bm[w]);
+            for (int g = g0; g < g1; g++) {
+                const unsigned h = hist[g];
+                int pc = 0;
+#pragma unroll
+                for (int q = 0; q < kPlanGroupWords; q++)
+                    pc += __popc(bm[g * kPlanGroupWords + q]);
+                gpop[g] = (unsigned short)pc;
+                if (h > (unsigned)kSegCut) {
+                    nd_local++;
+                    dlo = min(dlo, g);
+                    dhi = g;
+                }
+                sp += ((unsigned long long)h << 32) | (unsigned)pc;
+            }
+            if (nd_local) {
+                atomicMin(&misc[4], dlo);
+                atomicMax(&misc[5], dhi);
             }
             long long ndt;
             int dx = (int)block_excl_scan<NT, long long>(nd_local, ws, &ndt);
             const int nd = (int)ndt;
-            if (nd > kDenseMax)
+            if (nd > kDenseGroups)
                 fail = true;  // uniform
             if (!fail && nd > 0) {
-                for (int w = w0; w < w1; w++)
-                    if (hist[w] > (unsigned)kSegCut)
-                        dix[w] = (unsigned short)dx++;
-                for (int i = tid; i < nd * 32; i += NT)
+                for (int g = g0; g < g1; g++)
+                    if (hist[g] > (unsigned)kSegCut)
+                        dix[g] = (unsigned short)dx++;
+                for (int i = tid; i < nd * kPlanGroupBits; i += NT)
                     ccnt[i] = 0;
                 __syncthreads();
-                plan_products<NT>(P, bcol, a0, k, multi, lo, chi, lst, loffs, ws, [&](int rc) {
-                    if ((unsigned)rc < (unsigned)span && hist[rc >> 5] > (unsigned)kSegCut)
-                        atomicAdd(&ccnt[dix[rc >> 5] * 32 + (rc & 31)], 1u);
+                // only the columns from the first to the last dense group
+                const int dlo_c = lo + kPlanGroupBits * misc[4];
+                const int dhi_c = (int)min((long long)chi,
+                                           (long long)lo + (long long)kPlanGroupBits * (misc[5] + 1));
+                plan_products<NT>(P, bcol, a0, k, true, dlo_c, dhi_c, lo, lst, loffs, ws, [&](int rc) {
+                    if ((unsigned)rc < (unsigned)span) {
+                        const int g = rc >> kPlanGroupLog2;
+                        if (hist[g] > (unsigned)kSegCut)
+                            atomicAdd(&ccnt[dix[g] * kPlanGroupBits + (rc & (kPlanGroupBits - 1))], 1u);
+                    }
                 });
                 bool big = false;
-                for (int i = tid; i < nd * 32; i += NT)
+                for (int i = tid; i < nd * kPlanGroupBits; i += NT)
                     big |= ccnt[i] > (unsigned)kSegCap;
                 fail = __syncthreads_or(big) != 0;
             }
@@ -288,13 +324,13 @@ __global__ void __launch_bounds__(kPlanThreads) k_heavy_plan(CsrDev A, CsrDev B,
             int nstart = 0;
             if (!fail) {
                 unsigned long long run = ex;
-                unsigned ph = (w0 > 0 && w0 < nw) ? hist[w0 - 1] : 0u;
-                for (int w = w0; w < w1; w++) {
-                    const unsigned h = hist[w];
-                    plan_word_starts(w, h, ph, run, bm[w],
-                                     h > (unsigned)kSegCut ? ccnt + dix[w] * 32 : ccnt,
-                                     [&](int, unsigned, unsigned) { nstart++; });
-                    run += ((unsigned long long)h << 32) | (unsigned)__popc(bm[w]);
+                unsigned ph = (g0 > 0 && g0 < ng) ? hist[g0 - 1] : 0u;
+                for (int g = g0; g < g1; g++) {
+                    const unsigned h = hist[g];
+                    plan_group_starts(g, h, ph, run,
+                                      h > (unsigned)kSegCut ? ccnt + dix[g] * kPlanGroupBits : ccnt,
+                                      [&](int, unsigned, unsigned) { nstart++; });
+                    run += ((unsigned long long)h << 32) | (unsigned)gpop[g];
                     ph = h;
                 }
             }
@@ -306,31 +342,44 @@ __global__ void __launch_bounds__(kPlanThreads) k_heavy_plan(CsrDev A, CsrDev B,
             u_run += (long long)((unsigned long long)tot & 0xffffffffull);
             if (fail) {
                 __syncthreads();
+                for (int g = g0; g < g1; g++) {
+                    hist[g] = 0;
+#pragma unroll
+                    for (int q = 0; q < kPlanGroupWords; q++)
+                        bm[g * kPlanGroupWords + q] = 0;
+                }
+                __syncthreads();
                 continue;  // keep counting distinct columns; the row takes the spill path
             }
             // write the chunk's segments: c_lo, u_off and the product prefix
             {
                 unsigned long long run = ex;
-                unsigned ph = (w0 > 0 && w0 < nw) ? hist[w0 - 1] : 0u;
+                unsigned ph = (g0 > 0 && g0 < ng) ? hist[g0 - 1] : 0u;
                 int r = sx;
-                for (int w = w0; w < w1; w++) {
-                    const unsigned h = hist[w];
-                    plan_word_starts(w, h, ph, run, bm[w],
-                                     h > (unsigned)kSegCut ? ccnt + dix[w] * 32 : ccnt,
-                                     [&](int c, unsigned pe, unsigned ue) {
-                                         SegDesc &d = P.seg[base + nseg + r];
-                                         d.row = row;
-                                         d.c_lo = lo + 32 * w + c;
-                                         d.u_off = (int)(u_chunk + (long long)ue);
-                                         d.bidx = nseg + r;
-                                         d.nprod = (int)pe;  // prefix; a count below
-                                         r++;
-                                     });
-                    run += ((unsigned long long)h << 32) | (unsigned)__popc(bm[w]);
+                for (int g = g0; g < g1; g++) {
+                    const unsigned h = hist[g];
+                    plan_group_starts(g, h, ph, run,
+                                      h > (unsigned)kSegCut ? ccnt + dix[g] * kPlanGroupBits : ccnt,
+                                      [&](int c, unsigned pe, unsigned ue) {
+                                          SegDesc &d = P.seg[base + nseg + r];
+                                          d.row = row;
+                                          d.c_lo = lo + kPlanGroupBits * g + c;
+                                          d.u_off = (int)(u_chunk + (long long)ue);
+                                          d.bidx = nseg + r;
+                                          d.nprod = (int)pe;  // prefix; a count below
+                                          r++;
+                                      });
+                    run += ((unsigned long long)h << 32) | (unsigned)gpop[g];
                     ph = h;
                 }
             }
             __syncthreads();  // descriptors of this chunk visible to the block
+            for (int g = g0; g < g1; g++) {
+                hist[g] = 0;
+#pragma unroll
+                for (int q = 0; q < kPlanGroupWords; q++)
+                    bm[g * kPlanGroupWords + q] = 0;
+            }
             // c_hi and product count of each segment: read every neighbour
             // first, then write (rounds of NT segments)
             const int ctot_prod = (int)((unsigned long long)tot >> 32);
@@ -419,7 +468,7 @@ __global__ void __launch_bounds__(256) k_split(CsrDev A, CsrDev B, PlanDev P)
 // ---------------------------------------------------------------------------
 // 3. segment kernel
 // ---------------------------------------------------------------------------
-constexpr int kLongMin = 5;  // columns with this many products are reduced by warps
+constexpr int kLongMin = 9;  // columns with this many products are reduced by warps
 constexpr int kLongMax = kSegCap / kLongMin + 1;
 constexpr int kSegPWords = kSegCap / 32;  // words of a bitmap over a segment's products
 static_assert(kSegCap % 32 == 0 && kSegPWords <= 96, "p-bitmap prefix: three words per lane");
@@ -724,6 +773,29 @@ __global__ void __launch_bounds__(kSegThreads) k_seg_numeric(CsrDev A, CsrDev B,
                     leaf_cas(l1, v1, l2, v2);
                     v = trie4(l0, l1, l2, l3, v0, v1, v2, v3);
                 }
+            } else if (len <= 8) {
+                // sorting network and a register stack
+                int l8[8];
+                T v8[8];
+#pragma unroll
+                for (int j = 0; j < 8; j++) {
+                    if (j < len) {
+                        const int e = S[i0 + j];
+                        l8[j] = pleaf[e];
+                        v8[j] = pval[e];
+                    } else {
+                        l8[j] = INT_MAX;
+                        v8[j] = T(0);
+                    }
+                }
+                leaf_sort8(l8, v8);
+                RegShiftReduce<T, 8> sr;
+                sr.init(l8[0], v8[0]);
+#pragma unroll
+                for (int j = 1; j < 8; j++)
+                    if (j < len)
+                        sr.push(l8[j], v8[j]);
+                v = sr.finish();
             } else {
                 const int li = atomicAdd(&misc[1], 1);
                 if (li < kLongMax)
@@ -734,7 +806,7 @@ __global__ void __launch_bounds__(kSegThreads) k_seg_numeric(CsrDev A, CsrDev B,
             cval[obase + u] = v;
         }
         __syncthreads();
-        // columns with more than four products: one warp each puts them in
+        // columns with more than eight products: one warp each puts them in
         // leaf order (= staging order p, which it ranks with a bitmap over p)
         // into ia, then reduces them across its lanes (or, beyond 32, in its
         // first lane)
