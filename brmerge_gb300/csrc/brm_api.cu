@@ -5,6 +5,7 @@
 // the context's stream.  The only host synchronisations are the ones the
 // interface needs: nnz(C) after the symbolic phase (the caller allocates C),
 // and the error word after the numeric phase.
+#include <algorithm>
 #include <chrono>
 #include <climits>
 #include <cstdlib>
@@ -23,6 +24,7 @@ struct DevBuf {
 };
 
 constexpr int kNumEvents = 12;
+constexpr long long kLongElems = 16ll << 20;  // products in the long-column scratch
 
 }  // namespace
 
@@ -42,8 +44,9 @@ struct brm_context_s {
     int *h_bad = nullptr;            // pinned
     // per-A-entry list metadata (B-row start and length)
     DevBuf ameta;
-    // heavy-row segments: descriptors + written list, and the split table
-    DevBuf segbuf, splitbuf;
+    // heavy-row segments: descriptors + written list, the split table and the
+    // long-column scratch of the column reducer
+    DevBuf segbuf, splitbuf, longbuf;
     // spill scratch
     DevBuf spill;
     // Upper upper-bound buffer
@@ -321,6 +324,8 @@ bool plan_matches(brm_context ctx, const brm_csr *A, const brm_csr *B)
            ctx->b_col == B->col && ctx->pM == A->M && ctx->pK == A->N && ctx->pN == B->N;
 }
 
+size_t vsize(brm_dtype d) { return d == BRM_F64 ? 8 : 4; }
+
 int numeric_launch(brm_context ctx, brm_dtype dtype, bool upper, const brm_csr *A,
                    const brm_csr *B, const int *crpt, int *ccol, void *cval)
 {
@@ -333,6 +338,22 @@ int numeric_launch(brm_context ctx, brm_dtype dtype, bool upper, const brm_csr *
     BRM_TRY(grow(ctx->splitbuf, ((size_t)ctx->h_cnt->table_cap + 1) * sizeof(int)));
     P.split = (int *)ctx->splitbuf.p;
     ctx->plan.split = P.split;
+    {
+        // long-column scratch: at most kLongElems products (columns beyond it
+        // are reduced inside the segment kernel)
+        const long long elems = std::min<long long>((long long)ctx->h_cnt->total_flop, kLongElems);
+        const long long cols = elems / 8 + 1024;
+        const size_t b_col = a256(sizeof(brm::LongCol) * (size_t)cols);
+        const size_t b_leaf = a256(2 * (size_t)elems + 2);
+        BRM_TRY(grow(ctx->longbuf, b_col + b_leaf + vsize(dtype) * (size_t)elems + 8));
+        unsigned char *q = (unsigned char *)ctx->longbuf.p;
+        P.long_col = (brm::LongCol *)q;
+        P.long_leaf = (unsigned short *)(q + b_col);
+        P.long_val = q + b_col + b_leaf;
+        P.long_cap_cols = cols;
+        P.long_cap_elems = elems;
+        BRM_CK(cudaMemsetAsync(&P.cnt->long_used, 0, sizeof(unsigned long long), s));
+    }
     brm::CsrDev a = to_dev(A), b = to_dev(B);
     if (dtype == BRM_F64)
         brm::launch_numeric_f64(upper, a, b, P, crpt, ccol, cval, ctx->spill.p, ctx->spill_bytes,
@@ -355,7 +376,6 @@ int read_err(brm_context ctx)
 
 int check_dtype(brm_dtype d) { return (d == BRM_F64 || d == BRM_F32) ? BRM_SUCCESS : BRM_ERR_INVALID_VALUE; }
 
-size_t vsize(brm_dtype d) { return d == BRM_F64 ? 8 : 4; }
 
 // Upper after plan_phase(upper): numeric into C_bar, scan of the real row
 // sizes, compaction into the caller's C.  Events 4.. as in upper timing.
@@ -578,6 +598,7 @@ int brm_destroy(brm_context ctx)
     release(ctx->ameta);
     release(ctx->segbuf);
     release(ctx->splitbuf);
+    release(ctx->longbuf);
     release(ctx->bar_col);
     release(ctx->bar_val);
     release(ctx->io_arpt);

@@ -22,6 +22,7 @@ static void numeric_f64(const CsrDev &A, const CsrDev &B, const PlanDev &P, cons
     cudaFuncSetAttribute(k_seg_numeric<double, UPPER>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)ssm);
     k_seg_numeric<double, UPPER><<<num_sms * 2, kSegThreads, ssm, s>>>(A, B, P, crpt, ccol, cval);
+    k_long_reduce<double><<<num_sms * 4, 128, 0, s>>>(P, ccol, cval);
     const size_t smem = NumLayout<double>::bytes;
     cudaFuncSetAttribute(k_rows_numeric<double, UPPER>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)smem);

@@ -91,6 +91,9 @@ struct Counters {
     int work_plan;     // dynamic row counter of the heavy-row planning
     int n_huge;        // heavy rows above kHugeFlop products (listed from the end)
     int pad;
+    // long columns of the segment kernel handed to the column reducer:
+    // (columns << 40) | elements reserved so far
+    unsigned long long long_used;
 };
 
 // Descriptor slots reserved for a heavy row with F products: the cut rule
@@ -115,6 +118,17 @@ struct SegDesc {
     long long tab;  // split-table offset of the row (boundary-major, k entries each)
 };
 
+// A column of a heavy-row segment with many products, handed from the
+// segment kernel to the column reducer: its products' leaves and values in
+// leaf order at [off, off + len) of the long-column scratch, and the output
+// position.  len < 0: the segment kernel reduced the column itself.
+struct LongCol {
+    long long out;  // index into (ccol, cval)
+    long long off;  // first element in the scratch
+    int col;        // column of C
+    int len;
+};
+
 // Device arrays of a plan (all sized for M rows unless noted).
 struct PlanDev {
     int M;
@@ -137,6 +151,11 @@ struct PlanDev {
     SegDesc *seg;          // [Counters::seg_cap] segment descriptors (numbered per row)
     int *seg_list;         // [Counters::seg_cap] descriptor slot of every written segment
     int *split;            // [Counters::table_cap] split table (numeric phase)
+    LongCol *long_col;     // [long_cap_cols] long-column descriptors (numeric phase)
+    unsigned short *long_leaf;  // [long_cap_elems] leaves of the long columns' products
+    void *long_val;        // [long_cap_elems] their values (the value type)
+    long long long_cap_cols;
+    long long long_cap_elems;
     Counters *cnt;
 };
 

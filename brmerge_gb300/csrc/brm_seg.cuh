@@ -541,6 +541,10 @@ __global__ void __launch_bounds__(kSegThreads) k_seg_numeric(CsrDev A, CsrDev B,
         const int a0 = A.rpt[row];
         const int k = A.rpt[row + 1] - a0;
         const int span = d.c_hi - d.c_lo;
+        // distinct columns of the row up to the next segment (checked at the end)
+        int next_u = 0;
+        if (tid == 0)
+            next_u = (d.bidx + 1 < P.seg_n[row]) ? P.seg[slot + 1].u_off : P.nnz[row];
         const int nsum = (span + 1023) >> 10;
         const int *sp0 = P.split + d.tab + (long long)d.bidx * k;
         const int *sp1 = sp0 + k;
@@ -807,18 +811,27 @@ __global__ void __launch_bounds__(kSegThreads) k_seg_numeric(CsrDev A, CsrDev B,
         }
         __syncthreads();
         // columns with more than eight products: one warp each puts them in
-        // leaf order (= staging order p, which it ranks with a bitmap over p)
-        // into ia, then reduces them across its lanes (or, beyond 32, in its
-        // first lane)
+        // leaf order (= staging order p, which it ranks with a bitmap over
+        // p) and hands them to the column reducer through the long-column
+        // scratch; when the scratch is full it reduces them itself (across
+        // its lanes up to 32 products, in its first lane beyond)
         const int nlong = min(misc[1], kLongMax);
         {
             const int lane = tid & 31, wid = tid >> 5;
             unsigned *bmp = cw + wid * kSegPWords;
             unsigned short *wpre = (unsigned short *)(cw + L::NW * kSegPWords) + wid * kSegPWords;
             const int nwp = (nprod + 31) >> 5;
+            T *lval = (T *)P.long_val;
             for (int li = wid; li < nlong; li += L::NW) {
                 const int u = longu[li];
                 const int i0 = ucnt[u], i1 = ucnt[u + 1], len = i1 - i0;
+                unsigned long long rsv = 0;
+                if (lane == 0)
+                    rsv = atomicAdd(&P.cnt->long_used, (1ull << 40) | (unsigned long long)len);
+                rsv = __shfl_sync(kFull, rsv, 0);
+                const long long lci = (long long)(rsv >> 40);
+                const long long leo = (long long)(rsv & ((1ull << 40) - 1ull));
+                const bool handoff = lci < P.long_cap_cols && leo + len <= P.long_cap_elems;
                 for (int w = lane; w < nwp; w += 32)
                     bmp[w] = 0;
                 __syncwarp();
@@ -844,9 +857,24 @@ __global__ void __launch_bounds__(kSegThreads) k_seg_numeric(CsrDev A, CsrDev B,
                 for (int i = i0 + lane; i < i1; i += 32) {
                     const int p = S[i];
                     const int r = wpre[p >> 5] + __popc(bmp[p >> 5] & ((1u << (p & 31)) - 1u));
-                    ia[i0 + r] = (unsigned short)p;
+                    if (handoff) {
+                        P.long_leaf[leo + r] = pleaf[p];
+                        lval[leo + r] = pval[p];
+                    } else {
+                        ia[i0 + r] = (unsigned short)p;
+                    }
+                }
+                if (lci < P.long_cap_cols && lane == 0) {
+                    LongCol c;
+                    c.out = obase + u;
+                    c.off = leo;
+                    c.col = d.c_lo + prc[S[i0]];
+                    c.len = handoff ? len : -1;
+                    P.long_col[lci] = c;
                 }
                 __syncwarp();
+                if (handoff)
+                    continue;
                 if (len <= 32) {
                     const int e = ia[i0 + (lane < len ? lane : 0)];
                     const T r = warp_trie<T>(pleaf[e], pval[e], len);
@@ -865,14 +893,52 @@ __global__ void __launch_bounds__(kSegThreads) k_seg_numeric(CsrDev A, CsrDev B,
                 __syncwarp();
             }
         }
-        if (tid == 0) {
-            // the segment must produce exactly its share of the row's columns
-            const int nseg = P.seg_n[row];
-            const int next_u = (d.bidx + 1 < nseg) ? P.seg[slot + 1].u_off : P.nnz[row];
-            if (U != next_u - d.u_off)
-                atomicOr(&P.cnt->err, kErrNnzMismatch);
-        }
+        // the segment must produce exactly its share of the row's columns
+        if (tid == 0 && U != next_u - d.u_off)
+            atomicOr(&P.cnt->err, kErrNnzMismatch);
         __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// 4. column reducer: one thread per long column handed over by the segment
+//    kernel; its products are in leaf order, so the trie is one ShiftReduce
+//    pass with the stack in registers (leaves below 2^16: at most 16 entries
+//    below the top).
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(128) k_long_reduce(PlanDev P, int *ccol, T *cval)
+{
+    const unsigned long long used = P.cnt->long_used;
+    const long long n = min((long long)(used >> 40), P.long_cap_cols);
+    const T *__restrict__ lval = (const T *)P.long_val;
+    const unsigned short *__restrict__ lleaf = P.long_leaf;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        const LongCol c = P.long_col[i];
+        if (c.len <= 0)
+            continue;
+        RegShiftReduce<T, 17> sr;
+        sr.init(lleaf[c.off], lval[c.off]);
+        // elements in groups of kGatherBatch independent loads, so a long
+        // column does not wait for one load per element
+        for (int j0 = 1; j0 < c.len; j0 += kGatherBatch) {
+            int lf[kGatherBatch];
+            T lv[kGatherBatch];
+#pragma unroll
+            for (int q = 0; q < kGatherBatch; q++) {
+                if (j0 + q < c.len) {
+                    lf[q] = lleaf[c.off + j0 + q];
+                    lv[q] = lval[c.off + j0 + q];
+                }
+            }
+#pragma unroll
+            for (int q = 0; q < kGatherBatch; q++)
+                if (j0 + q < c.len)
+                    sr.push(lf[q], lv[q]);
+        }
+        ccol[c.out] = c.col;
+        cval[c.out] = sr.finish();
     }
 }
 
