@@ -7,14 +7,14 @@ products), float64, BRMerge-Precise, plain per-call GPU path.  A "step" is
 one SpGEMM call.  GFLOP/s = 2 * intermediate products / time, the
 reference's definition (BRMerge-SpGEMM/src/brmerge_precise.cpp:65-69).
 
-* value   -- device-resident inputs: brm_symbolic + brm_numeric (C ABI)
+* value   -- device-resident inputs: one brm_precise_device call (C ABI)
              timed with CUDA events on the call's stream, L2 flushed between
              steps (the inputs fit in L2).
 * e2e     -- the reference-facing host call brm_precise: pinned host inputs
              copied in, C copied back to host memory, wall clock per call.
-* roofline -- numeric phase (the dominant phase): algorithmic bytes
-             bytes(A) + bytes(B) + bytes(C) over its CUDA-event duration,
-             against the measured HBM copy bandwidth in MEASURED_PEAKS.json.
+* roofline -- the whole call: algorithmic bytes bytes(A) + bytes(B) +
+             bytes(C) over its CUDA-event duration, against the measured HBM
+             copy bandwidth in MEASURED_PEAKS.json.
 * cpu_baseline -- the oracle restatement of BRMerge-Precise (OpenMP, all
              host cores) on the same input.
 
@@ -233,39 +233,44 @@ def run_ours(args):
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
 
     def step(timed_events=None):
+        # one BRMerge-Precise call (brm_precise_device): symbolic and numeric
+        # phases, callee-allocated C; the PreciseTiming fields split it
         if timed_events:
             timed_events[0].record(stream)
-        crpt, cnnz = ctx.symbolic(dA, dA)
-        if timed_events:
-            timed_events[1].record(stream)
-        C = ctx.numeric(dA, dA, crpt, cnnz)
+        C = ctx.precise_device(dA, dA, timing=timed_events[1] if timed_events else None)
         if timed_events:
             timed_events[2].record(stream)
-        return C, cnnz
+        return C, C.nnz
 
     for _ in range(args.warmup):
         C, cnnz = step()
     torch.cuda.synchronize(dev)
-    ev = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(args.steps)]
+    ev = [[torch.cuda.Event(enable_timing=True), brm.PreciseTiming(),
+           torch.cuda.Event(enable_timing=True)] for _ in range(args.steps)]
+    L = brm._native.lib()
     barrier(ws)
     torch.cuda.synchronize(dev)
+    launches0 = L.brm_kernel_launches()
     with ClockSampler(dev.index if dev.index is not None else 0) as clk:
         for i in range(args.steps):
             flush.fill_(float(i))  # write 512 MB (> 129 MB L2) between steps
             C, cnnz = step(ev[i])
         torch.cuda.synchronize(dev)
+    launches = L.brm_kernel_launches() - launches0
     barrier(ws)
     step_ms = [e[0].elapsed_time(e[2]) for e in ev]
-    num_ms = [e[1].elapsed_time(e[2]) for e in ev]
     total_s = max_over_ranks(sum(step_ms) / 1e3, ws)
     value = 2 * products * args.steps * ws / total_s / 1e9
+    sym_ms = statistics.mean((e[1].compute_flop + e[1].symbolic + e[1].prefix_sum_nnz) * 1e3
+                             for e in ev)
+    num_ms = statistics.mean(e[1].compute * 1e3 for e in ev)
 
+    # roofline of the whole call (every kernel of the step, one stream):
+    # compulsory bytes = read A and B once, write C once
     vb = 8
     alg_bytes = csr_bytes(A.M, A.nnz, vb) * 2 + csr_bytes(A.M, cnnz, vb)
-    num_s = statistics.mean(num_ms) / 1e3
     peak, peak_kind = peaks()
-    achieved = alg_bytes / num_s / 1e9
-    call_achieved = alg_bytes / (sum(step_ms) / args.steps / 1e3) / 1e9
+    achieved = alg_bytes / (statistics.mean(step_ms) / 1e3) / 1e9
 
     # e2e through the host drop-in (brm_precise): pinned inputs, host outputs
     pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()
@@ -285,7 +290,6 @@ def run_ours(args):
     if rank != 0:
         return
     cpu = cpu_baseline(A, budget_s=args.cpu_budget) if not args.no_cpu else None
-    launches_per_step = 9 + (1 if ctx.last_device_error < 0 else 0)
     line = {
         "metric": "SpGEMM GFLOP/s (BRMerge-Precise, C=A*A)",
         "value": round(value, 3), "unit": "GFLOP/s", "n_gpus": ws, "steps": args.steps,
@@ -293,17 +297,18 @@ def run_ours(args):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic",
         "config": dict(desc, products=int(products), nnz_A=int(A.nnz), nnz_C=int(cnnz),
-                       method="precise", l2="flushed (512 MB write) between steps",
+                       method="precise", call="brm_precise_device (one call)",
+                       l2="flushed (512 MB write) between steps",
                        parallelism="replicas" if ws > 1 else "single_gpu",
-                       call_hbm_frac=round(call_achieved / peak, 4)),
+                       symbolic_ms=round(sym_ms, 4), numeric_ms=round(num_ms, 4)),
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak,
                      "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": None,
-                     "kernel": "numeric phase", "peak_kind": peak_kind,
-                     "algorithmic_bytes": int(alg_bytes)},
+                     "kernel": "whole Precise call (all kernels of a step)",
+                     "peak_kind": peak_kind, "algorithmic_bytes": int(alg_bytes)},
         "e2e": {"value": round(e2e_val, 3), "unit": "GFLOP/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h)},
         "clocks": clk.summary(),
-        "gpu_launches": launches_per_step * args.steps,
+        "gpu_launches": int(launches),
     }
     if cpu is not None:
         line["cpu_baseline"] = cpu

@@ -94,6 +94,7 @@ def lib() -> C.CDLL:
                    C.POINTER(vt), C.c_int, C.c_int, C.c_int, c_int_p, C.POINTER(tt)])
         _decl(L.brm_free, None, [vp])
         _decl(L.brm_host_cache_release, None, [])
+        _decl(L.brm_kernel_launches, C.c_longlong, [])
         _decl(L.brm_compute_flop, C.c_int, [vp, csrp, csrp, C.POINTER(C.c_longlong)])
         _decl(L.brm_upper_bound, C.c_int,
               [vp, C.c_int, csrp, csrp, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)])

@@ -169,6 +169,7 @@ void launch_analyze(const CsrDev &A, const CsrDev &B, const PlanDev &P, cudaStre
     constexpr int RPB = (kAnaThreads / 32) * kAnaRowsPerWarp;
     int grid = (A.M + RPB - 1) / RPB;
     k_analyze<<<grid, kAnaThreads, 0, s>>>(A, B, P);
+    count_launch();
 }
 
 // ---------------------------------------------------------------------------
@@ -275,8 +276,11 @@ static void scan_impl(const int *in, OutT *out, int n, Counters *cnt, void *tmp,
     if (tiles == 0)
         tiles = 1;
     k_scan_reduce<<<tiles, kScanThreads, 0, s>>>(in, n, ts);
+    count_launch();
     k_scan_tiles<<<1, kScanThreads, 0, s>>>(ts, tiles);
+    count_launch();
     k_scan_down<OutT><<<tiles, kScanThreads, 0, s>>>(in, n, ts, out, cnt);
+    count_launch();
 }
 
 void launch_scan_i32(const int *in, int *out, int n, Counters *cnt, void *tmp, cudaStream_t s)
@@ -319,12 +323,15 @@ void launch_compact(int dtype, const PlanDev &P, const int *bar_col, const void 
     int grid = (P.M + 7) / 8;
     if (grid > 65535 * 4)
         grid = 65535 * 4;
-    if (dtype == 0)
+    if (dtype == 0) {
         k_compact<double><<<grid, 256, 0, s>>>(P.M, P.scan_flop, P.nnz, bar_col,
                                                 (const double *)bar_val, crpt, ccol, (double *)cval);
-    else
+        count_launch();
+    } else {
         k_compact<float><<<grid, 256, 0, s>>>(P.M, P.scan_flop, P.nnz, bar_col,
                                                (const float *)bar_val, crpt, ccol, (float *)cval);
+        count_launch();
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -370,6 +377,7 @@ void launch_validate(const CsrDev &X, int ncols, int *bad_row, cudaStream_t s)
     if (grid > 65535 * 4)
         grid = 65535 * 4;
     k_validate<<<grid, 256, 0, s>>>(X, ncols, bad_row);
+    count_launch();
 }
 
 }  // namespace brm

@@ -6,6 +6,7 @@
 // interface needs: nnz(C) after the symbolic phase (the caller allocates C),
 // and the error word after the numeric phase.
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <climits>
 #include <cstdlib>
@@ -15,6 +16,12 @@
 #include "brm_hostpool.h"
 #include "brm_kernels.h"
 #include "brmerge.h"
+
+namespace {
+std::atomic<long long> g_launches{0};
+}  // namespace
+
+void brm::count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 
 namespace {
 
@@ -42,11 +49,17 @@ struct brm_context_s {
     int *d_bad = nullptr;
     brm::Counters *h_cnt = nullptr;  // pinned mirror of the device counters
     int *h_bad = nullptr;            // pinned
+    long long *h_mid = nullptr;      // pinned: entries of the mid-row scratch
     // per-A-entry list metadata (B-row start and length)
     DevBuf ameta;
     // heavy-row segments: descriptors + written list, the split table and the
     // long-column scratch of the column reducer
     DevBuf segbuf, splitbuf, longbuf;
+    // one-call Precise: mid rows computed with the plan (columns, values)
+    DevBuf midbuf;
+    int *mid_col = nullptr;
+    void *mid_val = nullptr;
+    bool mid_ready = false;
     // spill scratch
     DevBuf spill;
     // Upper upper-bound buffer
@@ -139,6 +152,8 @@ size_t workspace_bytes(int M)
     b += a256(4);                           // bad row
     return b;
 }
+
+size_t vsize(brm_dtype d) { return d == BRM_F64 ? 8 : 4; }
 
 int ensure_workspace(brm_context ctx, int M)
 {
@@ -265,9 +280,13 @@ double ev_sec(brm_context ctx, int a, int b)
 
 // Analysis + symbolic (+ crpt scan for Precise).  Leaves ctx->h_cnt filled.
 // Event indices: 0 start, 1 after analysis, 2 after symbolic, 3 after scan.
+// fused_dtype >= 0 (one-call Precise only): the mid rows are computed here,
+// values included, into ctx->midbuf, and the numeric phase only moves them.
 int plan_phase(brm_context ctx, const brm_csr *A, const brm_csr *B, int *crpt, bool upper,
-               bool timed)
+               bool timed, int fused_dtype = -1)
 {
+    const bool fused = fused_dtype >= 0 && !upper;
+    ctx->mid_ready = false;
     BRM_TRY(ensure_workspace(ctx, A->M));
     BRM_TRY(ensure_ameta(ctx, A->nnz));
     if (ctx->validate)
@@ -284,7 +303,17 @@ int plan_phase(brm_context ctx, const brm_csr *A, const brm_csr *B, int *crpt, b
     // the segment descriptors of heavy rows are sized by the analysis
     BRM_CK(cudaGetLastError());
     BRM_CK(cudaMemcpyAsync(ctx->h_cnt, P.cnt, sizeof(brm::Counters), cudaMemcpyDeviceToHost, s));
+    if (fused)
+        BRM_CK(cudaMemcpyAsync(ctx->h_mid, P.mid_pre + A->M, sizeof(long long),
+                               cudaMemcpyDeviceToHost, s));
     BRM_CK(cudaStreamSynchronize(s));
+    if (fused) {
+        const size_t n = (size_t)(*ctx->h_mid > 0 ? *ctx->h_mid : 1);
+        const size_t b_col = a256(4 * n);
+        BRM_TRY(grow(ctx->midbuf, b_col + vsize((brm_dtype)fused_dtype) * n));
+        ctx->mid_col = (int *)ctx->midbuf.p;
+        ctx->mid_val = (unsigned char *)ctx->midbuf.p + b_col;
+    }
     {
         const size_t cap = (size_t)ctx->h_cnt->seg_cap + 1;
         BRM_TRY(grow(ctx->segbuf, cap * (sizeof(brm::SegDesc) + sizeof(int))));
@@ -294,7 +323,13 @@ int plan_phase(brm_context ctx, const brm_csr *A, const brm_csr *B, int *crpt, b
         ctx->plan.seg_list = P.seg_list;
     }
     ev_record(ctx, timed, 1);
-    brm::launch_symbolic(a, b, P, ctx->num_sms, upper, s);
+    brm::launch_symbolic(a, b, P, ctx->num_sms, upper, fused, s);
+    if (fused) {
+        if (fused_dtype == BRM_F64)
+            brm::launch_mid_scratch_f64(a, b, P, ctx->mid_col, ctx->mid_val, ctx->num_sms, s);
+        else
+            brm::launch_mid_scratch_f32(a, b, P, ctx->mid_col, ctx->mid_val, ctx->num_sms, s);
+    }
     ev_record(ctx, timed, 2);
     if (upper)
         brm::launch_scan_i64(P.flop, P.scan_flop, A->M, ctx->scan_tmp, s);
@@ -315,6 +350,7 @@ int plan_phase(brm_context ctx, const brm_csr *A, const brm_csr *B, int *crpt, b
     ctx->pK = A->N;
     ctx->pN = B->N;
     ctx->spill_bytes = ctx->h_cnt->spill_bytes;
+    ctx->mid_ready = fused;
     return BRM_SUCCESS;
 }
 
@@ -324,11 +360,11 @@ bool plan_matches(brm_context ctx, const brm_csr *A, const brm_csr *B)
            ctx->b_col == B->col && ctx->pM == A->M && ctx->pK == A->N && ctx->pN == B->N;
 }
 
-size_t vsize(brm_dtype d) { return d == BRM_F64 ? 8 : 4; }
-
+// use_mid: take the mid rows from the one-call scratch (plan_phase fused).
 int numeric_launch(brm_context ctx, brm_dtype dtype, bool upper, const brm_csr *A,
-                   const brm_csr *B, const int *crpt, int *ccol, void *cval)
+                   const brm_csr *B, const int *crpt, int *ccol, void *cval, bool use_mid = false)
 {
+    const bool mid = use_mid && ctx->mid_ready && !upper;
     if (ctx->spill_bytes)
         BRM_TRY(grow(ctx->spill, ctx->spill_bytes));
     cudaStream_t s = ctx->stream;
@@ -355,12 +391,14 @@ int numeric_launch(brm_context ctx, brm_dtype dtype, bool upper, const brm_csr *
         BRM_CK(cudaMemsetAsync(&P.cnt->long_used, 0, sizeof(unsigned long long), s));
     }
     brm::CsrDev a = to_dev(A), b = to_dev(B);
+    const int *mcol = mid ? ctx->mid_col : nullptr;
+    const void *mval = mid ? ctx->mid_val : nullptr;
     if (dtype == BRM_F64)
         brm::launch_numeric_f64(upper, a, b, P, crpt, ccol, cval, ctx->spill.p, ctx->spill_bytes,
-                                ctx->num_sms, s);
+                                mcol, mval, ctx->num_sms, s);
     else
         brm::launch_numeric_f32(upper, a, b, P, crpt, ccol, cval, ctx->spill.p, ctx->spill_bytes,
-                                ctx->num_sms, s);
+                                mcol, mval, ctx->num_sms, s);
     BRM_CK(cudaGetLastError());
     return BRM_SUCCESS;
 }
@@ -447,14 +485,19 @@ int host_call(bool upper, const int *arpt, const int *acol, const T *aval, const
     int cnnz = 0;
     double t_sym0 = 0, t_sym1 = 0, t_num0 = 0, t_num1 = 0;
     if (!upper) {
+        // one call: symbolic with the mid rows computed in passing, numeric
         t_sym0 = now_sec();
-        BRM_TRY(brm_symbolic(ctx, &A, &B, (int *)ctx->io_crpt.p, &cnnz));
+        BRM_TRY(check_pair(&A, &B));
+        ctx->planned = false;
+        BRM_TRY(plan_phase(ctx, &A, &B, (int *)ctx->io_crpt.p, false, false, dtype));
+        cnnz = (int)ctx->h_cnt->cnnz;
         t_sym1 = now_sec();
         BRM_TRY(grow(ctx->io_ccol, 4 * (size_t)cnnz));
         BRM_TRY(grow(ctx->io_cval, sizeof(T) * (size_t)cnnz));
         t_num0 = now_sec();
-        BRM_TRY(brm_numeric(ctx, dtype, &A, &B, (const int *)ctx->io_crpt.p, (int *)ctx->io_ccol.p,
-                            ctx->io_cval.p));
+        BRM_TRY(numeric_launch(ctx, dtype, false, &A, &B, (const int *)ctx->io_crpt.p,
+                               (int *)ctx->io_ccol.p, ctx->io_cval.p, true));
+        BRM_TRY(read_err(ctx));
         t_num1 = now_sec();
     } else {
         t_sym0 = now_sec();
@@ -563,6 +606,8 @@ int brm_create(brm_context *out)
         e = cudaMallocHost(&ctx->h_cnt, sizeof(brm::Counters));
     if (e == cudaSuccess)
         e = cudaMallocHost(&ctx->h_bad, sizeof(int));
+    if (e == cudaSuccess)
+        e = cudaMallocHost(&ctx->h_mid, sizeof(long long));
     for (int i = 0; i < kNumEvents && e == cudaSuccess; i++)
         e = cudaEventCreate(&ctx->ev[i]);
     if (e == cudaSuccess) {
@@ -599,6 +644,7 @@ int brm_destroy(brm_context ctx)
     release(ctx->segbuf);
     release(ctx->splitbuf);
     release(ctx->longbuf);
+    release(ctx->midbuf);
     release(ctx->bar_col);
     release(ctx->bar_val);
     release(ctx->io_arpt);
@@ -614,6 +660,8 @@ int brm_destroy(brm_context ctx)
         cudaFreeHost(ctx->h_cnt);
     if (ctx->h_bad)
         cudaFreeHost(ctx->h_bad);
+    if (ctx->h_mid)
+        cudaFreeHost(ctx->h_mid);
     for (int i = 0; i < kNumEvents; i++)
         if (ctx->ev[i])
             cudaEventDestroy(ctx->ev[i]);
@@ -681,7 +729,7 @@ int brm_precise_device(brm_context ctx, brm_dtype dtype, const brm_csr *A, const
     BRM_CK(cudaMallocAsync((void **)&crpt, 4 * ((size_t)A->M + 1), ctx->stream));
     double t1 = now_sec();
     ctx->planned = false;
-    int st = plan_phase(ctx, A, B, crpt, false, timed);
+    int st = plan_phase(ctx, A, B, crpt, false, timed, dtype);
     if (st != BRM_SUCCESS) {
         cudaFreeAsync(crpt, ctx->stream);
         return st;
@@ -702,7 +750,7 @@ int brm_precise_device(brm_context ctx, brm_dtype dtype, const brm_csr *A, const
     }
     double t3 = now_sec();
     ev_record(ctx, timed, 4);
-    st = numeric_launch(ctx, dtype, false, A, B, crpt, ccol, cval);
+    st = numeric_launch(ctx, dtype, false, A, B, crpt, ccol, cval, true);
     ev_record(ctx, timed, 5);
     if (st == BRM_SUCCESS)
         st = read_err(ctx);
@@ -860,6 +908,8 @@ void brm_free(void *p)
 }
 
 void brm_host_cache_release(void) { brm::host_trim(); }
+
+long long brm_kernel_launches(void) { return g_launches.load(std::memory_order_relaxed); }
 
 int brm_compute_flop(brm_context ctx, const brm_csr *A, const brm_csr *B, long long *products)
 {

@@ -7,6 +7,10 @@
 
 namespace brm {
 
+// Counts one kernel launch of this library (brm_kernel_launches reports the
+// process-wide total); every launch site calls it right after <<<...>>>.
+void count_launch();
+
 // Row analysis: products per row, row bins and lists, total products
 // (replaces compute_flop and the static load balance, spgemm.h:31-56, :496-503).
 void launch_analyze(const CsrDev &A, const CsrDev &B, const PlanDev &P, cudaStream_t s);
@@ -25,14 +29,7 @@ size_t scan_tmp_bytes(int n);
 // restricts the row CTA pass to rows above kCap products (the Upper path uses
 // it only to route rows to the spill path).
 void launch_symbolic(const CsrDev &A, const CsrDev &B, const PlanDev &P, int num_sms,
-                     bool only_heavy, cudaStream_t s);
-
-// Numeric phase (spgemm.h:580-721).  Precise: rows are written at crpt[row].
-// Upper: rows are written at scan_flop[row] into (bar_col, bar_val) and their
-// lengths into P.nnz (spgemm.h:266-410).
-void launch_numeric(int dtype, bool upper, const CsrDev &A, const CsrDev &B, const PlanDev &P,
-                    const int *crpt, int *ccol, void *cval, void *spill_scratch,
-                    unsigned long long spill_bytes, int num_sms, cudaStream_t s);
+                     bool only_heavy, bool skip_mid, cudaStream_t s);
 
 // Upper compaction: C[crpt[i]..] = C_bar[scan_flop[i]..] (spgemm.h:429-444).
 void launch_compact(int dtype, const PlanDev &P, const int *bar_col, const void *bar_val,
@@ -46,10 +43,22 @@ void launch_validate(const CsrDev &X, int ncols, int *bad_row, cudaStream_t s);
 }  // namespace brm
 
 namespace brm {
+// Numeric launchers per value type.  mid_col/mid_val (Precise only): the
+// scratch written by launch_mid_scratch_*, moved to C instead of running the
+// mid-row kernel again.
 void launch_numeric_f64(bool upper, const CsrDev &A, const CsrDev &B, const PlanDev &P,
                         const int *crpt, int *ccol, void *cval, void *spill_scratch,
-                        unsigned long long spill_bytes, int num_sms, cudaStream_t s);
+                        unsigned long long spill_bytes, const int *mid_col, const void *mid_val,
+                        int num_sms, cudaStream_t s);
 void launch_numeric_f32(bool upper, const CsrDev &A, const CsrDev &B, const PlanDev &P,
                         const int *crpt, int *ccol, void *cval, void *spill_scratch,
-                        unsigned long long spill_bytes, int num_sms, cudaStream_t s);
+                        unsigned long long spill_bytes, const int *mid_col, const void *mid_val,
+                        int num_sms, cudaStream_t s);
+
+// One-call Precise: the mid rows' values and lengths (P.nnz) computed with
+// the plan, into a scratch of P.mid_pre[M] entries (row r at P.mid_pre[r]).
+void launch_mid_scratch_f64(const CsrDev &A, const CsrDev &B, const PlanDev &P, int *mid_col,
+                            void *mid_val, int num_sms, cudaStream_t s);
+void launch_mid_scratch_f32(const CsrDev &A, const CsrDev &B, const PlanDev &P, int *mid_col,
+                            void *mid_val, int num_sms, cudaStream_t s);
 }  // namespace brm

@@ -400,7 +400,11 @@ __device__ __forceinline__ void mid_merge_level(int L, const unsigned short *__r
 // ---------------------------------------------------------------------------
 // Numeric: stable merge by column, order-exact reduction, ordered store.
 // ---------------------------------------------------------------------------
-template <typename T, bool UPPER>
+// SCRATCH: the one-call Precise form runs this kernel before nnz(C) is
+// known and writes each row at P.mid_pre[row] of a scratch pair (ccol, cval)
+// sized by the batch weights, with its length in P.nnz; k_mid_compact moves
+// the rows to C once crpt exists.
+template <typename T, bool UPPER, bool SCRATCH = false>
 __global__ void __launch_bounds__(kMidThreads) k_mid_numeric(CsrDev A, CsrDev B, PlanDev P,
                                                              const int *crpt, int *ccol, T *cval)
 {
@@ -527,7 +531,8 @@ __global__ void __launch_bounds__(kMidThreads) k_mid_numeric(CsrDev A, CsrDev B,
                 const int e = src[p];
                 const int s = t.lslot[lidx[e]];
                 const int row = t.s_row[s];
-                const long long base = UPPER ? P.scan_flop[row] : (long long)crpt[row];
+                const long long base = SCRATCH ? P.mid_pre[row]
+                                       : (UPPER ? P.scan_flop[row] : (long long)crpt[row]);
                 const long long o = base + (h - s_hb[s]);
                 int q = p + 1;
                 T v;
@@ -550,7 +555,7 @@ __global__ void __launch_bounds__(kMidThreads) k_mid_numeric(CsrDev A, CsrDev B,
         if (tid < nslots) {
             const int row = t.s_row[tid];
             const int len = s_hb[tid + 1] - s_hb[tid];
-            if (UPPER)
+            if (UPPER || SCRATCH)
                 P.nnz[row] = len;
             else if (len != crpt[row + 1] - crpt[row])
                 atomicOr(&P.cnt->err, kErrNnzMismatch);
@@ -574,6 +579,29 @@ __global__ void __launch_bounds__(256) k_batch_starts(PlanDev P, int M)
         P.batch_start[b] = r;
     if (r == M)
         P.cnt->n_batch = (int)((hi + kMidFlop - 1) / kMidFlop);
+}
+
+// Moves the mid rows written by k_mid_numeric<..., SCRATCH> from the
+// scratch (row at P.mid_pre[row], P.nnz[row] entries) to C at crpt[row].
+// One warp per row; rows that are not mid rows are skipped.
+template <typename T>
+__global__ void __launch_bounds__(256) k_mid_compact(PlanDev P, int M, const int *__restrict__ scol,
+                                                     const T *__restrict__ sval, const int *crpt,
+                                                     int *ccol, T *cval)
+{
+    const int lane = threadIdx.x & 31;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    for (int row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; row < M; row += nwarps) {
+        if (P.mid_flop[row] == 0)
+            continue;
+        const long long src = P.mid_pre[row];
+        const long long dst = crpt[row];
+        const int n = P.nnz[row];
+        for (int i = lane; i < n; i += 32) {
+            ccol[dst + i] = scol[src + i];
+            cval[dst + i] = sval[src + i];
+        }
+    }
 }
 
 }  // namespace brm

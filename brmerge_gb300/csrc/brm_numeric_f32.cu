@@ -9,39 +9,72 @@ namespace brm {
 template <bool UPPER>
 static void numeric_f32(const CsrDev &A, const CsrDev &B, const PlanDev &P, const int *crpt,
                        int *ccol, float *cval, void *spill_scratch, unsigned long long spill_bytes,
-                       int num_sms, cudaStream_t s)
+                       const int *mid_col, const void *mid_val, int num_sms, cudaStream_t s)
 {
     k_copy_numeric<float, UPPER><<<num_sms * 8, 256, 0, s>>>(A, B, P, crpt, ccol, cval);
+    count_launch();
     k_warp_numeric<float, UPPER><<<num_sms * 8, 256, 0, s>>>(A, B, P, crpt, ccol, cval);
-    const size_t msm = MidNumLayout<float>::bytes;
-    cudaFuncSetAttribute(k_mid_numeric<float, UPPER>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)msm);
-    k_mid_numeric<float, UPPER><<<num_sms * 2, kMidThreads, msm, s>>>(A, B, P, crpt, ccol, cval);
+    count_launch();
+    if (mid_col) {
+        // mid rows were computed with the plan (one-call Precise): move them
+        k_mid_compact<float><<<num_sms * 8, 256, 0, s>>>(P, A.M, mid_col, (const float *)mid_val,
+                                                          crpt, ccol, cval);
+        count_launch();
+    } else {
+        const size_t msm = MidNumLayout<float>::bytes;
+        cudaFuncSetAttribute(k_mid_numeric<float, UPPER>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)msm);
+        k_mid_numeric<float, UPPER><<<num_sms * 2, kMidThreads, msm, s>>>(A, B, P, crpt, ccol,
+                                                                            cval);
+        count_launch();
+    }
     k_split<0><<<num_sms * 8, 256, 0, s>>>(A, B, P);
+    count_launch();
     const size_t ssm = SegLayout<float>::bytes;
     cudaFuncSetAttribute(k_seg_numeric<float, UPPER>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)ssm);
     k_seg_numeric<float, UPPER><<<num_sms * 2, kSegThreads, ssm, s>>>(A, B, P, crpt, ccol, cval);
+    count_launch();
     k_long_reduce<float><<<num_sms * 4, 128, 0, s>>>(P, ccol, cval);
+    count_launch();
     const size_t smem = NumLayout<float>::bytes;
     cudaFuncSetAttribute(k_rows_numeric<float, UPPER>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)smem);
     k_rows_numeric<float, UPPER><<<num_sms, kRowThreads, smem, s>>>(A, B, P, crpt, ccol, cval);
-    if (spill_bytes)
+    count_launch();
+    if (spill_bytes) {
         k_spill_numeric<float, UPPER><<<num_sms * 4, 32, 0, s>>>(
             A, B, P, crpt, ccol, cval, (unsigned char *)spill_scratch, spill_bytes);
+        count_launch();
+    }
 }
 
 void launch_numeric_f32(bool upper, const CsrDev &A, const CsrDev &B, const PlanDev &P,
                        const int *crpt, int *ccol, void *cval, void *spill_scratch,
-                       unsigned long long spill_bytes, int num_sms, cudaStream_t s)
+                       unsigned long long spill_bytes, const int *mid_col, const void *mid_val,
+                       int num_sms, cudaStream_t s)
 {
     if (A.M <= 0)
         return;
     if (upper)
-        numeric_f32<true>(A, B, P, crpt, ccol, (float *)cval, spill_scratch, spill_bytes, num_sms, s);
+        numeric_f32<true>(A, B, P, crpt, ccol, (float *)cval, spill_scratch, spill_bytes, nullptr,
+                          nullptr, num_sms, s);
     else
-        numeric_f32<false>(A, B, P, crpt, ccol, (float *)cval, spill_scratch, spill_bytes, num_sms, s);
+        numeric_f32<false>(A, B, P, crpt, ccol, (float *)cval, spill_scratch, spill_bytes, mid_col,
+                           mid_val, num_sms, s);
+}
+
+void launch_mid_scratch_f32(const CsrDev &A, const CsrDev &B, const PlanDev &P, int *mid_col,
+                            void *mid_val, int num_sms, cudaStream_t s)
+{
+    if (A.M <= 0)
+        return;
+    const size_t msm = MidNumLayout<float>::bytes;
+    cudaFuncSetAttribute(k_mid_numeric<float, false, true>,
+                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)msm);
+    k_mid_numeric<float, false, true><<<num_sms * 2, kMidThreads, msm, s>>>(
+        A, B, P, nullptr, mid_col, (float *)mid_val);
+    count_launch();
 }
 
 }  // namespace brm

@@ -12,33 +12,41 @@ void launch_batches(const PlanDev &P, int M, void *tmp, cudaStream_t s)
         return;
     launch_scan_i64(P.mid_flop, P.mid_pre, M, tmp, s);
     k_batch_starts<0><<<(M + 1 + 255) / 256, 256, 0, s>>>(P, M);
+    count_launch();
 }
 
 void launch_symbolic(const CsrDev &A, const CsrDev &B, const PlanDev &P, int num_sms,
-                     bool only_heavy, cudaStream_t s)
+                     bool only_heavy, bool skip_mid, cudaStream_t s)
 {
     if (A.M <= 0)
         return;
     if (!only_heavy) {
         k_warp_symbolic<0><<<num_sms * 8, 256, 0, s>>>(A, B, P);
-        const size_t msm = MidSymLayout::bytes;
-        cudaFuncSetAttribute(k_mid_symbolic<0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)msm);
-        k_mid_symbolic<0><<<num_sms * 2, kMidThreads, msm, s>>>(A, B, P);
+        count_launch();
+        if (!skip_mid) {
+            const size_t msm = MidSymLayout::bytes;
+            cudaFuncSetAttribute(k_mid_symbolic<0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)msm);
+            k_mid_symbolic<0><<<num_sms * 2, kMidThreads, msm, s>>>(A, B, P);
+            count_launch();
+        }
     }
     // heavy rows: exact nnz and segment plan (both Precise and Upper)
     const size_t psm = PlanLayout::bytes;
     cudaFuncSetAttribute(k_heavy_plan<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)psm);
     k_heavy_plan<0><<<num_sms * 3, kPlanThreads, psm, s>>>(A, B, P);
+    count_launch();
     const size_t smem = SymLayout::bytes;
     if (only_heavy) {
         cudaFuncSetAttribute(k_rows_symbolic<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)smem);
         k_rows_symbolic<true><<<num_sms * 4, kRowThreads, smem, s>>>(A, B, P);
+        count_launch();
     } else {
         cudaFuncSetAttribute(k_rows_symbolic<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)smem);
         k_rows_symbolic<false><<<num_sms * 4, kRowThreads, smem, s>>>(A, B, P);
+        count_launch();
     }
 }
 

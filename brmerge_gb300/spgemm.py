@@ -258,31 +258,24 @@ class Context:
         _native.check(fn(self._h, code, C.byref(a), C.byref(b), C.byref(pr), C.byref(pc),
                          C.byref(pv), C.byref(cnnz), C.byref(tc)),
                       "brm_upper_device" if upper else "brm_precise_device")
-        try:
-            n = cnnz.value
-            dev = A.rpt.device
-            crpt = torch.empty(A.M + 1, dtype=torch.int32, device=dev)
-            ccol = torch.empty(n, dtype=torch.int32, device=dev)
-            cval = torch.empty(n, dtype=A.val.dtype, device=dev)
-            torch.cuda.synchronize(dev)
-            _cuda_copy(crpt, pr.value, crpt.numel() * 4)
-            if n:
-                _cuda_copy(ccol, pc.value, n * 4)
-                _cuda_copy(cval, pv.value, n * cval.element_size())
-        finally:
-            for p in (pr, pc, pv):
-                self._L.brm_device_free(self._h, p)
-            torch.cuda.synchronize(A.rpt.device)
+        n = cnnz.value
+        dev = A.rpt.device
+        vt = "<f8" if A.val.dtype == torch.float64 else "<f4"
+        # the callee-allocated buffers become the tensors' storage; each is
+        # released with brm_device_free when its tensor is collected
+        crpt = _device_tensor(self._L, pr.value, A.M + 1, "<i4", dev)
+        ccol = _device_tensor(self._L, pc.value, n, "<i4", dev)
+        cval = _device_tensor(self._L, pv.value, n, vt, dev)
         if timing is not None:
             timing._load(tc)
         return DeviceCSR(A.M, B.N, crpt, ccol, cval)
 
     def precise_device(self, A: DeviceCSR, B: DeviceCSR, timing=None) -> DeviceCSR:
-        """brm_precise_device (callee-allocated outputs), copied into torch tensors."""
+        """brm_precise_device: one call, callee-allocated outputs (no copy)."""
         return self._device_call(False, A, B, timing)
 
     def upper(self, A: DeviceCSR, B: DeviceCSR, timing=None) -> DeviceCSR:
-        """brm_upper_device, copied into torch tensors."""
+        """brm_upper_device: one call, callee-allocated outputs (no copy)."""
         return self._device_call(True, A, B, timing)
 
     def compute_flop(self, A: DeviceCSR, B: DeviceCSR) -> int:
@@ -318,12 +311,29 @@ class _RawDevice:
             "shape": (n,), "typestr": typestr, "data": (ptr, False), "version": 2, "strides": None}
 
 
-def _cuda_copy(dst_tensor, src_ptr: int, nbytes: int) -> None:
+class _DeviceBlock(_RawDevice):
+    """A callee-allocated device buffer that brm_device_free releases when
+    the last tensor viewing it is gone (stream-ordered on the legacy stream)."""
+
+    def __init__(self, L, ptr: int, n: int, typestr: str):
+        super().__init__(ptr, n, typestr)
+        self._L, self._p = L, ptr
+
+    def __del__(self):
+        if self._p:
+            self._L.brm_device_free(None, self._p)
+            self._p = None
+
+
+def _device_tensor(L, ptr, n: int, typestr: str, device):
     import torch
-    n = dst_tensor.numel()
-    typestr = {torch.int32: "<i4", torch.float64: "<f8", torch.float32: "<f4"}[dst_tensor.dtype]
-    src = torch.as_tensor(_RawDevice(src_ptr, n, typestr), device=dst_tensor.device)
-    dst_tensor.copy_(src)
+    dt = {"<i4": torch.int32, "<f8": torch.float64, "<f4": torch.float32}[typestr]
+    if not ptr:
+        return torch.empty(n, dtype=dt, device=device)
+    if n == 0:
+        L.brm_device_free(None, ptr)
+        return torch.empty(0, dtype=dt, device=device)
+    return torch.as_tensor(_DeviceBlock(L, ptr, n, typestr), device=device)
 
 
 def compute_flop_host(A: CSR, B: CSR) -> int:

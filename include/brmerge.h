@@ -165,6 +165,12 @@ void brm_free(void *p);
  * MiB of unused blocks. */
 void brm_host_cache_release(void);
 
+/* Kernels this library has launched in this process so far (all contexts
+ * and threads; the two of brm_compute_flop_noalloc are not counted).  No
+ * counterpart in the reference (a CPU library); a caller reads it around a
+ * region to count the GPU work the region issued. */
+long long brm_kernel_launches(void);
+
 /* ---- helpers ---------------------------------------------------------------- */
 
 /* Intermediate products of A*B (compute_flop, spgemm.h:59-66); GFLOP/s in

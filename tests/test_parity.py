@@ -36,6 +36,11 @@ def gpu_upper(ctx, A, B):
     return ctx.upper(dev(A), dev(B)).to_host()
 
 
+def gpu_precise_one_call(ctx, A, B):
+    """brm_precise_device: mid rows computed during the plan, moved after."""
+    return ctx.precise_device(dev(A), dev(B)).to_host()
+
+
 def assert_f32_close(C32, R64):
     assert np.array_equal(C32.rpt, R64.rpt) and np.array_equal(C32.col, R64.col)
     ref = np.asarray(R64.val, np.float64)
@@ -91,6 +96,12 @@ def test_precise_matches_oracle(ctx, oracle_mod, name, A, B):
 
 
 @pytest.mark.parametrize("name,A,B", CASES, ids=[c[0] for c in CASES])
+def test_precise_one_call_matches_oracle(ctx, oracle_mod, name, A, B):
+    B = A if B is None else B
+    assert_same_csr(gpu_precise_one_call(ctx, A, B), oracle_mod.precise(A, B), name)
+
+
+@pytest.mark.parametrize("name,A,B", CASES, ids=[c[0] for c in CASES])
 def test_upper_matches_oracle(ctx, oracle_mod, name, A, B):
     B = A if B is None else B
     assert_same_csr(gpu_upper(ctx, A, B), oracle_mod.precise(A, B), name)
@@ -104,6 +115,7 @@ def test_f32(ctx, oracle_mod, name, A, B):
     assert_same_csr(C32, oracle_mod.precise(A32, B32), name + " f32 order-exact")
     assert_f32_close(C32, oracle_mod.precise(A, B))
     assert_same_csr(gpu_upper(ctx, A32, B32), C32, name + " f32 upper")
+    assert_same_csr(gpu_precise_one_call(ctx, A32, B32), C32, name + " f32 one call")
 
 
 def test_host_drop_in_matches_device(ctx):
@@ -301,6 +313,7 @@ def test_rmat_config_full(ctx, oracle_mod):
     A = brm.gen_rmat(18, int(2.35 * (1 << 18)), seed=0)
     R = oracle_mod.precise(A, A)
     assert_same_csr(gpu_precise(ctx, A, A), R, "rmat18 precise")
+    assert_same_csr(gpu_precise_one_call(ctx, A, A), R, "rmat18 precise one call")
     assert_same_csr(gpu_upper(ctx, A, A), R, "rmat18 upper")
 
 
