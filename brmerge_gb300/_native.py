@@ -36,6 +36,13 @@ class CsrC(C.Structure):
                 ("rpt", C.c_void_p), ("col", C.c_void_p), ("val", C.c_void_p)]
 
 
+class BatchC(C.Structure):
+    """Mirror of brm_batch."""
+    _fields_ = [("n", C.c_int), ("rows", C.c_longlong), ("nnz", C.c_longlong),
+                ("row_off", C.POINTER(C.c_longlong)), ("nnz_off", C.POINTER(C.c_longlong)),
+                ("crpt", C.c_void_p), ("ccol", C.c_void_p), ("cval", C.c_void_p)]
+
+
 class HostCsrC(C.Structure):
     """Mirror of brm_host_csr (generator output)."""
     _fields_ = [("M", C.c_int), ("N", C.c_int), ("nnz", C.c_int),
@@ -95,6 +102,8 @@ def lib() -> C.CDLL:
         _decl(L.brm_free, None, [vp])
         _decl(L.brm_host_cache_release, None, [])
         _decl(L.brm_kernel_launches, C.c_longlong, [])
+        _decl(L.brm_batch_precise, C.c_int, [vp, C.c_int, C.c_int, csrp, csrp, C.POINTER(BatchC)])
+        _decl(L.brm_batch_free, C.c_int, [vp, C.POINTER(BatchC)])
         _decl(L.brm_compute_flop, C.c_int, [vp, csrp, csrp, C.POINTER(C.c_longlong)])
         _decl(L.brm_upper_bound, C.c_int,
               [vp, C.c_int, csrp, csrp, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)])

@@ -30,6 +30,7 @@ CUDA_SOURCES = [
     "brm_numeric_f32.cu",
     "brm_noalloc.cu",
     "brm_hostpool.cu",
+    "brm_batch.cu",
 ]
 HOST_SOURCES = ["host/gen.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

@@ -444,6 +444,23 @@ double now_sec()
     return duration<double>(steady_clock::now().time_since_epoch()).count();
 }
 
+// Result arrays of a host drop-in, released unless handed to the caller.
+template <typename T>
+struct HostResult {
+    int *rpt = nullptr;
+    int *col = nullptr;
+    T *val = nullptr;
+    bool keep = false;
+    ~HostResult()
+    {
+        if (!keep) {
+            brm_free(rpt);
+            brm_free(col);
+            brm_free(val);
+        }
+    }
+};
+
 // Host drop-in shared by the four host entry points.
 template <typename T>
 int host_call(bool upper, const int *arpt, const int *acol, const T *aval, const int *brpt,
@@ -484,6 +501,32 @@ int host_call(bool upper, const int *arpt, const int *acol, const T *aval, const
     double t_pre = now_sec();
     int cnnz = 0;
     double t_sym0 = 0, t_sym1 = 0, t_num0 = 0, t_num1 = 0;
+    // result arrays: page-locked, device-mapped blocks from the host cache
+    // (released by brm_free); the kernels store ccol/cval straight into them
+    // when the mapping exists, else into device buffers that are copied back
+    HostResult<T> R;
+    int *dcol = nullptr;
+    void *dval = nullptr;
+    auto alloc_results = [&]() -> int {
+        R.rpt = (int *)brm::host_alloc(4 * ((size_t)M + 1));
+        R.col = (int *)brm::host_alloc(4 * (size_t)(cnnz > 0 ? cnnz : 1));
+        R.val = (T *)brm::host_alloc(sizeof(T) * (size_t)(cnnz > 0 ? cnnz : 1));
+        if (!R.rpt || !R.col || !R.val)
+            return BRM_ERR_ALLOC;
+        void *pc = nullptr, *pv = nullptr;
+        if (cudaHostGetDevicePointer(&pc, R.col, 0) == cudaSuccess &&
+            cudaHostGetDevicePointer(&pv, R.val, 0) == cudaSuccess) {
+            dcol = (int *)pc;
+            dval = pv;
+        } else {
+            (void)cudaGetLastError();
+            BRM_TRY(grow(ctx->io_ccol, 4 * (size_t)cnnz));
+            BRM_TRY(grow(ctx->io_cval, sizeof(T) * (size_t)cnnz));
+            dcol = (int *)ctx->io_ccol.p;
+            dval = ctx->io_cval.p;
+        }
+        return BRM_SUCCESS;
+    };
     if (!upper) {
         // one call: symbolic with the mid rows computed in passing, numeric
         t_sym0 = now_sec();
@@ -492,13 +535,10 @@ int host_call(bool upper, const int *arpt, const int *acol, const T *aval, const
         BRM_TRY(plan_phase(ctx, &A, &B, (int *)ctx->io_crpt.p, false, false, dtype));
         cnnz = (int)ctx->h_cnt->cnnz;
         t_sym1 = now_sec();
-        BRM_TRY(grow(ctx->io_ccol, 4 * (size_t)cnnz));
-        BRM_TRY(grow(ctx->io_cval, sizeof(T) * (size_t)cnnz));
+        BRM_TRY(alloc_results());
         t_num0 = now_sec();
-        BRM_TRY(numeric_launch(ctx, dtype, false, &A, &B, (const int *)ctx->io_crpt.p,
-                               (int *)ctx->io_ccol.p, ctx->io_cval.p, true));
-        BRM_TRY(read_err(ctx));
-        t_num1 = now_sec();
+        BRM_TRY(numeric_launch(ctx, dtype, false, &A, &B, (const int *)ctx->io_crpt.p, dcol, dval,
+                               true));
     } else {
         t_sym0 = now_sec();
         BRM_TRY(plan_phase(ctx, &A, &B, nullptr, true, false));
@@ -511,37 +551,22 @@ int host_call(bool upper, const int *arpt, const int *acol, const T *aval, const
         BRM_TRY(device_err_status(ctx->h_cnt->err));
         cnnz = (int)ctx->h_cnt->cnnz;
         t_sym1 = now_sec();
-        BRM_TRY(grow(ctx->io_ccol, 4 * (size_t)cnnz));
-        BRM_TRY(grow(ctx->io_cval, sizeof(T) * (size_t)cnnz));
+        BRM_TRY(alloc_results());
         t_num0 = now_sec();
         brm::launch_compact(dtype == BRM_F64 ? 0 : 1, ctx->plan, (const int *)ctx->bar_col.p,
-                            ctx->bar_val.p, (const int *)ctx->io_crpt.p, (int *)ctx->io_ccol.p,
-                            ctx->io_cval.p, s);
+                            ctx->bar_val.p, (const int *)ctx->io_crpt.p, dcol, dval, s);
         BRM_CK(cudaGetLastError());
-        BRM_TRY(read_err(ctx));
-        t_num1 = now_sec();
     }
-    // result arrays: page-locked blocks from the host cache (released by brm_free)
-    int *crpt = (int *)brm::host_alloc(4 * ((size_t)M + 1));
-    int *ccol = (int *)brm::host_alloc(4 * (size_t)(cnnz > 0 ? cnnz : 1));
-    T *cval = (T *)brm::host_alloc(sizeof(T) * (size_t)(cnnz > 0 ? cnnz : 1));
-    if (!crpt || !ccol || !cval) {
-        brm_free(crpt);
-        brm_free(ccol);
-        brm_free(cval);
-        return BRM_ERR_ALLOC;
+    BRM_CK(cudaMemcpyAsync(R.rpt, ctx->io_crpt.p, 4 * ((size_t)M + 1), cudaMemcpyDeviceToHost, s));
+    if (dcol == (int *)ctx->io_ccol.p && cnnz > 0) {
+        BRM_CK(cudaMemcpyAsync(R.col, dcol, 4 * (size_t)cnnz, cudaMemcpyDeviceToHost, s));
+        BRM_CK(cudaMemcpyAsync(R.val, dval, sizeof(T) * (size_t)cnnz, cudaMemcpyDeviceToHost, s));
     }
-    cudaError_t e1 = cudaMemcpyAsync(crpt, ctx->io_crpt.p, 4 * ((size_t)M + 1), cudaMemcpyDeviceToHost, s);
-    cudaError_t e2 = cudaMemcpyAsync(ccol, ctx->io_ccol.p, 4 * (size_t)cnnz, cudaMemcpyDeviceToHost, s);
-    cudaError_t e3 = cudaMemcpyAsync(cval, ctx->io_cval.p, sizeof(T) * (size_t)cnnz, cudaMemcpyDeviceToHost, s);
-    cudaError_t e4 = cudaStreamSynchronize(s);
-    if (e1 != cudaSuccess || e2 != cudaSuccess || e3 != cudaSuccess || e4 != cudaSuccess) {
-        brm_free(crpt);
-        brm_free(ccol);
-        brm_free(cval);
-        (void)cudaGetLastError();
-        return BRM_ERR_CUDA;
-    }
+    BRM_TRY(read_err(ctx));  // synchronises the stream
+    t_num1 = now_sec();
+    int *crpt = R.rpt, *ccol = R.col;
+    T *cval = R.val;
+    R.keep = true;
     double t_end = now_sec();
     *crpt_ = crpt;
     *ccol_ = ccol;
@@ -569,6 +594,10 @@ int host_call(bool upper, const int *arpt, const int *acol, const T *aval, const
 }
 
 }  // namespace
+
+cudaStream_t brm::context_stream(brm_context ctx) { return ctx->stream; }
+
+int brm::context_num_sms(brm_context ctx) { return ctx->num_sms; }
 
 extern "C" {
 

@@ -1,0 +1,330 @@
+// brm_batch.cu -- many independent products C_i = A_i * B_i in one pipeline.
+//
+// The reference multiplies one pair per call (BRMerge-SpGEMM/inc/spgemm.h:
+// 468-735).  Rows of C depend only on their own A row and the B rows it
+// names, so a batch of n pairs is one product of block-diagonal matrices:
+// A_bd = diag(A_1 .. A_n) and B_bd = diag(B_1 .. B_n), with A_i's columns
+// shifted by the B rows before it and B_i's columns by the B columns before
+// it.  Every row of C_bd is the merge of exactly the lists of its own pair,
+// in the same leaf order, so each C_i is bit-identical to a separate call.
+// The batch runs as one Precise pipeline (about twenty kernel launches for
+// all pairs together); C_i's columns are shifted back afterwards.
+#include <algorithm>
+#include <climits>
+#include <cstdlib>
+#include <cstring>
+#include <vector>
+
+#include "brm_common.cuh"
+#include "brm_kernels.h"
+#include "brmerge.h"
+
+namespace brm {
+
+// One pair on the device: its input views and its offsets in the
+// block-diagonal operands (A rows, A entries, B rows = A columns, B entries,
+// B columns = C columns).
+struct BatchPair {
+    const int *arpt, *acol, *brpt, *bcol;
+    const void *aval, *bval;
+    long long row_a, nnz_a, row_b, nnz_b, col_b;
+    int M, K, N, nnzA, nnzB;
+};
+
+// Index of the pair whose [off[i], off[i+1]) holds x (off non-decreasing,
+// off[0] = 0, x < off[n]); empty pairs are skipped.
+__device__ __forceinline__ int pair_of(const long long *off, int n, long long x)
+{
+    int lo = 0, hi = n;  // invariant: off[lo] <= x < off[hi]
+    while (hi - lo > 1) {
+        const int m = (lo + hi) >> 1;
+        if (off[m] <= x)
+            lo = m;
+        else
+            hi = m;
+    }
+    return lo;
+}
+
+// Row pointers of A_bd (which = 0) or B_bd (which = 1): one thread per row
+// of the concatenation (plus the closing entry).
+__global__ void __launch_bounds__(256) k_batch_rows(const BatchPair *pairs, int n,
+                                                    const long long *row_off, long long rows,
+                                                    int which, int *rpt)
+{
+    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r <= rows;
+         r += (long long)gridDim.x * blockDim.x) {
+        if (r == rows) {
+            const BatchPair &q = pairs[n - 1];
+            rpt[r] = which == 0 ? (int)(q.nnz_a + q.nnzA) : (int)(q.nnz_b + q.nnzB);
+            continue;
+        }
+        const int i = pair_of(row_off, n, r);
+        const BatchPair &q = pairs[i];
+        if (which == 0)
+            rpt[r] = (int)(q.nnz_a + q.arpt[r - q.row_a]);
+        else
+            rpt[r] = (int)(q.nnz_b + q.brpt[r - q.row_b]);
+    }
+}
+
+// Columns and values of A_bd (which = 0) or B_bd (which = 1): one thread per
+// entry of the concatenation.
+template <typename T>
+__global__ void __launch_bounds__(256) k_batch_entries(const BatchPair *pairs, int n,
+                                                       const long long *nnz_off, long long nnz,
+                                                       int which, int *col, T *val)
+{
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < nnz;
+         e += (long long)gridDim.x * blockDim.x) {
+        const int i = pair_of(nnz_off, n, e);
+        const BatchPair &q = pairs[i];
+        if (which == 0) {
+            const long long j = e - q.nnz_a;
+            col[e] = (int)(q.acol[j] + q.row_b);
+            val[e] = ((const T *)q.aval)[j];
+        } else {
+            const long long j = e - q.nnz_b;
+            col[e] = (int)(q.bcol[j] + q.col_b);
+            val[e] = ((const T *)q.bval)[j];
+        }
+    }
+}
+
+// C_bd -> the pairs' own columns, and each pair's first entry in C_bd.  One
+// warp per row.
+__global__ void __launch_bounds__(256) k_batch_unshift(const BatchPair *pairs, int n,
+                                                       const long long *row_off, int rows,
+                                                       const int *crpt, int *ccol,
+                                                       long long *nnz_first)
+{
+    const int lane = threadIdx.x & 31;
+    const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+    for (long long r = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < rows;
+         r += nwarps) {
+        const int i = pair_of(row_off, n, r);
+        const int shift = (int)pairs[i].col_b;
+        const int s = crpt[r], e = crpt[r + 1];
+        for (int j = s + lane; j < e; j += 32)
+            ccol[j] -= shift;
+    }
+    // pair starts (every pair, including empty ones)
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i <= n;
+         i += (long long)gridDim.x * blockDim.x)
+        nnz_first[i] = crpt[i < n ? pairs[i].row_a : rows];
+}
+
+}  // namespace brm
+
+namespace {
+
+struct Buf {
+    void *p = nullptr;
+    size_t cap = 0;
+};
+
+int grow_buf(Buf &b, size_t bytes, cudaStream_t s)
+{
+    if (bytes <= b.cap && b.p)
+        return BRM_SUCCESS;
+    if (b.p)
+        cudaFreeAsync(b.p, s);
+    b.p = nullptr;
+    b.cap = 0;
+    bytes = std::max<size_t>(bytes, 256);
+    if (cudaMallocAsync(&b.p, bytes, s) != cudaSuccess) {
+        (void)cudaGetLastError();
+        return BRM_ERR_ALLOC;
+    }
+    b.cap = bytes;
+    return BRM_SUCCESS;
+}
+
+size_t a256(size_t x) { return (x + 255) & ~size_t(255); }
+
+}  // namespace
+
+extern "C" {
+
+int brm_batch_precise(brm_context ctx, brm_dtype dtype, int n, const brm_csr *A, const brm_csr *B,
+                      brm_batch *out)
+{
+    if (!ctx || !out || n < 0 || (n > 0 && (!A || !B)))
+        return BRM_ERR_INVALID_VALUE;
+    if (dtype != BRM_F64 && dtype != BRM_F32)
+        return BRM_ERR_INVALID_VALUE;
+    std::memset(out, 0, sizeof(*out));
+    out->n = n;
+    // offsets of every pair in the block-diagonal operands
+    std::vector<brm::BatchPair> hp((size_t)n);
+    std::vector<long long> off((size_t)(n + 1) * 4, 0);  // row_a, nnz_a, row_b, nnz_b
+    long long ra = 0, na = 0, rb = 0, nb = 0, cb = 0;
+    for (int i = 0; i < n; i++) {
+        const brm_csr &a = A[i], &b = B[i];
+        if (a.M < 0 || a.N < 0 || b.M < 0 || b.N < 0 || a.nnz < 0 || b.nnz < 0 || a.N != b.M ||
+            !a.rpt || !b.rpt || (a.nnz > 0 && (!a.col || !a.val)) ||
+            (b.nnz > 0 && (!b.col || !b.val)))
+            return BRM_ERR_INVALID_VALUE;
+        brm::BatchPair &q = hp[(size_t)i];
+        q.arpt = a.rpt;
+        q.acol = a.col;
+        q.aval = a.val;
+        q.brpt = b.rpt;
+        q.bcol = b.col;
+        q.bval = b.val;
+        q.M = a.M;
+        q.K = a.N;
+        q.N = b.N;
+        q.nnzA = a.nnz;
+        q.nnzB = b.nnz;
+        q.row_a = ra;
+        q.nnz_a = na;
+        q.row_b = rb;
+        q.nnz_b = nb;
+        q.col_b = cb;
+        off[(size_t)i] = ra;
+        off[(size_t)(n + 1) + i] = na;
+        off[(size_t)2 * (n + 1) + i] = rb;
+        off[(size_t)3 * (n + 1) + i] = nb;
+        ra += a.M;
+        na += a.nnz;
+        rb += a.N;
+        nb += b.nnz;
+        cb += b.N;
+    }
+    off[(size_t)n] = ra;
+    off[(size_t)(n + 1) + n] = na;
+    off[(size_t)2 * (n + 1) + n] = rb;
+    off[(size_t)3 * (n + 1) + n] = nb;
+    if (ra >= INT_MAX || na > INT_MAX || rb >= INT_MAX || nb > INT_MAX || cb > INT_MAX)
+        return BRM_ERR_CAPACITY;  // the concatenation must fit int32 indices
+    out->rows = ra;
+    if (n == 0)
+        return BRM_SUCCESS;
+    cudaStream_t s = brm::context_stream(ctx);
+    const size_t vb = dtype == BRM_F64 ? 8 : 4;
+    // device scratch: pair table, offsets, A_bd, B_bd (freed at the end)
+    Buf tab, abd, bbd;
+    auto cleanup = [&]() {
+        if (tab.p)
+            cudaFreeAsync(tab.p, s);
+        if (abd.p)
+            cudaFreeAsync(abd.p, s);
+        if (bbd.p)
+            cudaFreeAsync(bbd.p, s);
+    };
+    const size_t b_pairs = a256(sizeof(brm::BatchPair) * (size_t)n);
+    const size_t b_off = sizeof(long long) * off.size();
+    int st = grow_buf(tab, b_pairs + a256(b_off) + sizeof(long long) * (size_t)(n + 1), s);
+    const size_t a_rpt = a256(4 * (size_t)(ra + 1)), a_col = a256(4 * (size_t)std::max(na, 1LL));
+    const size_t b_rpt = a256(4 * (size_t)(rb + 1)), b_col = a256(4 * (size_t)std::max(nb, 1LL));
+    if (st == BRM_SUCCESS)
+        st = grow_buf(abd, a_rpt + a_col + vb * (size_t)std::max(na, 1LL), s);
+    if (st == BRM_SUCCESS)
+        st = grow_buf(bbd, b_rpt + b_col + vb * (size_t)std::max(nb, 1LL), s);
+    if (st != BRM_SUCCESS) {
+        cleanup();
+        return st;
+    }
+    brm::BatchPair *dp = (brm::BatchPair *)tab.p;
+    long long *doff = (long long *)((char *)tab.p + b_pairs);
+    long long *dfirst = (long long *)((char *)tab.p + b_pairs + a256(b_off));
+    int *A_rpt = (int *)abd.p, *A_col = (int *)((char *)abd.p + a_rpt);
+    void *A_val = (char *)abd.p + a_rpt + a_col;
+    int *B_rpt = (int *)bbd.p, *B_col = (int *)((char *)bbd.p + b_rpt);
+    void *B_val = (char *)bbd.p + b_rpt + b_col;
+    cudaError_t e = cudaMemcpyAsync(dp, hp.data(), sizeof(brm::BatchPair) * (size_t)n,
+                                    cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(doff, off.data(), b_off, cudaMemcpyHostToDevice, s);
+    const int sms = brm::context_num_sms(ctx);
+    if (e == cudaSuccess) {
+        const int g = std::max(sms, 1) * 16;
+        brm::k_batch_rows<<<g, 256, 0, s>>>(dp, n, doff, ra, 0, A_rpt);
+        brm::count_launch();
+        brm::k_batch_rows<<<g, 256, 0, s>>>(dp, n, doff + 2 * (n + 1), rb, 1, B_rpt);
+        brm::count_launch();
+        if (dtype == BRM_F64) {
+            brm::k_batch_entries<double><<<g, 256, 0, s>>>(dp, n, doff + (n + 1), na, 0, A_col,
+                                                           (double *)A_val);
+            brm::count_launch();
+            brm::k_batch_entries<double><<<g, 256, 0, s>>>(dp, n, doff + 3 * (n + 1), nb, 1,
+                                                           B_col, (double *)B_val);
+            brm::count_launch();
+        } else {
+            brm::k_batch_entries<float><<<g, 256, 0, s>>>(dp, n, doff + (n + 1), na, 0, A_col,
+                                                          (float *)A_val);
+            brm::count_launch();
+            brm::k_batch_entries<float><<<g, 256, 0, s>>>(dp, n, doff + 3 * (n + 1), nb, 1,
+                                                          B_col, (float *)B_val);
+            brm::count_launch();
+        }
+        e = cudaGetLastError();
+    }
+    if (e != cudaSuccess) {
+        (void)cudaGetLastError();
+        cleanup();
+        return BRM_ERR_CUDA;
+    }
+    // one Precise call on the block-diagonal operands
+    brm_csr Abd{(int)ra, (int)rb, (int)na, A_rpt, A_col, A_val};
+    brm_csr Bbd{(int)rb, (int)cb, (int)nb, B_rpt, B_col, B_val};
+    int *crpt = nullptr, *ccol = nullptr;
+    void *cval = nullptr;
+    int cnnz = 0;
+    st = brm_precise_device(ctx, dtype, &Abd, &Bbd, &crpt, &ccol, &cval, &cnnz, nullptr);
+    if (st != BRM_SUCCESS) {
+        cleanup();
+        return st;
+    }
+    {
+        const int g = std::max(sms, 1) * 16;
+        brm::k_batch_unshift<<<g, 256, 0, s>>>(dp, n, doff, (int)ra, crpt, ccol, dfirst);
+        brm::count_launch();
+    }
+    long long *hf = (long long *)std::malloc(sizeof(long long) * (size_t)(n + 1));
+    long long *hr = (long long *)std::malloc(sizeof(long long) * (size_t)(n + 1));
+    e = cudaGetLastError();
+    if (hf && hr && e == cudaSuccess)
+        e = cudaMemcpyAsync(hf, dfirst, sizeof(long long) * (size_t)(n + 1), cudaMemcpyDeviceToHost,
+                            s);
+    if (e == cudaSuccess)
+        e = cudaStreamSynchronize(s);
+    cleanup();
+    if (!hf || !hr || e != cudaSuccess) {
+        (void)cudaGetLastError();
+        std::free(hf);
+        std::free(hr);
+        brm_device_free(ctx, crpt);
+        brm_device_free(ctx, ccol);
+        brm_device_free(ctx, cval);
+        return (!hf || !hr) ? BRM_ERR_ALLOC : BRM_ERR_CUDA;
+    }
+    std::memcpy(hr, off.data(), sizeof(long long) * (size_t)(n + 1));
+    out->row_off = hr;
+    out->nnz_off = hf;
+    out->nnz = cnnz;
+    out->crpt = crpt;
+    out->ccol = ccol;
+    out->cval = cval;
+    return BRM_SUCCESS;
+}
+
+int brm_batch_free(brm_context ctx, brm_batch *b)
+{
+    if (!b)
+        return BRM_SUCCESS;
+    int st = BRM_SUCCESS;
+    if (b->crpt)
+        st = brm_device_free(ctx, b->crpt);
+    if (b->ccol && st == BRM_SUCCESS)
+        st = brm_device_free(ctx, b->ccol);
+    if (b->cval && st == BRM_SUCCESS)
+        st = brm_device_free(ctx, b->cval);
+    std::free(b->row_off);
+    std::free(b->nnz_off);
+    std::memset(b, 0, sizeof(*b));
+    return st;
+}
+
+}  // extern "C"

@@ -4,8 +4,13 @@
 #include <cuda_runtime.h>
 
 #include "brm_plan.h"
+#include "brmerge.h"
 
 namespace brm {
+
+// The stream and SM count of a context (brm_api.cu).
+cudaStream_t context_stream(brm_context ctx);
+int context_num_sms(brm_context ctx);
 
 // Counts one kernel launch of this library (brm_kernel_launches reports the
 // process-wide total); every launch site calls it right after <<<...>>>.

@@ -274,6 +274,39 @@ class Context:
         """brm_precise_device: one call, callee-allocated outputs (no copy)."""
         return self._device_call(False, A, B, timing)
 
+    def batch_precise(self, pairs) -> list:
+        """brm_batch_precise: C_i = A_i * B_i for a list of (A_i, B_i)
+        DeviceCSR pairs of one value type, in one pipeline.  Returns the C_i
+        as DeviceCSR views into the batch's concatenated arrays."""
+        import torch
+        n = len(pairs)
+        if n == 0:
+            return []
+        dt = pairs[0][0].val.dtype
+        if any(a.val.dtype != dt or b.val.dtype != dt for a, b in pairs):
+            raise TypeError("all pairs of a batch must have the same value type")
+        code = _dtype_code(np.float64 if dt == torch.float64 else np.float32)
+        As = (_native.CsrC * n)(*[a.c() for a, _ in pairs])
+        Bs = (_native.CsrC * n)(*[b.c() for _, b in pairs])
+        out = _native.BatchC()
+        _native.check(self._L.brm_batch_precise(self._h, code, n, As, Bs, C.byref(out)),
+                      "brm_batch_precise")
+        dev = pairs[0][0].rpt.device
+        vt = "<f8" if dt == torch.float64 else "<f4"
+        crpt = _device_tensor(self._L, out.crpt, out.rows + 1, "<i4", dev)
+        ccol = _device_tensor(self._L, out.ccol, out.nnz, "<i4", dev)
+        cval = _device_tensor(self._L, out.cval, out.nnz, vt, dev)
+        roff = np.ctypeslib.as_array(out.row_off, shape=(n + 1,)).copy()
+        noff = np.ctypeslib.as_array(out.nnz_off, shape=(n + 1,)).copy()
+        out.crpt = out.ccol = out.cval = None  # owned by the tensors now
+        self._L.brm_batch_free(self._h, C.byref(out))
+        res = []
+        for i, (a, b) in enumerate(pairs):
+            r0, r1, n0, n1 = int(roff[i]), int(roff[i + 1]), int(noff[i]), int(noff[i + 1])
+            rpt = (crpt[r0:r1 + 1] - n0).to(torch.int32)
+            res.append(DeviceCSR(a.M, b.N, rpt, ccol[n0:n1], cval[n0:n1]))
+        return res
+
     def upper(self, A: DeviceCSR, B: DeviceCSR, timing=None) -> DeviceCSR:
         """brm_upper_device: one call, callee-allocated outputs (no copy)."""
         return self._device_call(True, A, B, timing)

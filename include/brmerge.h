@@ -171,6 +171,36 @@ void brm_host_cache_release(void);
  * region to count the GPU work the region issued. */
 long long brm_kernel_launches(void);
 
+/* ---- batches: many independent products in one pipeline ---------------------- */
+
+/* Result of brm_batch_precise: the n products C_i = A_i * B_i concatenated
+ * by rows.  C_i has row_off[i+1] - row_off[i] rows; its row pointers are
+ * crpt[row_off[i] .. row_off[i+1]] minus nnz_off[i] (crpt holds offsets into
+ * the concatenated ccol/cval), and its columns are C_i's own (0 .. N_i-1).
+ * crpt, ccol and cval are device memory owned by the batch (brm_batch_free);
+ * row_off and nnz_off are host arrays of n + 1 entries. */
+typedef struct brm_batch {
+    int n;
+    long long rows;       /* sum of M_i */
+    long long nnz;        /* sum of nnz(C_i) */
+    long long *row_off;   /* host, n + 1 */
+    long long *nnz_off;   /* host, n + 1 */
+    int *crpt;            /* device, rows + 1 */
+    int *ccol;            /* device, nnz */
+    void *cval;           /* device, nnz (dtype) */
+} brm_batch;
+
+/* C_i = A_i * B_i (BRMerge-Precise) for n independent pairs of device CSR
+ * matrices of one value type, in one pipeline: the pairs form one product of
+ * block-diagonal matrices, so the kernels see every row of every pair at
+ * once.  Each C_i is bit-identical to brm_precise_device(A_i, B_i).  No
+ * counterpart in the reference (one pair per call).  The concatenated rows,
+ * entries and columns must each fit int32 (else BRM_ERR_CAPACITY); nnz of
+ * all C_i together must fit int32 (else BRM_ERR_OVERFLOW). */
+int brm_batch_precise(brm_context ctx, brm_dtype dtype, int n, const brm_csr *A, const brm_csr *B,
+                      brm_batch *out);
+int brm_batch_free(brm_context ctx, brm_batch *batch);
+
 /* ---- helpers ---------------------------------------------------------------- */
 
 /* Intermediate products of A*B (compute_flop, spgemm.h:59-66); GFLOP/s in
