@@ -72,6 +72,12 @@ struct brm_context_s {
     int last_err = 0;
     // device copies for the host drop-ins
     DevBuf io_arpt, io_acol, io_aval, io_brpt, io_bcol, io_bval, io_crpt, io_ccol, io_cval;
+    // host drop-in, numeric by row parts: part bounds and the segment list
+    // ordered by part (device), and a second stream that copies finished
+    // parts of C back while the next part computes
+    DevBuf partbuf;
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t part_ev[brm::kMaxParts] = {};
     cudaEvent_t ev[kNumEvents] = {};
 };
 
@@ -292,9 +298,11 @@ int plan_phase(brm_context ctx, const brm_csr *A, const brm_csr *B, int *crpt, b
     if (ctx->validate)
         BRM_TRY(validate_pair(ctx, A, B));
     brm::CsrDev a = to_dev(A), b = to_dev(B);
-    brm::PlanDev P = ctx->plan;
-    P.M = A->M;
     ctx->plan.M = A->M;
+    ctx->plan.r_lo = 0;
+    ctx->plan.r_hi = A->M;
+    ctx->plan.seg_range = nullptr;
+    brm::PlanDev P = ctx->plan;
     cudaStream_t s = ctx->stream;
     ev_record(ctx, timed, 0);
     BRM_CK(cudaMemsetAsync(P.cnt, 0, sizeof(brm::Counters), s));
@@ -361,14 +369,29 @@ bool plan_matches(brm_context ctx, const brm_csr *A, const brm_csr *B)
 }
 
 // use_mid: take the mid rows from the one-call scratch (plan_phase fused).
+// A row part of the numeric phase: rows [r_lo, r_hi) and, when seg_list is
+// set, the part's slice seg_range of that reordered segment list.
+struct RowPart {
+    int r_lo = 0;
+    int r_hi = -1;  // -1: every row
+    const int *seg_range = nullptr;
+    const int *seg_list = nullptr;
+};
+
 int numeric_launch(brm_context ctx, brm_dtype dtype, bool upper, const brm_csr *A,
-                   const brm_csr *B, const int *crpt, int *ccol, void *cval, bool use_mid = false)
+                   const brm_csr *B, const int *crpt, int *ccol, void *cval, bool use_mid = false,
+                   const RowPart &part = RowPart())
 {
     const bool mid = use_mid && ctx->mid_ready && !upper;
     if (ctx->spill_bytes)
         BRM_TRY(grow(ctx->spill, ctx->spill_bytes));
     cudaStream_t s = ctx->stream;
     brm::PlanDev P = ctx->plan;
+    P.r_lo = part.r_lo;
+    P.r_hi = part.r_hi < 0 ? A->M : part.r_hi;
+    P.seg_range = part.seg_range;
+    if (part.seg_list)
+        P.seg_list = (int *)part.seg_list;
     BRM_CK(cudaMemsetAsync(&P.cnt->work_num, 0, 2 * sizeof(int), s));  // work_num, err
     BRM_CK(cudaMemsetAsync(&P.cnt->work_bnum, 0, 2 * sizeof(int), s));  // work_bnum, work_seg
     BRM_TRY(grow(ctx->splitbuf, ((size_t)ctx->h_cnt->table_cap + 1) * sizeof(int)));
@@ -444,6 +467,76 @@ double now_sec()
     return duration<double>(steady_clock::now().time_since_epoch()).count();
 }
 
+// Host drop-in numeric phase (Precise, after a fused plan_phase) with the
+// copy of C overlapped: the rows are cut into parts of about equal nnz, the
+// segment list is grouped by part, and while part p+1 computes on the
+// context stream, the copy stream moves part p of ccol/cval to the host
+// blocks.  crpt (device io_crpt) is copied first; it also gives the cuts.
+int numeric_by_parts(brm_context ctx, brm_dtype dtype, const brm_csr *A, const brm_csr *B, int M,
+                     int cnnz, size_t vb, int *h_rpt, int *h_col, void *h_val, int *dcol,
+                     void *dval)
+{
+    cudaStream_t s = ctx->stream, cs = ctx->copy_stream;
+    const int *d_rpt = (const int *)ctx->io_crpt.p;
+    BRM_CK(cudaMemcpyAsync(h_rpt, d_rpt, 4 * ((size_t)M + 1), cudaMemcpyDeviceToHost, s));
+    // parts: one per 32 MB of C, at most kHostParts
+    constexpr int kHostParts = 4;
+    const long long bytes = (long long)cnnz * (long long)(4 + vb);
+    const int nparts = (int)std::min<long long>(kHostParts, std::max<long long>(1, bytes >> 25));
+    if (nparts <= 1) {
+        BRM_TRY(numeric_launch(ctx, dtype, false, A, B, d_rpt, dcol, dval, true));
+        if (cnnz > 0) {
+            BRM_CK(cudaMemcpyAsync(h_col, dcol, 4 * (size_t)cnnz, cudaMemcpyDeviceToHost, s));
+            BRM_CK(cudaMemcpyAsync((char *)h_val, dval, vb * (size_t)cnnz, cudaMemcpyDeviceToHost, s));
+        }
+        return BRM_SUCCESS;
+    }
+    BRM_CK(cudaStreamSynchronize(s));  // h_rpt
+    int pb[brm::kMaxParts + 1];
+    pb[0] = 0;
+    for (int p = 1; p < nparts; p++) {
+        const long long target = (long long)cnnz * p / nparts;
+        const int r = (int)(std::lower_bound(h_rpt, h_rpt + M + 1, (int)target) - h_rpt);
+        pb[p] = std::max(pb[p - 1], std::min(r, M));
+    }
+    pb[nparts] = M;
+    // device: pb, cnt, fill, ranges, reordered segment list
+    const int nseg = ctx->h_cnt->n_seg;
+    const size_t b_small = a256(sizeof(int) * (size_t)(4 * brm::kMaxParts + 4));
+    BRM_TRY(grow(ctx->partbuf, b_small + sizeof(int) * (size_t)(nseg + 1)));
+    int *d_pb = (int *)ctx->partbuf.p;
+    int *d_cnt = d_pb + (brm::kMaxParts + 1);
+    int *d_fill = d_cnt + brm::kMaxParts;
+    int *d_ranges = d_fill + brm::kMaxParts;
+    int *d_list = (int *)((char *)ctx->partbuf.p + b_small);
+    BRM_CK(cudaMemcpyAsync(d_pb, pb, sizeof(int) * (size_t)(nparts + 1), cudaMemcpyHostToDevice, s));
+    BRM_CK(cudaMemsetAsync(d_cnt, 0, sizeof(int) * 2 * brm::kMaxParts, s));  // cnt, fill
+    if (nseg > 0)
+        brm::launch_seg_partition(ctx->plan, d_pb, nparts, d_cnt, d_fill, d_list, d_ranges,
+                                  ctx->num_sms, s);
+    for (int p = 0; p < nparts; p++) {
+        RowPart part;
+        part.r_lo = pb[p];
+        part.r_hi = pb[p + 1];
+        if (nseg > 0) {
+            part.seg_range = d_ranges + 2 * p;
+            part.seg_list = d_list;
+        }
+        BRM_TRY(numeric_launch(ctx, dtype, false, A, B, d_rpt, dcol, dval, true, part));
+        const long long e0 = h_rpt[pb[p]], e1 = h_rpt[pb[p + 1]];
+        if (e1 > e0) {
+            BRM_CK(cudaEventRecord(ctx->part_ev[p], s));
+            BRM_CK(cudaStreamWaitEvent(cs, ctx->part_ev[p], 0));
+            BRM_CK(cudaMemcpyAsync(h_col + e0, dcol + e0, 4 * (size_t)(e1 - e0),
+                                   cudaMemcpyDeviceToHost, cs));
+            BRM_CK(cudaMemcpyAsync((char *)h_val + vb * (size_t)e0, (char *)dval + vb * (size_t)e0,
+                                   vb * (size_t)(e1 - e0), cudaMemcpyDeviceToHost, cs));
+        }
+    }
+    BRM_CK(cudaStreamSynchronize(cs));
+    return BRM_SUCCESS;
+}
+
 // Result arrays of a host drop-in, released unless handed to the caller.
 template <typename T>
 struct HostResult {
@@ -500,10 +593,13 @@ int host_call(bool upper, const int *arpt, const int *acol, const T *aval, const
     BRM_TRY(grow(ctx->io_crpt, 4 * ((size_t)M + 1)));
     double t_pre = now_sec();
     int cnnz = 0;
+    bool copied = false;  // C already copied back part by part
     double t_sym0 = 0, t_sym1 = 0, t_num0 = 0, t_num1 = 0;
-    // result arrays: page-locked, device-mapped blocks from the host cache
-    // (released by brm_free); the kernels store ccol/cval straight into them
-    // when the mapping exists, else into device buffers that are copied back
+    // result arrays: page-locked blocks from the host cache (released by
+    // brm_free).  The kernels write C to device buffers, which are copied
+    // back: on this part, stores from the kernels straight into mapped host
+    // memory ran the numeric phase at the host link's speed and took longer
+    // than the device phase plus one copy.
     HostResult<T> R;
     int *dcol = nullptr;
     void *dval = nullptr;
@@ -513,18 +609,10 @@ int host_call(bool upper, const int *arpt, const int *acol, const T *aval, const
         R.val = (T *)brm::host_alloc(sizeof(T) * (size_t)(cnnz > 0 ? cnnz : 1));
         if (!R.rpt || !R.col || !R.val)
             return BRM_ERR_ALLOC;
-        void *pc = nullptr, *pv = nullptr;
-        if (cudaHostGetDevicePointer(&pc, R.col, 0) == cudaSuccess &&
-            cudaHostGetDevicePointer(&pv, R.val, 0) == cudaSuccess) {
-            dcol = (int *)pc;
-            dval = pv;
-        } else {
-            (void)cudaGetLastError();
-            BRM_TRY(grow(ctx->io_ccol, 4 * (size_t)cnnz));
-            BRM_TRY(grow(ctx->io_cval, sizeof(T) * (size_t)cnnz));
-            dcol = (int *)ctx->io_ccol.p;
-            dval = ctx->io_cval.p;
-        }
+        BRM_TRY(grow(ctx->io_ccol, 4 * (size_t)cnnz));
+        BRM_TRY(grow(ctx->io_cval, sizeof(T) * (size_t)cnnz));
+        dcol = (int *)ctx->io_ccol.p;
+        dval = ctx->io_cval.p;
         return BRM_SUCCESS;
     };
     if (!upper) {
@@ -537,8 +625,9 @@ int host_call(bool upper, const int *arpt, const int *acol, const T *aval, const
         t_sym1 = now_sec();
         BRM_TRY(alloc_results());
         t_num0 = now_sec();
-        BRM_TRY(numeric_launch(ctx, dtype, false, &A, &B, (const int *)ctx->io_crpt.p, dcol, dval,
-                               true));
+        BRM_TRY(numeric_by_parts(ctx, dtype, &A, &B, M, cnnz, sizeof(T), R.rpt, R.col, R.val, dcol,
+                                 dval));
+        copied = true;
     } else {
         t_sym0 = now_sec();
         BRM_TRY(plan_phase(ctx, &A, &B, nullptr, true, false));
@@ -557,10 +646,12 @@ int host_call(bool upper, const int *arpt, const int *acol, const T *aval, const
                             ctx->bar_val.p, (const int *)ctx->io_crpt.p, dcol, dval, s);
         BRM_CK(cudaGetLastError());
     }
-    BRM_CK(cudaMemcpyAsync(R.rpt, ctx->io_crpt.p, 4 * ((size_t)M + 1), cudaMemcpyDeviceToHost, s));
-    if (dcol == (int *)ctx->io_ccol.p && cnnz > 0) {
-        BRM_CK(cudaMemcpyAsync(R.col, dcol, 4 * (size_t)cnnz, cudaMemcpyDeviceToHost, s));
-        BRM_CK(cudaMemcpyAsync(R.val, dval, sizeof(T) * (size_t)cnnz, cudaMemcpyDeviceToHost, s));
+    if (!copied) {
+        BRM_CK(cudaMemcpyAsync(R.rpt, ctx->io_crpt.p, 4 * ((size_t)M + 1), cudaMemcpyDeviceToHost, s));
+        if (cnnz > 0) {
+            BRM_CK(cudaMemcpyAsync(R.col, dcol, 4 * (size_t)cnnz, cudaMemcpyDeviceToHost, s));
+            BRM_CK(cudaMemcpyAsync(R.val, dval, sizeof(T) * (size_t)cnnz, cudaMemcpyDeviceToHost, s));
+        }
     }
     BRM_TRY(read_err(ctx));  // synchronises the stream
     t_num1 = now_sec();
@@ -639,6 +730,10 @@ int brm_create(brm_context *out)
         e = cudaMallocHost(&ctx->h_mid, sizeof(long long));
     for (int i = 0; i < kNumEvents && e == cudaSuccess; i++)
         e = cudaEventCreate(&ctx->ev[i]);
+    for (int i = 0; i < brm::kMaxParts && e == cudaSuccess; i++)
+        e = cudaEventCreateWithFlags(&ctx->part_ev[i], cudaEventDisableTiming);
+    if (e == cudaSuccess)
+        e = cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) {
         // keep freed stream-ordered allocations cached in this process so
         // repeated calls do not return memory to the driver between calls
@@ -694,6 +789,14 @@ int brm_destroy(brm_context ctx)
     for (int i = 0; i < kNumEvents; i++)
         if (ctx->ev[i])
             cudaEventDestroy(ctx->ev[i]);
+    for (int i = 0; i < brm::kMaxParts; i++)
+        if (ctx->part_ev[i])
+            cudaEventDestroy(ctx->part_ev[i]);
+    if (ctx->copy_stream) {
+        cudaStreamSynchronize(ctx->copy_stream);
+        cudaStreamDestroy(ctx->copy_stream);
+    }
+    release(ctx->partbuf);
     delete ctx;
     return BRM_SUCCESS;
 }

@@ -9,10 +9,6 @@
 // from page-locked blocks that brm_free hands back to this cache, so a
 // caller that multiplies repeatedly copies straight into pinned memory.
 //
-// The blocks are mapped into the device address space, so the numeric
-// kernels can store C straight into them over the host link (no staging in
-// device memory and no separate copy).
-//
 // Blocks are cached by capacity (multiples of 2 MiB).  A request takes the
 // smallest cached block that is at least as large and at most twice as
 // large; freed blocks beyond BRM_HOST_CACHE_MB (default 16384) of cached
@@ -80,8 +76,7 @@ void *host_alloc(size_t bytes)
         }
     }
     void *p = nullptr;
-    // mapped: kernels can store results straight into the block
-    if (cudaHostAlloc(&p, need, cudaHostAllocMapped) != cudaSuccess) {
+    if (cudaHostAlloc(&p, need, cudaHostAllocDefault) != cudaSuccess) {
         (void)cudaGetLastError();
         return std::malloc(bytes ? bytes : 1);
     }

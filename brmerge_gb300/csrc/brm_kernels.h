@@ -36,6 +36,12 @@ size_t scan_tmp_bytes(int n);
 void launch_symbolic(const CsrDev &A, const CsrDev &B, const PlanDev &P, int num_sms,
                      bool only_heavy, bool skip_mid, cudaStream_t s);
 
+// Reorders the segment list by row part (rows [pb[p], pb[p+1]), nparts <=
+// 16): out holds the parts' segments contiguously, ranges[2p..2p+1] the
+// slice of part p.  cnt and fill (nparts ints each) must be zero.
+void launch_seg_partition(const PlanDev &P, const int *pb, int nparts, int *cnt, int *fill,
+                          int *out, int *ranges, int num_sms, cudaStream_t s);
+
 // Upper compaction: C[crpt[i]..] = C_bar[scan_flop[i]..] (spgemm.h:429-444).
 void launch_compact(int dtype, const PlanDev &P, const int *bar_col, const void *bar_val,
                     const int *crpt, int *ccol, void *cval, cudaStream_t s);

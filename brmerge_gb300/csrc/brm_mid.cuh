@@ -591,7 +591,9 @@ __global__ void __launch_bounds__(256) k_mid_compact(PlanDev P, int M, const int
 {
     const int lane = threadIdx.x & 31;
     const int nwarps = (gridDim.x * blockDim.x) >> 5;
-    for (int row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; row < M; row += nwarps) {
+    const int r1 = min(M, P.r_hi);
+    for (int row = P.r_lo + ((blockIdx.x * blockDim.x + threadIdx.x) >> 5); row < r1;
+         row += nwarps) {
         if (P.mid_flop[row] == 0)
             continue;
         const long long src = P.mid_pre[row];

@@ -44,6 +44,7 @@ constexpr int kSegCap = 3072;
 constexpr int kSegCut = kSegCap / 2;      // target products between cuts
 constexpr int kSegMaxK = 65535;           // leaf index stored in 16 bits
 constexpr int kHugeFlop = 16 * kSegCap;   // heavy rows planned first (longest first)
+constexpr int kMaxParts = 16;             // row parts of a numeric phase run part by part
 constexpr int kPlanWordsLog2 = 13;
 constexpr int kPlanWords = 1 << kPlanWordsLog2;  // bitmap words per planning chunk
 constexpr int kPlanBits = kPlanWords * 32;       // 2^18 columns
@@ -156,6 +157,12 @@ struct PlanDev {
     void *long_val;        // [long_cap_elems] their values (the value type)
     long long long_cap_cols;
     long long long_cap_elems;
+    // numeric launches may cover only rows [r_lo, r_hi) (a part of C copied
+    // back while the next part computes); seg_range (device, 2 ints), when
+    // set, is the part's range of seg_list
+    int r_lo;
+    int r_hi;
+    const int *seg_range;
     Counters *cnt;
 };
 

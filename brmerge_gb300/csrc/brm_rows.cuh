@@ -624,7 +624,7 @@ __global__ void __launch_bounds__(kRowThreads, 1)
         if (item >= ntot)
             break;
         const int row = item < nheavy ? heavy[item] : mid[item - nheavy];
-        if (P.spill[row])
+        if (P.spill[row] || row < P.r_lo || row >= P.r_hi)
             continue;
         long long base;
         int expect = 0;
@@ -719,6 +719,8 @@ __global__ void __launch_bounds__(256) k_warp_numeric(CsrDev A, CsrDev B, PlanDe
     const int *rows = P.rows + (size_t)kBinWarp * A.M;
     for (int it = gw; it < n; it += nwarps) {
         const int row = rows[it];
+        if (row < P.r_lo || row >= P.r_hi)
+            continue;
         const int a0 = A.rpt[row], k = A.rpt[row + 1] - a0;
         int c, leaf;
         T v;
@@ -798,6 +800,8 @@ __global__ void __launch_bounds__(256) k_copy_numeric(CsrDev A, CsrDev B, PlanDe
     const int *rows = P.rows + (size_t)kBinCopy * A.M;
     for (int it = gw; it < n; it += nwarps) {
         const int row = rows[it];
+        if (row < P.r_lo || row >= P.r_hi)
+            continue;
         const int j = A.rpt[row] + P.copy_leaf[row];
         const int b = A.col[j];
         const T a = ((const T *)A.val)[j];
@@ -826,6 +830,8 @@ __global__ void __launch_bounds__(32) k_spill_numeric(CsrDev A, CsrDev B, PlanDe
     const int n = P.cnt->spill_count;
     for (int it = blockIdx.x; it < n; it += gridDim.x) {
         const int row = P.spill_rows[it];
+        if (row < P.r_lo || row >= P.r_hi)
+            continue;
         const int a0 = A.rpt[row], k = A.rpt[row + 1] - a0;
         const long long F = P.flop[row];
         const unsigned long long off = P.spill_off[it];

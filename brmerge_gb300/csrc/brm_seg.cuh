@@ -443,9 +443,10 @@ __global__ void __launch_bounds__(kPlanThreads) k_heavy_plan(CsrDev A, CsrDev B,
 template <int UNUSED = 0>
 __global__ void __launch_bounds__(256) k_split(CsrDev A, CsrDev B, PlanDev P)
 {
-    const int nsegs = P.cnt->n_seg;
+    const int i0 = P.seg_range ? P.seg_range[0] : 0;
+    const int nsegs = P.seg_range ? P.seg_range[1] : P.cnt->n_seg;
     const int *__restrict__ bcol = B.col;
-    for (int it = blockIdx.x; it < nsegs; it += gridDim.x) {
+    for (int it = i0 + blockIdx.x; it < nsegs; it += gridDim.x) {
         const int slot = P.seg_list[it];
         const int row = P.seg[slot].row;
         const int b = P.seg[slot].bidx;
@@ -523,13 +524,14 @@ __global__ void __launch_bounds__(kSegThreads) k_seg_numeric(CsrDev A, CsrDev B,
     int *wsi = (int *)(smem + L::o_ws);
     int *misc = (int *)(smem + L::o_misc);
     const int tid = threadIdx.x;
-    const int nsegs = P.cnt->n_seg;
+    const int i0 = P.seg_range ? P.seg_range[0] : 0;
+    const int nsegs = P.seg_range ? P.seg_range[1] : P.cnt->n_seg;
     const int *__restrict__ bcol = B.col;
     const T *__restrict__ bval = (const T *)B.val;
     const T *__restrict__ aval = (const T *)A.val;
     for (;;) {
         if (tid == 0)
-            misc[0] = atomicAdd(&P.cnt->work_seg, 1);
+            misc[0] = i0 + atomicAdd(&P.cnt->work_seg, 1);
         __syncthreads();
         const int item = misc[0];
         __syncthreads();
@@ -939,6 +941,56 @@ __global__ void __launch_bounds__(128) k_long_reduce(PlanDev P, int *ccol, T *cv
         }
         ccol[c.out] = c.col;
         cval[c.out] = sr.finish();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// 5. segments grouped by row parts: for a numeric phase run part by part
+//    (rows [pb[p], pb[p+1]) for p < nparts), the segment list is reordered so
+//    every part's segments are contiguous, and ranges[2p], ranges[2p+1] give
+//    the part's slice.  cnt (nparts ints) must be zero before the count pass.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int part_of_row(const int *pb, int nparts, int row)
+{
+    int p = 0;
+    while (p + 1 < nparts && row >= pb[p + 1])
+        p++;
+    return p;
+}
+
+template <int UNUSED = 0>
+__global__ void __launch_bounds__(256) k_seg_part_count(PlanDev P, const int *pb, int nparts,
+                                                        int *cnt)
+{
+    const int n = P.cnt->n_seg;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        atomicAdd(&cnt[part_of_row(pb, nparts, P.seg[P.seg_list[i]].row)], 1);
+}
+
+template <int UNUSED = 0>
+__global__ void __launch_bounds__(256) k_seg_part_scatter(PlanDev P, const int *pb, int nparts,
+                                                          const int *cnt, int *fill, int *out,
+                                                          int *ranges)
+{
+    __shared__ int base[kMaxParts + 1];
+    if (threadIdx.x == 0) {
+        int s = 0;
+        for (int p = 0; p < nparts; p++) {
+            base[p] = s;
+            s += cnt[p];
+        }
+        base[nparts] = s;
+    }
+    __syncthreads();
+    if (blockIdx.x == 0 && threadIdx.x < nparts) {
+        ranges[2 * threadIdx.x] = base[threadIdx.x];
+        ranges[2 * threadIdx.x + 1] = base[threadIdx.x + 1];
+    }
+    const int n = P.cnt->n_seg;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int slot = P.seg_list[i];
+        const int p = part_of_row(pb, nparts, P.seg[slot].row);
+        out[base[p] + atomicAdd(&fill[p], 1)] = slot;
     }
 }
 

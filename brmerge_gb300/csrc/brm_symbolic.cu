@@ -50,4 +50,13 @@ void launch_symbolic(const CsrDev &A, const CsrDev &B, const PlanDev &P, int num
     }
 }
 
+void launch_seg_partition(const PlanDev &P, const int *pb, int nparts, int *cnt, int *fill,
+                          int *out, int *ranges, int num_sms, cudaStream_t s)
+{
+    k_seg_part_count<0><<<num_sms * 4, 256, 0, s>>>(P, pb, nparts, cnt);
+    count_launch();
+    k_seg_part_scatter<0><<<num_sms * 4, 256, 0, s>>>(P, pb, nparts, cnt, fill, out, ranges);
+    count_launch();
+}
+
 }  // namespace brm
