@@ -214,6 +214,87 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+BATCH_PAIRS = 4096
+
+
+def make_batch(npairs: int, seed: int, dtype=np.float64):
+    """Uneven batch: C_i = A_i * B_i, n_i ~ U[256, 8192], rows lognormal(ln 6,
+    0.8) capped at 256, uniform random columns, values U[-1, 1]."""
+    import brmerge_gb300 as brm
+    rng = np.random.default_rng(seed)
+    ns = rng.integers(256, 8193, npairs)
+    pairs = []
+    for i, n in enumerate(ns):
+        A = brm.gen_lognormal(int(n), int(n), seed=seed * 100003 + 2 * i)
+        B = brm.gen_lognormal(int(n), int(n), seed=seed * 100003 + 2 * i + 1)
+        pairs.append((A.astype(dtype), B.astype(dtype)))
+    return pairs
+
+
+def upload_pairs(pairs, dev):
+    """All matrices in three device arrays; DeviceCSR views per matrix."""
+    import torch
+    import brmerge_gb300 as brm
+    mats = [m for ab in pairs for m in ab]
+    rpt = torch.from_numpy(np.concatenate([m.rpt for m in mats])).to(dev)
+    col = torch.from_numpy(np.concatenate([m.col for m in mats])).to(dev)
+    val = torch.from_numpy(np.concatenate([m.val for m in mats])).to(dev)
+    views, r, e = [], 0, 0
+    for m in mats:
+        views.append(brm.DeviceCSR(m.M, m.N, rpt[r:r + m.M + 1], col[e:e + m.nnz],
+                                   val[e:e + m.nnz]))
+        r += m.M + 1
+        e += m.nnz
+    return [(views[2 * i], views[2 * i + 1]) for i in range(len(pairs))], (rpt, col, val)
+
+
+def batched_section(ctx, dev, stream, steps: int):
+    """The uneven batch through brm_batch_precise (one pipeline for every
+    pair) against a loop of plain per-pair brm_precise_device calls."""
+    import torch
+    import brmerge_gb300 as brm
+    L = brm._native.lib()
+    pairs = make_batch(BATCH_PAIRS, seed=7)
+    products = sum(brm.compute_flop_host(A, B) for A, B in pairs)
+    dpairs, keep = upload_pairs(pairs, dev)
+    del pairs
+    out = ctx.batch_precise_raw(dpairs)  # warm-up (pools, workspaces)
+    nnz = int(out[1].numel())
+    del out
+    torch.cuda.synchronize(dev)
+    ts = []
+    l0 = L.brm_kernel_launches()
+    for _ in range(steps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        out = ctx.batch_precise_raw(dpairs)
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        ts.append(e0.elapsed_time(e1))
+        del out
+    launches = (L.brm_kernel_launches() - l0) / steps
+    # plain per-call loop over the same pairs (one pass, results released)
+    for a, b in dpairs[:16]:
+        ctx.precise_device(a, b)
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    for a, b in dpairs:
+        C = ctx.precise_device(a, b)
+        del C
+    torch.cuda.synchronize(dev)
+    plain_s = time.perf_counter() - t0
+    b_ms = statistics.mean(ts)
+    return {
+        "workload": f"{BATCH_PAIRS} pairs, n_i~U[256,8192], rows lognormal(ln6,0.8) cap 256, f64",
+        "pairs": BATCH_PAIRS, "products": int(products), "nnz_C": nnz,
+        "ms": round(b_ms, 3), "gflops": round(2 * products / (b_ms / 1e3) / 1e9, 3),
+        "plain_loop_ms": round(plain_s * 1e3, 2),
+        "plain_gflops": round(2 * products / plain_s / 1e9, 3),
+        "speedup_vs_plain": round(plain_s * 1e3 / b_ms, 2),
+        "launches_per_batch": launches, "steps": steps,
+    }
+
+
 def run_ours(args):
     import torch
     import brmerge_gb300 as brm
@@ -278,15 +359,23 @@ def run_ours(args):
     for _ in range(max(1, args.warmup)):
         brm.brmerge_precise(hA, hA)
     e2e_t = []
+    d2h = 0
     for _ in range(args.steps):
         t0 = time.perf_counter()
         Ch = brm.brmerge_precise(hA, hA)
         e2e_t.append(time.perf_counter() - t0)
+        d2h = csr_bytes(A.M, len(Ch.col), vb)
+        # the reference's driver releases C between calls, outside its timing
+        # (BRMerge-SpGEMM/src/brmerge_precise.cpp:73-79)
+        del Ch
     e2e_s = max_over_ranks(sum(e2e_t), ws)
     e2e_val = 2 * products * args.steps * ws / e2e_s / 1e9
     h2d = csr_bytes(A.M, A.nnz, vb)  # A and B are the same host arrays: copied once
-    d2h = csr_bytes(A.M, len(Ch.col), vb)
 
+    batched = None
+    if not args.no_batch:
+        del C
+        batched = batched_section(ctx, dev, stream, steps=max(1, min(args.steps, 3)))
     if rank != 0:
         return
     cpu = cpu_baseline(A, budget_s=args.cpu_budget) if not args.no_cpu else None
@@ -312,6 +401,8 @@ def run_ours(args):
     }
     if cpu is not None:
         line["cpu_baseline"] = cpu
+    if batched is not None:
+        line["batched"] = batched
     print(json.dumps(line), flush=True)
     if ws > 1:
         import torch.distributed as dist
@@ -327,6 +418,7 @@ def main():
     ap.add_argument("--workload", choices=["rmat", "er", "stencil"], default="rmat")
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-batch", action="store_true", help="skip the uneven-batch section")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -274,14 +274,13 @@ class Context:
         """brm_precise_device: one call, callee-allocated outputs (no copy)."""
         return self._device_call(False, A, B, timing)
 
-    def batch_precise(self, pairs) -> list:
-        """brm_batch_precise: C_i = A_i * B_i for a list of (A_i, B_i)
-        DeviceCSR pairs of one value type, in one pipeline.  Returns the C_i
-        as DeviceCSR views into the batch's concatenated arrays."""
+    def batch_precise_raw(self, pairs):
+        """brm_batch_precise on a list of (A_i, B_i) DeviceCSR pairs of one
+        value type.  Returns (crpt, ccol, cval, row_off, nnz_off): the
+        concatenated C_i as device tensors (crpt holds offsets into ccol/cval,
+        columns are each C_i's own) and the host offsets of every pair."""
         import torch
         n = len(pairs)
-        if n == 0:
-            return []
         dt = pairs[0][0].val.dtype
         if any(a.val.dtype != dt or b.val.dtype != dt for a, b in pairs):
             raise TypeError("all pairs of a batch must have the same value type")
@@ -300,6 +299,16 @@ class Context:
         noff = np.ctypeslib.as_array(out.nnz_off, shape=(n + 1,)).copy()
         out.crpt = out.ccol = out.cval = None  # owned by the tensors now
         self._L.brm_batch_free(self._h, C.byref(out))
+        return crpt, ccol, cval, roff, noff
+
+    def batch_precise(self, pairs) -> list:
+        """brm_batch_precise: C_i = A_i * B_i for a list of (A_i, B_i)
+        DeviceCSR pairs of one value type, in one pipeline.  Returns the C_i
+        as DeviceCSR views into the batch's concatenated arrays."""
+        import torch
+        if len(pairs) == 0:
+            return []
+        crpt, ccol, cval, roff, noff = self.batch_precise_raw(pairs)
         res = []
         for i, (a, b) in enumerate(pairs):
             r0, r1, n0, n1 = int(roff[i]), int(roff[i + 1]), int(noff[i]), int(noff[i + 1])
