@@ -40,7 +40,20 @@ class BatchC(C.Structure):
     """Mirror of brm_batch."""
     _fields_ = [("n", C.c_int), ("rows", C.c_longlong), ("nnz", C.c_longlong),
                 ("row_off", C.POINTER(C.c_longlong)), ("nnz_off", C.POINTER(C.c_longlong)),
-                ("crpt", C.c_void_p), ("ccol", C.c_void_p), ("cval", C.c_void_p)]
+                ("crpt", C.c_void_p), ("ccol", C.c_void_p), ("cval", C.c_void_p),
+                ("rpt_local", C.c_void_p)]
+
+
+class ServerConfigC(C.Structure):
+    """Mirror of brm_server_config."""
+    _fields_ = [("mem_cap_bytes", C.c_longlong), ("max_batch", C.c_int), ("workers", C.c_int)]
+
+
+class ServerResultC(C.Structure):
+    """Mirror of brm_server_result."""
+    _fields_ = [("status", C.c_int), ("M", C.c_int), ("N", C.c_int), ("nnz", C.c_int),
+                ("rpt", C.c_void_p), ("col", C.c_void_p), ("val", C.c_void_p),
+                ("queued_s", C.c_double), ("latency_s", C.c_double), ("batch_size", C.c_int)]
 
 
 class HostCsrC(C.Structure):
@@ -104,6 +117,12 @@ def lib() -> C.CDLL:
         _decl(L.brm_kernel_launches, C.c_longlong, [])
         _decl(L.brm_batch_precise, C.c_int, [vp, C.c_int, C.c_int, csrp, csrp, C.POINTER(BatchC)])
         _decl(L.brm_batch_free, C.c_int, [vp, C.POINTER(BatchC)])
+        _decl(L.brm_server_create, C.c_int, [C.POINTER(ServerConfigC), ctxp])
+        _decl(L.brm_server_submit, C.c_int, [vp, C.c_int, csrp, csrp, C.POINTER(C.c_longlong)])
+        _decl(L.brm_server_wait, C.c_int,
+              [vp, C.c_longlong, C.c_double, C.POINTER(ServerResultC)])
+        _decl(L.brm_server_release, C.c_int, [vp, C.c_longlong])
+        _decl(L.brm_server_destroy, C.c_int, [vp])
         _decl(L.brm_compute_flop, C.c_int, [vp, csrp, csrp, C.POINTER(C.c_longlong)])
         _decl(L.brm_upper_bound, C.c_int,
               [vp, C.c_int, csrp, csrp, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)])

@@ -31,6 +31,7 @@ CUDA_SOURCES = [
     "brm_noalloc.cu",
     "brm_hostpool.cu",
     "brm_batch.cu",
+    "brm_server.cu",
 ]
 HOST_SOURCES = ["host/gen.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

@@ -114,6 +114,22 @@ __global__ void __launch_bounds__(256) k_batch_unshift(const BatchPair *pairs, i
         nnz_first[i] = crpt[i < n ? pairs[i].row_a : rows];
 }
 
+// Each pair's own row pointers (starting at 0), pair i at out[row_off[i] +
+// i .. row_off[i+1] + i].
+__global__ void __launch_bounds__(256) k_batch_local_rpt(int n, const long long *row_off,
+                                                         long long rows, const int *crpt,
+                                                         const long long *first, int *out)
+{
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    for (long long r = t; r < rows; r += stride) {
+        const int i = pair_of(row_off, n, r);
+        out[r + i] = (int)(crpt[r] - first[i]);
+    }
+    for (long long i = t; i < n; i += stride)
+        out[row_off[i + 1] + i] = (int)(first[i + 1] - first[i]);
+}
+
 }  // namespace brm
 
 namespace {
@@ -277,14 +293,19 @@ int brm_batch_precise(brm_context ctx, brm_dtype dtype, int n, const brm_csr *A,
         cleanup();
         return st;
     }
-    {
+    int *lrpt = nullptr;
+    e = cudaMallocAsync((void **)&lrpt, sizeof(int) * (size_t)(ra + n), s);
+    if (e == cudaSuccess) {
         const int g = std::max(sms, 1) * 16;
         brm::k_batch_unshift<<<g, 256, 0, s>>>(dp, n, doff, (int)ra, crpt, ccol, dfirst);
+        brm::count_launch();
+        brm::k_batch_local_rpt<<<g, 256, 0, s>>>(n, doff, ra, crpt, dfirst, lrpt);
         brm::count_launch();
     }
     long long *hf = (long long *)std::malloc(sizeof(long long) * (size_t)(n + 1));
     long long *hr = (long long *)std::malloc(sizeof(long long) * (size_t)(n + 1));
-    e = cudaGetLastError();
+    if (e == cudaSuccess)
+        e = cudaGetLastError();
     if (hf && hr && e == cudaSuccess)
         e = cudaMemcpyAsync(hf, dfirst, sizeof(long long) * (size_t)(n + 1), cudaMemcpyDeviceToHost,
                             s);
@@ -298,6 +319,7 @@ int brm_batch_precise(brm_context ctx, brm_dtype dtype, int n, const brm_csr *A,
         brm_device_free(ctx, crpt);
         brm_device_free(ctx, ccol);
         brm_device_free(ctx, cval);
+        brm_device_free(ctx, lrpt);
         return (!hf || !hr) ? BRM_ERR_ALLOC : BRM_ERR_CUDA;
     }
     std::memcpy(hr, off.data(), sizeof(long long) * (size_t)(n + 1));
@@ -307,6 +329,7 @@ int brm_batch_precise(brm_context ctx, brm_dtype dtype, int n, const brm_csr *A,
     out->crpt = crpt;
     out->ccol = ccol;
     out->cval = cval;
+    out->rpt_local = lrpt;
     return BRM_SUCCESS;
 }
 
@@ -321,6 +344,8 @@ int brm_batch_free(brm_context ctx, brm_batch *b)
         st = brm_device_free(ctx, b->ccol);
     if (b->cval && st == BRM_SUCCESS)
         st = brm_device_free(ctx, b->cval);
+    if (b->rpt_local && st == BRM_SUCCESS)
+        st = brm_device_free(ctx, b->rpt_local);
     std::free(b->row_off);
     std::free(b->nnz_off);
     std::memset(b, 0, sizeof(*b));

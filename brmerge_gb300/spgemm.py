@@ -276,9 +276,10 @@ class Context:
 
     def batch_precise_raw(self, pairs):
         """brm_batch_precise on a list of (A_i, B_i) DeviceCSR pairs of one
-        value type.  Returns (crpt, ccol, cval, row_off, nnz_off): the
-        concatenated C_i as device tensors (crpt holds offsets into ccol/cval,
-        columns are each C_i's own) and the host offsets of every pair."""
+        value type.  Returns (crpt, ccol, cval, row_off, nnz_off, rpt_local):
+        the concatenated C_i as device tensors (crpt holds offsets into
+        ccol/cval, columns are each C_i's own), the host offsets of every pair,
+        and every pair's own row pointers (pair i at row_off[i] + i)."""
         import torch
         n = len(pairs)
         dt = pairs[0][0].val.dtype
@@ -295,11 +296,12 @@ class Context:
         crpt = _device_tensor(self._L, out.crpt, out.rows + 1, "<i4", dev)
         ccol = _device_tensor(self._L, out.ccol, out.nnz, "<i4", dev)
         cval = _device_tensor(self._L, out.cval, out.nnz, vt, dev)
+        lrpt = _device_tensor(self._L, out.rpt_local, out.rows + n, "<i4", dev)
         roff = np.ctypeslib.as_array(out.row_off, shape=(n + 1,)).copy()
         noff = np.ctypeslib.as_array(out.nnz_off, shape=(n + 1,)).copy()
-        out.crpt = out.ccol = out.cval = None  # owned by the tensors now
+        out.crpt = out.ccol = out.cval = out.rpt_local = None  # owned by the tensors now
         self._L.brm_batch_free(self._h, C.byref(out))
-        return crpt, ccol, cval, roff, noff
+        return crpt, ccol, cval, roff, noff, lrpt
 
     def batch_precise(self, pairs) -> list:
         """brm_batch_precise: C_i = A_i * B_i for a list of (A_i, B_i)
@@ -308,12 +310,11 @@ class Context:
         import torch
         if len(pairs) == 0:
             return []
-        crpt, ccol, cval, roff, noff = self.batch_precise_raw(pairs)
+        _, ccol, cval, roff, noff, lrpt = self.batch_precise_raw(pairs)
         res = []
         for i, (a, b) in enumerate(pairs):
             r0, r1, n0, n1 = int(roff[i]), int(roff[i + 1]), int(noff[i]), int(noff[i + 1])
-            rpt = (crpt[r0:r1 + 1] - n0).to(torch.int32)
-            res.append(DeviceCSR(a.M, b.N, rpt, ccol[n0:n1], cval[n0:n1]))
+            res.append(DeviceCSR(a.M, b.N, lrpt[r0 + i:r1 + i + 1], ccol[n0:n1], cval[n0:n1]))
         return res
 
     def upper(self, A: DeviceCSR, B: DeviceCSR, timing=None) -> DeviceCSR:
@@ -351,6 +352,85 @@ class _RawDevice:
     def __init__(self, ptr: int, n: int, typestr: str):
         self.__cuda_array_interface__ = {
             "shape": (n,), "typestr": typestr, "data": (ptr, False), "version": 2, "strides": None}
+
+
+class _Ticket:
+    """A finished server request; released when its last view is collected."""
+
+    def __init__(self, server, ticket: int):
+        self._srv, self.ticket = server, ticket
+
+    def __del__(self):
+        self._srv._release(self.ticket)
+
+
+class _ServerBlock(_RawDevice):
+    def __init__(self, owner: _Ticket, ptr: int, n: int, typestr: str):
+        super().__init__(ptr, n, typestr)
+        self._owner = owner
+
+
+class Server:
+    """brm_server: C = A * B requests from any thread, batched by worker
+    threads under a memory cap (one block-diagonal pipeline per batch)."""
+
+    def __init__(self, mem_cap_bytes: int = 0, max_batch: int = 0, workers: int = 0):
+        self._L = _native.lib()
+        self._h = C.c_void_p()
+        cfg = _native.ServerConfigC(mem_cap_bytes, max_batch, workers)
+        _native.check(self._L.brm_server_create(C.byref(cfg), C.byref(self._h)),
+                      "brm_server_create")
+        self._inputs = {}  # ticket -> (A, B): kept alive until the result is waited for
+
+    def submit(self, A: "DeviceCSR", B: "DeviceCSR") -> int:
+        import torch
+        code = _dtype_code(np.float64 if A.val.dtype == torch.float64 else np.float32)
+        t = C.c_longlong(0)
+        a, b = A.c(), B.c()
+        _native.check(self._L.brm_server_submit(self._h, code, C.byref(a), C.byref(b),
+                                                C.byref(t)), "brm_server_submit")
+        self._inputs[t.value] = (A, B)
+        return t.value
+
+    def wait(self, ticket: int, timeout: float = -1.0):
+        """Returns (C as DeviceCSR views, stats); the views keep the result
+        alive, and it is released when the last of them is collected."""
+        import torch
+        r = _native.ServerResultC()
+        st = self._L.brm_server_wait(self._h, ticket, timeout, C.byref(r))
+        if st == 8:  # BRM_ERR_TIMEOUT
+            raise TimeoutError(f"request {ticket} not done after {timeout} s")
+        A, B = self._inputs.pop(ticket)
+        owner = _Ticket(self, ticket)
+        _native.check(st, "brm_server_wait")
+        dev = A.rpt.device
+        vt = "<f8" if A.val.dtype == torch.float64 else "<f4"
+
+        def view(ptr, n, ts, dt):
+            if n == 0 or not ptr:
+                return torch.empty(n, dtype=dt, device=dev)
+            return torch.as_tensor(_ServerBlock(owner, ptr, n, ts), device=dev)
+
+        rpt = view(r.rpt, r.M + 1, "<i4", torch.int32)
+        col = view(r.col, r.nnz, "<i4", torch.int32)
+        val = view(r.val, r.nnz, vt, A.val.dtype)
+        stats = {"queued_s": r.queued_s, "latency_s": r.latency_s, "batch_size": r.batch_size}
+        return DeviceCSR(r.M, r.N, rpt, col, val), stats
+
+    def _release(self, ticket: int):
+        if self._h:
+            self._L.brm_server_release(self._h, ticket)
+
+    def close(self):
+        if self._h:
+            self._L.brm_server_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class _DeviceBlock(_RawDevice):

@@ -188,6 +188,8 @@ typedef struct brm_batch {
     int *crpt;            /* device, rows + 1 */
     int *ccol;            /* device, nnz */
     void *cval;           /* device, nnz (dtype) */
+    int *rpt_local;       /* device, rows + n: C_i's own row pointers (from 0)
+                             at rpt_local[row_off[i] + i ..  row_off[i+1] + i] */
 } brm_batch;
 
 /* C_i = A_i * B_i (BRMerge-Precise) for n independent pairs of device CSR
@@ -200,6 +202,50 @@ typedef struct brm_batch {
 int brm_batch_precise(brm_context ctx, brm_dtype dtype, int n, const brm_csr *A, const brm_csr *B,
                       brm_batch *out);
 int brm_batch_free(brm_context ctx, brm_batch *batch);
+
+/* ---- serving: a request loop over batches ---------------------------------- */
+
+/* A server takes C = A * B requests (Precise, device CSR) from any thread.
+ * Worker threads, each with its own context and stream, take whatever is
+ * queued (one value type per batch, arrival order), admit requests while the
+ * summed upper-bound bytes (brm_upper_bound plus the operands' copies) of
+ * everything admitted and not yet released stay under mem_cap_bytes, and run
+ * them as one brm_batch_precise.  Requests that arrive while batches run wait
+ * for the next free worker; the batches of different workers overlap on the
+ * device.  Every result is bit-identical to brm_precise_device on its pair.
+ * No counterpart in the reference (one library call per product). */
+typedef struct brm_server_s *brm_server;
+
+typedef struct brm_server_config {
+    long long mem_cap_bytes; /* <= 0: 60 GiB */
+    int max_batch;           /* requests per batch, <= 0: 4096 */
+    int workers;             /* concurrent batches, <= 0: 2 (at most 16) */
+} brm_server_config;
+
+typedef struct brm_server_result {
+    int status;              /* brm_status of the request */
+    int M, N, nnz;
+    const int *rpt;          /* device, M + 1 row pointers starting at 0 */
+    const int *col;          /* device, nnz */
+    const void *val;         /* device, nnz (the request's dtype) */
+    double queued_s;         /* submit -> start of its batch */
+    double latency_s;        /* submit -> result ready */
+    int batch_size;          /* requests in the batch that computed it */
+} brm_server_result;
+
+/* On the current device; cfg may be NULL. */
+int brm_server_create(const brm_server_config *cfg, brm_server *srv);
+/* A and B must stay valid until the request is done.  Rejects a request
+ * whose bound alone exceeds the cap with BRM_ERR_CAPACITY. */
+int brm_server_submit(brm_server srv, brm_dtype dtype, const brm_csr *A, const brm_csr *B,
+                      long long *ticket);
+/* Waits up to timeout_s (< 0: forever; BRM_ERR_TIMEOUT when not done) and
+ * fills *res; the arrays stay valid until brm_server_release(ticket). */
+int brm_server_wait(brm_server srv, long long ticket, double timeout_s, brm_server_result *res);
+int brm_server_release(brm_server srv, long long ticket);
+/* Finishes the queued requests, then frees everything (unreleased results
+ * included). */
+int brm_server_destroy(brm_server srv);
 
 /* ---- helpers ---------------------------------------------------------------- */
 
