@@ -295,6 +295,109 @@ def batched_section(ctx, dev, stream, steps: int):
     }
 
 
+def served_section(dev, rate: float, nreq: int, seed: int = 11):
+    """Poisson request stream into brm_server (continuous batching under a
+    60 GiB cap): 70% uneven-batch sizes, 25% R-MAT n=2^16 degree 8, 5% R-MAT
+    n=2^20 degree 16; float64 and float32 mixed.  Latency = submit -> result
+    ready; the isolated latency of each class is one call on an idle GPU."""
+    import queue as q
+    import torch
+    import brmerge_gb300 as brm
+    rng = np.random.default_rng(seed)
+    up = lambda X: brm.DeviceCSR.from_host(X, dev)
+    small = [(up(A), up(B)) for A, B in make_batch(64, seed=seed)]
+    small32 = [(up(A.astype(np.float32)), up(B.astype(np.float32)))
+               for A, B in make_batch(16, seed=seed + 1)]
+    r16h = [brm.gen_rmat(16, 8 << 16, seed=seed + 10 + i) for i in range(4)]
+    r16 = [(up(A), up(A)) for A in r16h]
+    r16_32 = [(up(A.astype(np.float32)),) * 2 for A in r16h[:2]]
+    big = brm.gen_rmat(20, 16 << 20, seed=seed + 20)
+    r20 = [(up(big), up(big))]
+    r20_32 = [(up(big.astype(np.float32)),) * 2]
+    del big
+    classes = {"batch_size": (small, small32), "rmat16": (r16, r16_32), "rmat20": (r20, r20_32)}
+    prob = [("batch_size", 0.70), ("rmat16", 0.25), ("rmat20", 0.05)]
+    flops = {}
+    ctx = brm.Context()
+    iso = {}
+    for name, (p64, _) in classes.items():
+        a, b = p64[0]
+        flops[name] = 2 * ctx.compute_flop(a, b)
+        _, bound = ctx.upper_bound(a, b)
+        if bound > (60 << 30):
+            iso[name] = f"rejected: upper bound {bound / 2**30:.0f} GiB > 60 GiB cap"
+            continue
+        ts = []
+        for _ in range(3):
+            torch.cuda.synchronize(dev)
+            t0 = time.perf_counter()
+            try:
+                C = ctx.precise_device(a, b)
+                torch.cuda.synchronize(dev)
+                ts.append(time.perf_counter() - t0)
+                del C
+            except brm.BrmError as e:  # nnz(C) beyond int32 CSR
+                iso[name] = f"rejected: {e}"
+                break
+        if name not in iso:
+            iso[name] = round(statistics.median(ts) * 1e3, 3)
+    ctx.close()
+    # the stream
+    names = [p[0] for p in prob]
+    kinds = rng.choice(len(names), size=nreq, p=[p[1] for p in prob])
+    f32 = rng.random(nreq) < 0.5
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, nreq))
+    srv = brm.Server(mem_cap_bytes=60 << 30, workers=2)
+    tickets = q.Queue()
+    rejected = {n: 0 for n in names}
+    t_start = time.perf_counter()
+
+    def submitter():
+        for i in range(nreq):
+            now = time.perf_counter() - t_start
+            if arrivals[i] > now:
+                time.sleep(arrivals[i] - now)
+            name = names[kinds[i]]
+            pool = classes[name][1 if f32[i] else 0]
+            a, b = pool[int(rng.integers(len(pool)))]
+            try:
+                tickets.put((i, name, srv.submit(a, b)))
+            except brm.BrmError:
+                rejected[name] += 1
+        tickets.put(None)
+
+    lat = {n: [] for n in names}
+    batch_sizes = []
+    done_flop = 0
+    th = threading.Thread(target=submitter)
+    th.start()
+    while True:
+        item = tickets.get()
+        if item is None:
+            break
+        i, name, t = item
+        C, st = srv.wait(t, timeout=600.0)
+        lat[name].append(st["latency_s"] * 1e3)
+        batch_sizes.append(st["batch_size"])
+        done_flop += flops[name]
+        del C
+    th.join()
+    wall = time.perf_counter() - t_start
+    srv.close()
+    allv = [x for v in lat.values() for x in v]
+    pct = lambda v, p: round(float(np.percentile(v, p)), 3) if v else None
+    per_class = {n: {"n": len(v), "p50_ms": pct(v, 50), "p99_ms": pct(v, 99),
+                     "isolated_ms": iso[n], "rejected": rejected[n]} for n, v in lat.items()}
+    return {
+        "offered_rate_per_s": rate, "requests": nreq, "completed": len(allv),
+        "wall_s": round(wall, 3), "throughput_req_per_s": round(len(allv) / wall, 1),
+        "gflops": round(done_flop / wall / 1e9, 3),
+        "p50_ms": pct(allv, 50), "p99_ms": pct(allv, 99),
+        "mean_batch": round(float(np.mean(batch_sizes)), 2) if batch_sizes else None,
+        "classes": per_class, "mem_cap_gib": 60, "workers": 2,
+    }
+
+
 def run_ours(args):
     import torch
     import brmerge_gb300 as brm
@@ -372,10 +475,11 @@ def run_ours(args):
     e2e_val = 2 * products * args.steps * ws / e2e_s / 1e9
     h2d = csr_bytes(A.M, A.nnz, vb)  # A and B are the same host arrays: copied once
 
-    batched = None
+    batched = served = None
     if not args.no_batch:
         del C
         batched = batched_section(ctx, dev, stream, steps=max(1, min(args.steps, 3)))
+        served = [served_section(dev, rate, args.serve_requests) for rate in (2000.0, 500.0)]
     if rank != 0:
         return
     cpu = cpu_baseline(A, budget_s=args.cpu_budget) if not args.no_cpu else None
@@ -403,6 +507,8 @@ def run_ours(args):
         line["cpu_baseline"] = cpu
     if batched is not None:
         line["batched"] = batched
+    if served is not None:
+        line["served"] = served
     print(json.dumps(line), flush=True)
     if ws > 1:
         import torch.distributed as dist
@@ -418,7 +524,9 @@ def main():
     ap.add_argument("--workload", choices=["rmat", "er", "stencil"], default="rmat")
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--no-batch", action="store_true", help="skip the uneven-batch section")
+    ap.add_argument("--no-batch", action="store_true",
+                    help="skip the uneven-batch and served-stream sections")
+    ap.add_argument("--serve-requests", type=int, default=600)
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -7,14 +7,15 @@
 // leaf index of a product, and therefore the order of its additions, does
 // not depend on the cut.  Three steps:
 //
-//   1. planning (symbolic phase, one CTA per heavy row): a bitmap of the
-//      row's columns and a product count per 32-column word over chunks of
-//      kPlanBits columns give the row's exact nnz and the cut points: a cut
-//      before word w when the running product count crosses a multiple of
-//      kSegCut and around words holding more than kSegCut products (inside
-//      such a word the cuts are per column); a segment then holds <= kSegCap
-//      products.  Its output offset within the row (distinct columns before
-//      c_lo) comes from the same bitmap.
+//   1. planning (symbolic phase, one CTA per heavy row, longest rows first):
+//      a bitmap of the row's columns and a product count per 128-column group
+//      over chunks of kPlanBits columns give the row's exact nnz and the cut
+//      points: a cut before group g when the running product count crosses a
+//      multiple of kSegCut and around groups holding more than kSegCut
+//      products (inside such a group the cuts are per column, from 16-bit
+//      per-column counts); a segment then holds <= kSegCap products.  Its
+//      output offset within the row (distinct columns before c_lo) comes
+//      from the same bitmap.
 //   2. split table (numeric phase): for every segment boundary and every list
 //      of the row, the first list position at or after the boundary column
 //      (one block per boundary, one binary search per list).
@@ -22,9 +23,14 @@
 //      segment's products in list-major order; the rank u of every product's
 //      column among the segment's distinct columns comes from a two-level
 //      bitmap (a summary bit per nonempty 32-column word, then the compressed
-//      words); a stable radix sort on u puts each column's contributions in
-//      leaf order; one thread per output column evaluates the merge tree with
-//      ShiftReduce and stores column u at position u (coalesced).
+//      words); a counting sort on u groups each column's contributions; one
+//      thread per output column puts up to eight of them in leaf order in
+//      registers and evaluates the merge tree (closed forms for three and
+//      four, a register ShiftReduce up to eight); longer columns are ranked
+//      by leaf by a warp and handed to the column reducer (step 4).  Column u
+//      is stored at position u of the row's segment (coalesced).
+//   4. column reducer: one thread per long column, ShiftReduce with the
+//      stack in registers over the leaf-ordered products.
 #pragma once
 
 #include <climits>
@@ -43,7 +49,7 @@ constexpr int kPlanGroupLog2 = 7;
 constexpr int kPlanGroupBits = 1 << kPlanGroupLog2;      // 128 columns
 constexpr int kPlanGroupWords = kPlanGroupBits / 32;     // 4 bitmap words
 constexpr int kPlanGroups = kPlanBits / kPlanGroupBits;  // 2048 per chunk
-constexpr int kDenseGroups = 32;
+constexpr int kDenseGroups = 128;  // 16-bit column counts: a count is at most k <= 65535
 
 struct PlanLayout {
     static constexpr size_t o_bm = 0;
@@ -51,7 +57,7 @@ struct PlanLayout {
     static constexpr size_t o_gpop = o_hist + kPlanGroups * 4;
     static constexpr size_t o_dix = o_gpop + kPlanGroups * 2;
     static constexpr size_t o_ccnt = o_dix + kPlanGroups * 2;
-    static constexpr size_t o_lst = o_ccnt + kDenseGroups * kPlanGroupBits * 4;
+    static constexpr size_t o_lst = o_ccnt + kDenseGroups * kPlanGroupBits * 2;
     static constexpr size_t o_loffs = o_lst + (kPlanThreads + 1) * 4;
     static constexpr size_t o_ws = o_loffs + (kPlanThreads + 1) * 4 + 8;
     static constexpr size_t o_misc = o_ws + (kPlanThreads / 32 + 1) * 8;
@@ -136,7 +142,8 @@ __device__ __forceinline__ void plan_products(const PlanDev &P, const int *__res
 // of kSegCut, so a segment holds less than 2 * kSegCut = kSegCap products.
 template <typename Fn>
 __device__ __forceinline__ void plan_group_starts(int g, unsigned h, unsigned ph,
-                                                  unsigned long long run, const unsigned *ccnt,
+                                                  unsigned long long run,
+                                                  const unsigned short *ccnt,
                                                   Fn f)
 {
     const unsigned pe = (unsigned)(run >> 32);
@@ -175,7 +182,9 @@ __global__ void __launch_bounds__(kPlanThreads) k_heavy_plan(CsrDev A, CsrDev B,
     unsigned *hist = (unsigned *)(smem + PlanLayout::o_hist);
     unsigned short *gpop = (unsigned short *)(smem + PlanLayout::o_gpop);
     unsigned short *dix = (unsigned short *)(smem + PlanLayout::o_dix);
-    unsigned *ccnt = (unsigned *)(smem + PlanLayout::o_ccnt);
+    // per-column product counts of dense groups, two 16-bit counters a word
+    unsigned *ccnt2 = (unsigned *)(smem + PlanLayout::o_ccnt);
+    const unsigned short *ccnt = (const unsigned short *)(smem + PlanLayout::o_ccnt);
     int *lst = (int *)(smem + PlanLayout::o_lst);
     int *loffs = (int *)(smem + PlanLayout::o_loffs);
     long long *ws = (long long *)(smem + PlanLayout::o_ws);
@@ -298,8 +307,8 @@ __global__ void __launch_bounds__(kPlanThreads) k_heavy_plan(CsrDev A, CsrDev B,
                 for (int g = g0; g < g1; g++)
                     if (hist[g] > (unsigned)kSegCut)
                         dix[g] = (unsigned short)dx++;
-                for (int i = tid; i < nd * kPlanGroupBits; i += NT)
-                    ccnt[i] = 0;
+                for (int i = tid; i < nd * kPlanGroupBits / 2; i += NT)
+                    ccnt2[i] = 0;
                 __syncthreads();
                 // only the columns from the first to the last dense group
                 const int dlo_c = lo + kPlanGroupBits * misc[4];
@@ -308,13 +317,15 @@ __global__ void __launch_bounds__(kPlanThreads) k_heavy_plan(CsrDev A, CsrDev B,
                 plan_products<NT>(P, bcol, a0, k, true, dlo_c, dhi_c, lo, lst, loffs, ws, [&](int rc) {
                     if ((unsigned)rc < (unsigned)span) {
                         const int g = rc >> kPlanGroupLog2;
-                        if (hist[g] > (unsigned)kSegCut)
-                            atomicAdd(&ccnt[dix[g] * kPlanGroupBits + (rc & (kPlanGroupBits - 1))], 1u);
+                        if (hist[g] > (unsigned)kSegCut) {
+                            const int slot = dix[g] * kPlanGroupBits + (rc & (kPlanGroupBits - 1));
+                            atomicAdd(&ccnt2[slot >> 1], 1u << (16 * (slot & 1)));
+                        }
                     }
                 });
                 bool big = false;
                 for (int i = tid; i < nd * kPlanGroupBits; i += NT)
-                    big |= ccnt[i] > (unsigned)kSegCap;
+                    big |= ccnt[i] > kSegCap;
                 fail = __syncthreads_or(big) != 0;
             }
             long long tot;
