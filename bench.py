@@ -64,6 +64,17 @@ def make_workload(name: str):
     return A, desc
 
 
+def measured_traffic():
+    """DRAM bytes of one Precise call on the R-MAT workload, from the committed
+    ncu launch-list summary (a capture of this bench's own command)."""
+    p = ROOT / "profiles" / "rmat18_precise_launches.md"
+    if p.exists():
+        for line in p.read_text().splitlines():
+            if line.startswith("traffic_bytes_per_step:"):
+                return int(line.split(":")[1])
+    return None
+
+
 def peaks():
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
@@ -479,7 +490,7 @@ def run_ours(args):
     if not args.no_batch:
         del C
         batched = batched_section(ctx, dev, stream, steps=max(1, min(args.steps, 3)))
-        served = [served_section(dev, rate, args.serve_requests) for rate in (2000.0, 500.0)]
+        served = [served_section(dev, rate, args.serve_requests) for rate in (2000.0, 400.0, 150.0)]
     if rank != 0:
         return
     cpu = cpu_baseline(A, budget_s=args.cpu_budget) if not args.no_cpu else None
@@ -495,7 +506,10 @@ def run_ours(args):
                        parallelism="replicas" if ws > 1 else "single_gpu",
                        symbolic_ms=round(sym_ms, 4), numeric_ms=round(num_ms, 4)),
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak,
-                     "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": None,
+                     "unit": "GB/s", "frac": round(achieved / peak, 4),
+                     "traffic": measured_traffic() if args.workload == "rmat" else None,
+                     "traffic_source": "profiles/rmat18_precise_launches.md (ncu DRAM bytes "
+                                       "of every kernel of one call)",
                      "kernel": "whole Precise call (all kernels of a step)",
                      "peak_kind": peak_kind, "algorithmic_bytes": int(alg_bytes)},
         "e2e": {"value": round(e2e_val, 3), "unit": "GFLOP/s", "h2d_bytes_per_step": int(h2d),

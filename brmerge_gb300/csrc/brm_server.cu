@@ -29,6 +29,8 @@
 
 namespace {
 
+constexpr long long kSizeRatio = 16;  // largest bound ratio within one batch
+
 double now_s()
 {
     using namespace std::chrono;
@@ -103,11 +105,16 @@ void brm_server_s::work(int w)
                     // first fit in arrival order: the head's value type, while
                     // the admitted bytes stay under the cap (the head is always
                     // admitted when nothing else is in flight)
+                    // requests whose bounds differ from the head's by more
+                    // than kSizeRatio wait for a batch of their own size, so a
+                    // small request does not wait for a large one's batch
                     const brm_dtype dt = queue.front()->dtype;
+                    const long long hb = std::max(queue.front()->bound, 1LL);
                     for (auto it = queue.begin();
                          it != queue.end() && (int)batch.size() < max_batch;) {
                         Request *r = *it;
-                        if (r->dtype != dt) {
+                        const long long rb = std::max(r->bound, 1LL);
+                        if (r->dtype != dt || rb > hb * kSizeRatio || rb * kSizeRatio < hb) {
                             ++it;
                             continue;
                         }

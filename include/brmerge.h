@@ -207,7 +207,9 @@ int brm_batch_free(brm_context ctx, brm_batch *batch);
 
 /* A server takes C = A * B requests (Precise, device CSR) from any thread.
  * Worker threads, each with its own context and stream, take whatever is
- * queued (one value type per batch, arrival order), admit requests while the
+ * queued (one value type per batch, arrival order, bounds within 16x of the
+ * oldest queued request's, so small requests do not wait behind large
+ * ones), admit requests while the
  * summed upper-bound bytes (brm_upper_bound plus the operands' copies) of
  * everything admitted and not yet released stay under mem_cap_bytes, and run
  * them as one brm_batch_precise.  Requests that arrive while batches run wait
