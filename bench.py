@@ -273,17 +273,26 @@ def batched_section(ctx, dev, stream, steps: int):
     nnz = int(out[1].numel())
     del out
     torch.cuda.synchronize(dev)
-    ts = []
-    l0 = L.brm_kernel_launches()
-    for _ in range(steps):
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        out = ctx.batch_precise_raw(dpairs)
-        e1.record(stream)
-        torch.cuda.synchronize(dev)
-        ts.append(e0.elapsed_time(e1))
-        del out
-    launches = (L.brm_kernel_launches() - l0) / steps
+
+    def timed():
+        ts = []
+        l0 = L.brm_kernel_launches()
+        for _ in range(steps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            out = ctx.batch_precise_raw(dpairs)
+            e1.record(stream)
+            torch.cuda.synchronize(dev)
+            ts.append(e0.elapsed_time(e1))
+            del out
+        return statistics.mean(ts), (L.brm_kernel_launches() - l0) / steps
+
+    default_ms, _ = timed()
+    t0 = time.perf_counter()
+    tuning = ctx.autotune(dpairs)  # bin thresholds chosen on this batch
+    tune_s = time.perf_counter() - t0
+    b_ms, launches = timed()
+    ctx.set_tuning()  # the plain loop below runs with the defaults
     # plain per-call loop over the same pairs (one pass, results released)
     for a, b in dpairs[:16]:
         ctx.precise_device(a, b)
@@ -294,8 +303,9 @@ def batched_section(ctx, dev, stream, steps: int):
         del C
     torch.cuda.synchronize(dev)
     plain_s = time.perf_counter() - t0
-    b_ms = statistics.mean(ts)
     return {
+        "tuning": tuning, "default_tuning_ms": round(default_ms, 3),
+        "autotune_s": round(tune_s, 2),
         "workload": f"{BATCH_PAIRS} pairs, n_i~U[256,8192], rows lognormal(ln6,0.8) cap 256, f64",
         "pairs": BATCH_PAIRS, "products": int(products), "nnz_C": nnz,
         "ms": round(b_ms, 3), "gflops": round(2 * products / (b_ms / 1e3) / 1e9, 3),

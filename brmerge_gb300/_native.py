@@ -36,6 +36,11 @@ class CsrC(C.Structure):
                 ("rpt", C.c_void_p), ("col", C.c_void_p), ("val", C.c_void_p)]
 
 
+class TuningC(C.Structure):
+    """Mirror of brm_tuning."""
+    _fields_ = [("seg_cut", C.c_int), ("mid_flop", C.c_int)]
+
+
 class BatchC(C.Structure):
     """Mirror of brm_batch."""
     _fields_ = [("n", C.c_int), ("rows", C.c_longlong), ("nnz", C.c_longlong),
@@ -115,6 +120,9 @@ def lib() -> C.CDLL:
         _decl(L.brm_free, None, [vp])
         _decl(L.brm_host_cache_release, None, [])
         _decl(L.brm_kernel_launches, C.c_longlong, [])
+        _decl(L.brm_set_tuning, C.c_int, [vp, C.POINTER(TuningC)])
+        _decl(L.brm_get_tuning, C.c_int, [vp, C.POINTER(TuningC)])
+        _decl(L.brm_autotune, C.c_int, [vp, C.c_int, C.c_int, csrp, csrp, C.POINTER(TuningC)])
         _decl(L.brm_batch_precise, C.c_int, [vp, C.c_int, C.c_int, csrp, csrp, C.POINTER(BatchC)])
         _decl(L.brm_batch_free, C.c_int, [vp, C.POINTER(BatchC)])
         _decl(L.brm_server_create, C.c_int, [C.POINTER(ServerConfigC), ctxp])

@@ -83,7 +83,7 @@ __global__ void __launch_bounds__(kAnaThreads) k_analyze(CsrDev A, CsrDev B, Pla
             bin = kBinCopy;
         else if (f <= kWarpMaxFlop)
             bin = kBinWarp;
-        else if (f <= kMidFlop && 2 * nl <= kMidFlop && a1 - a0 <= kMidMaxK)
+        else if (f <= P.mid_limit && 2 * nl <= P.mid_limit && a1 - a0 <= kMidMaxK)
             bin = kBinBatch;
         else if (a1 - a0 <= kSegMaxK)
             bin = kBinHeavy;  // segmented (brm_seg.cuh)
@@ -113,7 +113,7 @@ __global__ void __launch_bounds__(kAnaThreads) k_analyze(CsrDev A, CsrDev B, Pla
                 atomicOr(&P.cnt->err, kErrOverflow);
             P.flop[row] = (int)f;
             if (bin == kBinHeavy)
-                P.seg_base[row] = atomicAdd(&P.cnt->seg_cap, seg_bound(f, B.N));
+                P.seg_base[row] = atomicAdd(&P.cnt->seg_cap, seg_bound(f, B.N, P.seg_cut));
             P.mid_flop[row] = bin == kBinBatch ? max((int)f, 2 * nl) : 0;  // batch weight
             P.spill[row] = 0;
             if (bin == kBinEmpty)

@@ -32,6 +32,9 @@ struct DevBuf {
 
 constexpr int kNumEvents = 12;
 constexpr long long kLongElems = 16ll << 20;  // products in the long-column scratch
+// candidates of brm_autotune (heavy-row cut target x mid-row weight limit)
+constexpr int kTuneSegCut[] = {1536, 1024, 768, 512};
+constexpr int kTuneMidFlop[] = {2048, 1024, 512};
 
 }  // namespace
 
@@ -721,6 +724,8 @@ int brm_create(brm_context *out)
     if (!ctx)
         return BRM_ERR_ALLOC;
     ctx->device = dev;
+    ctx->plan.seg_cut = brm::kSegCut;
+    ctx->plan.mid_limit = brm::kMidFlop;
     cudaError_t e = cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, dev);
     if (e == cudaSuccess)
         e = cudaMallocHost(&ctx->h_cnt, sizeof(brm::Counters));
@@ -814,6 +819,89 @@ int brm_set_validate(brm_context ctx, int on)
     if (!ctx)
         return BRM_ERR_INVALID_VALUE;
     ctx->validate = on != 0;
+    return BRM_SUCCESS;
+}
+
+int brm_set_tuning(brm_context ctx, const brm_tuning *t)
+{
+    if (!ctx)
+        return BRM_ERR_INVALID_VALUE;
+    const int cut = t ? t->seg_cut : brm::kSegCut;
+    const int mid = t ? t->mid_flop : brm::kMidFlop;
+    if (cut < brm::kMinSegCut || cut > brm::kSegCut || mid < brm::kMinMidFlop ||
+        mid > brm::kMidFlop)
+        return BRM_ERR_INVALID_VALUE;
+    ctx->plan.seg_cut = cut;
+    ctx->plan.mid_limit = mid;
+    ctx->planned = false;  // a plan made under other knobs is not reused
+    return BRM_SUCCESS;
+}
+
+int brm_get_tuning(brm_context ctx, brm_tuning *t)
+{
+    if (!ctx || !t)
+        return BRM_ERR_INVALID_VALUE;
+    t->seg_cut = ctx->plan.seg_cut;
+    t->mid_flop = ctx->plan.mid_limit;
+    return BRM_SUCCESS;
+}
+
+int brm_autotune(brm_context ctx, brm_dtype dtype, int n, const brm_csr *A, const brm_csr *B,
+                 brm_tuning *best)
+{
+    if (!ctx || n < 1 || !A || !B)
+        return BRM_ERR_INVALID_VALUE;
+    BRM_TRY(check_dtype(dtype));
+    brm_tuning keep;
+    BRM_TRY(brm_get_tuning(ctx, &keep));
+    // one call of the form the caller will use: a single product or a batch
+    auto run_once = [&](double *sec) -> int {
+        const double t0 = now_sec();
+        if (n == 1) {
+            int *crpt = nullptr, *ccol = nullptr;
+            void *cval = nullptr;
+            int cnnz = 0;
+            BRM_TRY(brm_precise_device(ctx, dtype, A, B, &crpt, &ccol, &cval, &cnnz, nullptr));
+            *sec = now_sec() - t0;
+            brm_device_free(ctx, crpt);
+            brm_device_free(ctx, ccol);
+            brm_device_free(ctx, cval);
+        } else {
+            brm_batch b;
+            BRM_TRY(brm_batch_precise(ctx, dtype, n, A, B, &b));
+            *sec = now_sec() - t0;
+            brm_batch_free(ctx, &b);
+        }
+        return BRM_SUCCESS;
+    };
+    double warm = 0;
+    BRM_TRY(brm_set_tuning(ctx, nullptr));
+    BRM_TRY(run_once(&warm));  // allocations and caches out of the timed runs
+    brm_tuning pick = {brm::kSegCut, brm::kMidFlop};
+    double pick_s = 1e300;
+    for (const int cut : kTuneSegCut) {
+        for (const int mid : kTuneMidFlop) {
+            brm_tuning t = {cut, mid};
+            BRM_TRY(brm_set_tuning(ctx, &t));
+            double s = 1e300;
+            for (int rep = 0; rep < 2; rep++) {  // best of two
+                double r = 0;
+                const int st = run_once(&r);
+                if (st != BRM_SUCCESS) {
+                    brm_set_tuning(ctx, &keep);
+                    return st;
+                }
+                s = std::min(s, r);
+            }
+            if (s < pick_s) {
+                pick_s = s;
+                pick = t;
+            }
+        }
+    }
+    BRM_TRY(brm_set_tuning(ctx, &pick));
+    if (best)
+        *best = pick;
     return BRM_SUCCESS;
 }
 

@@ -565,20 +565,22 @@ __global__ void __launch_bounds__(kMidThreads) k_mid_numeric(CsrDev A, CsrDev B,
 }
 
 // Batch starts: batch b begins at the first row whose mid-weight prefix is
-// >= b * kMidFlop; n_batch = ceil(total / kMidFlop).
+// >= b * W; n_batch = ceil(total / W), W = P.mid_limit (<= kMidFlop, every
+// mid row weighs at most W, so a batch weighs less than 2 W <= kMidCap).
 template <int UNUSED = 0>
 __global__ void __launch_bounds__(256) k_batch_starts(PlanDev P, int M)
 {
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r > M)
         return;
+    const long long W = P.mid_limit;
     const long long hi = P.mid_pre[r];
     const long long lo = r > 0 ? P.mid_pre[r - 1] : -1;
-    const long long b = hi / kMidFlop;
-    if (b * kMidFlop > lo && b <= M)
+    const long long b = hi / W;
+    if (b * W > lo && b <= M)
         P.batch_start[b] = r;
     if (r == M)
-        P.cnt->n_batch = (int)((hi + kMidFlop - 1) / kMidFlop);
+        P.cnt->n_batch = (int)((hi + W - 1) / W);
 }
 
 // Moves the mid rows written by k_mid_numeric<..., SCRATCH> from the

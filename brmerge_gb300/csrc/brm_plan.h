@@ -97,16 +97,26 @@ struct Counters {
     unsigned long long long_used;
 };
 
-// Descriptor slots reserved for a heavy row with F products: the cut rule
-// makes at most F / kSegCut cuts at product thresholds (plus one per chunk),
-// 2 per dense word (a word with more than kSegCut products; at most
-// F / kSegCut of them) and at most 2 h / kSegCut + 1 inside a dense word of h
-// products, plus one chunk start per kPlanBits columns.
-__host__ __device__ inline unsigned long long seg_bound(long long F, int N)
+// Descriptor slots reserved for a heavy row with F products and the cut
+// target `cut` (<= kSegCut): the cut rule makes at most F / cut cuts at
+// product thresholds (plus one per chunk), 2 per dense group (a group with
+// more than kSegCap - cut >= cut products; at most F / cut of them) and at
+// most 2 h / cut + 1 inside a dense group of h products, plus one chunk start
+// per kPlanBits columns.
+__host__ __device__ inline unsigned long long seg_bound(long long F, int N, int cut)
 {
-    return 6ull * (unsigned long long)((F + kSegCut - 1) / kSegCut) +
+    return 6ull * (unsigned long long)((F + cut - 1) / cut) +
            2ull * ((unsigned)N / (unsigned)kPlanBits) + 8ull;
 }
+
+// Runtime policy knobs of the row classes (chosen by brm_autotune or
+// brm_set_tuning; every capacity stays compile-time): the heavy-row cut
+// target seg_cut in [kMinSegCut, kSegCut] (segments hold at most kSegCap
+// products whatever the target) and the mid-row weight limit mid_flop in
+// [kMinMidFlop, kMidFlop] (batches hold at most 2 * mid_flop <= kMidCap).
+// The results do not depend on them: only where rows and segments are cut.
+constexpr int kMinSegCut = 256;
+constexpr int kMinMidFlop = 128;
 
 // One column segment of a heavy row.
 struct SegDesc {
@@ -163,6 +173,9 @@ struct PlanDev {
     int r_lo;
     int r_hi;
     const int *seg_range;
+    // policy knobs (see kMinSegCut): heavy-row cut target, mid-row weight limit
+    int seg_cut;
+    int mid_limit;
     Counters *cnt;
 };
 

@@ -11,9 +11,10 @@
 //      a bitmap of the row's columns and a product count per 128-column group
 //      over chunks of kPlanBits columns give the row's exact nnz and the cut
 //      points: a cut before group g when the running product count crosses a
-//      multiple of kSegCut and around groups holding more than kSegCut
-//      products (inside such a group the cuts are per column, from 16-bit
-//      per-column counts); a segment then holds <= kSegCap products.  Its
+//      multiple of the cut target (at most kSegCut, a runtime knob) and
+//      around groups holding more than kSegCap minus the target (inside such
+//      a group the cuts are per column, from 16-bit per-column counts); a
+//      segment then holds <= kSegCap products.  Its
 //      output offset within the row (distinct columns before c_lo) comes
 //      from the same bitmap.
 //   2. split table (numeric phase): for every segment boundary and every list
@@ -43,7 +44,7 @@ namespace brm {
 
 constexpr int kPlanThreads = 512;
 // Segment cuts are placed at planning-group boundaries (kPlanGroupBits
-// columns); a group with more than kSegCut products gets per-column counts
+// columns); a dense group (more than kSegCap - cut products) gets per-column counts
 // (at most kDenseGroups such groups per chunk).
 constexpr int kPlanGroupLog2 = 7;
 constexpr int kPlanGroupBits = 1 << kPlanGroupLog2;      // 128 columns
@@ -135,27 +136,29 @@ __device__ __forceinline__ void plan_products(const PlanDev &P, const int *__res
 // Walks the segment starts of planning group g (chunk-relative) in column
 // order and calls f(column_in_group, product_prefix, distinct_prefix) for
 // each.  `run` packs (products << 32 | distinct columns) before group g and
-// ph is the product count of group g-1.  A group with more than kSegCut
-// products is always cut before and after; inside it, a new segment starts
-// at a column when the running product count would exceed kSegCut.  Any
-// other group starts a segment when the group before it crossed a multiple
-// of kSegCut, so a segment holds less than 2 * kSegCut = kSegCap products.
+// ph is the product count of group g-1.  A dense group (more than
+// dense = kSegCap - cut >= cut products) is always cut before and after;
+// inside it, a new segment starts at a column when the running product count
+// would exceed `cut` (a single column above `cut` is a segment of its own).
+// Any other group starts a segment when the group before it crossed a
+// multiple of `cut`, so a segment holds less than cut + dense = kSegCap
+// products.
 template <typename Fn>
 __device__ __forceinline__ void plan_group_starts(int g, unsigned h, unsigned ph,
                                                   unsigned long long run,
-                                                  const unsigned short *ccnt,
-                                                  Fn f)
+                                                  const unsigned short *ccnt, unsigned cut,
+                                                  unsigned dense, Fn f)
 {
     const unsigned pe = (unsigned)(run >> 32);
     const unsigned ue = (unsigned)(run & 0xffffffffu);
-    if (h > (unsigned)kSegCut) {
+    if (h > dense) {
         f(0, pe, ue);
         unsigned acc = 0, pp = pe, uu = ue;
         for (int c = 0; c < kPlanGroupBits; c++) {
             const unsigned cc = ccnt[c];
             if (cc == 0)
                 continue;
-            if (acc > 0 && acc + cc > (unsigned)kSegCut) {
+            if (acc > 0 && acc + cc > cut) {
                 f(c, pp, uu);
                 acc = 0;
             }
@@ -165,7 +168,7 @@ __device__ __forceinline__ void plan_group_starts(int g, unsigned h, unsigned ph
         }
         return;
     }
-    const bool start = (g == 0) || ph > (unsigned)kSegCut || (pe / kSegCut) != ((pe - ph) / kSegCut);
+    const bool start = (g == 0) || ph > dense || (pe / cut) != ((pe - ph) / cut);
     if (start)
         f(0, pe, ue);
 }
@@ -196,6 +199,8 @@ __global__ void __launch_bounds__(kPlanThreads) k_heavy_plan(CsrDev A, CsrDev B,
     const int nrows = P.cnt->bin_count[kBinHeavy] + nhuge;
     const int *rows = P.rows + (size_t)kBinHeavy * M;
     const int *__restrict__ bcol = B.col;
+    const unsigned cut = (unsigned)P.seg_cut;                // <= kSegCut
+    const unsigned dense = (unsigned)(kSegCap - P.seg_cut);  // >= cut
     for (int i = tid; i < kPlanWords; i += NT)
         bm[i] = 0;
     for (int i = tid; i < kPlanGroups; i += NT)
@@ -213,7 +218,7 @@ __global__ void __launch_bounds__(kPlanThreads) k_heavy_plan(CsrDev A, CsrDev B,
         const int k = A.rpt[row + 1] - a0;
         const long long F = P.flop[row];
         const unsigned long long base = P.seg_base[row];
-        const unsigned long long bound = seg_bound(F, B.N);
+        const unsigned long long bound = seg_bound(F, B.N, P.seg_cut);
         const int2 cr = P.crange[row];  // written by the analysis
         const int mn = cr.x, mx = cr.y;
         if (mx < 0 || mn < 0 || mx >= B.N) {
@@ -287,7 +292,7 @@ __global__ void __launch_bounds__(kPlanThreads) k_heavy_plan(CsrDev A, CsrDev B,
                 for (int q = 0; q < kPlanGroupWords; q++)
                     pc += __popc(bm[g * kPlanGroupWords + q]);
                 gpop[g] = (unsigned short)pc;
-                if (h > (unsigned)kSegCut) {
+                if (h > dense) {
                     nd_local++;
                     dlo = min(dlo, g);
                     dhi = g;
@@ -305,7 +310,7 @@ __global__ void __launch_bounds__(kPlanThreads) k_heavy_plan(CsrDev A, CsrDev B,
                 fail = true;  // uniform
             if (!fail && nd > 0) {
                 for (int g = g0; g < g1; g++)
-                    if (hist[g] > (unsigned)kSegCut)
+                    if (hist[g] > dense)
                         dix[g] = (unsigned short)dx++;
                 for (int i = tid; i < nd * kPlanGroupBits / 2; i += NT)
                     ccnt2[i] = 0;
@@ -317,7 +322,7 @@ __global__ void __launch_bounds__(kPlanThreads) k_heavy_plan(CsrDev A, CsrDev B,
                 plan_products<NT>(P, bcol, a0, k, true, dlo_c, dhi_c, lo, lst, loffs, ws, [&](int rc) {
                     if ((unsigned)rc < (unsigned)span) {
                         const int g = rc >> kPlanGroupLog2;
-                        if (hist[g] > (unsigned)kSegCut) {
+                        if (hist[g] > dense) {
                             const int slot = dix[g] * kPlanGroupBits + (rc & (kPlanGroupBits - 1));
                             atomicAdd(&ccnt2[slot >> 1], 1u << (16 * (slot & 1)));
                         }
@@ -339,8 +344,8 @@ __global__ void __launch_bounds__(kPlanThreads) k_heavy_plan(CsrDev A, CsrDev B,
                 for (int g = g0; g < g1; g++) {
                     const unsigned h = hist[g];
                     plan_group_starts(g, h, ph, run,
-                                      h > (unsigned)kSegCut ? ccnt + dix[g] * kPlanGroupBits : ccnt,
-                                      [&](int, unsigned, unsigned) { nstart++; });
+                                      h > dense ? ccnt + dix[g] * kPlanGroupBits : ccnt, cut,
+                                      dense, [&](int, unsigned, unsigned) { nstart++; });
                     run += ((unsigned long long)h << 32) | (unsigned)gpop[g];
                     ph = h;
                 }
@@ -370,8 +375,8 @@ __global__ void __launch_bounds__(kPlanThreads) k_heavy_plan(CsrDev A, CsrDev B,
                 for (int g = g0; g < g1; g++) {
                     const unsigned h = hist[g];
                     plan_group_starts(g, h, ph, run,
-                                      h > (unsigned)kSegCut ? ccnt + dix[g] * kPlanGroupBits : ccnt,
-                                      [&](int c, unsigned pe, unsigned ue) {
+                                      h > dense ? ccnt + dix[g] * kPlanGroupBits : ccnt, cut,
+                                      dense, [&](int c, unsigned pe, unsigned ue) {
                                           SegDesc &d = P.seg[base + nseg + r];
                                           d.row = row;
                                           d.c_lo = lo + kPlanGroupBits * g + c;

@@ -100,6 +100,32 @@ int brm_destroy(brm_context ctx);
 /* cudaStream_t passed as void*; NULL selects the legacy default stream. */
 int brm_set_stream(brm_context ctx, void *stream);
 int brm_set_validate(brm_context ctx, int on);
+
+/* Row-class policy of a context.  The reference balances rows over threads
+ * by flop (spgemm.h:496-503); here rows are binned and heavy rows cut into
+ * segments, and two thresholds of that are runtime knobs: seg_cut, the
+ * products between cuts of a heavy row (256 .. 1536; segments hold at most
+ * 3072 products), and mid_flop, the largest row weight of the batched
+ * mid-row kernels (128 .. 2048; batches hold at most 4096).  Results do not
+ * depend on them, only speed does. */
+typedef struct brm_tuning {
+    int seg_cut;
+    int mid_flop;
+} brm_tuning;
+
+/* NULL restores the defaults (1536, 2048); out-of-range values are
+ * BRM_ERR_INVALID_VALUE. */
+int brm_set_tuning(brm_context ctx, const brm_tuning *t);
+int brm_get_tuning(brm_context ctx, brm_tuning *t);
+
+/* Times the one-call Precise form on the caller's own input (n == 1:
+ * brm_precise_device on A[0], B[0]; n > 1: brm_batch_precise on the n pairs)
+ * under each candidate setting (seg_cut in {1536, 1024, 768, 512} x mid_flop
+ * in {2048, 1024, 512}, best of two runs each after one warm-up), keeps the
+ * fastest in the context and returns it in *best (may be NULL).  No
+ * counterpart in the reference. */
+int brm_autotune(brm_context ctx, brm_dtype dtype, int n, const brm_csr *A, const brm_csr *B,
+                 brm_tuning *best);
 /* Device-side error bits of the last call on this context (diagnostics). */
 int brm_last_device_error(brm_context ctx);
 const char *brm_status_string(int status);
