@@ -120,6 +120,10 @@ def lib() -> C.CDLL:
         _decl(L.brm_free, None, [vp])
         _decl(L.brm_host_cache_release, None, [])
         _decl(L.brm_kernel_launches, C.c_longlong, [])
+        _decl(L.brm_batch_graph_create, C.c_int,
+              [vp, C.c_int, C.c_int, csrp, csrp, ctxp, C.POINTER(BatchC)])
+        _decl(L.brm_batch_graph_launch, C.c_int, [vp, vp])
+        _decl(L.brm_batch_graph_destroy, C.c_int, [vp])
         _decl(L.brm_set_tuning, C.c_int, [vp, C.POINTER(TuningC)])
         _decl(L.brm_get_tuning, C.c_int, [vp, C.POINTER(TuningC)])
         _decl(L.brm_autotune, C.c_int, [vp, C.c_int, C.c_int, csrp, csrp, C.POINTER(TuningC)])

@@ -693,6 +693,20 @@ cudaStream_t brm::context_stream(brm_context ctx) { return ctx->stream; }
 
 int brm::context_num_sms(brm_context ctx) { return ctx->num_sms; }
 
+int brm::numeric_async(brm_context ctx, brm_dtype dtype, const brm_csr *A, const brm_csr *B,
+                       const int *crpt, int *ccol, void *cval)
+{
+    if (!ctx || !crpt)
+        return BRM_ERR_INVALID_VALUE;
+    BRM_TRY(check_dtype(dtype));
+    BRM_TRY(check_pair(A, B));
+    if (!plan_matches(ctx, A, B))
+        return BRM_ERR_NOT_PLANNED;
+    return numeric_launch(ctx, dtype, false, A, B, crpt, ccol, cval);
+}
+
+int brm::read_device_error(brm_context ctx) { return read_err(ctx); }
+
 extern "C" {
 
 const char *brm_status_string(int status)

@@ -158,23 +158,17 @@ int grow_buf(Buf &b, size_t bytes, cudaStream_t s)
 
 size_t a256(size_t x) { return (x + 255) & ~size_t(255); }
 
-}  // namespace
-
-extern "C" {
-
-int brm_batch_precise(brm_context ctx, brm_dtype dtype, int n, const brm_csr *A, const brm_csr *B,
-                      brm_batch *out)
+// Offsets of every pair in the block-diagonal operands: hp[i] and, in off,
+// four arrays of n + 1 prefixes (A rows, A entries, B rows, B entries); the
+// totals in ra, na, rb, nb and cb (B columns).  BRM_ERR_INVALID_VALUE for a
+// malformed pair, BRM_ERR_CAPACITY when a total does not fit int32.
+int batch_layout(int n, const brm_csr *A, const brm_csr *B, std::vector<brm::BatchPair> &hp,
+                 std::vector<long long> &off, long long &ra, long long &na, long long &rb,
+                 long long &nb, long long &cb)
 {
-    if (!ctx || !out || n < 0 || (n > 0 && (!A || !B)))
-        return BRM_ERR_INVALID_VALUE;
-    if (dtype != BRM_F64 && dtype != BRM_F32)
-        return BRM_ERR_INVALID_VALUE;
-    std::memset(out, 0, sizeof(*out));
-    out->n = n;
-    // offsets of every pair in the block-diagonal operands
-    std::vector<brm::BatchPair> hp((size_t)n);
-    std::vector<long long> off((size_t)(n + 1) * 4, 0);  // row_a, nnz_a, row_b, nnz_b
-    long long ra = 0, na = 0, rb = 0, nb = 0, cb = 0;
+    hp.assign((size_t)n, brm::BatchPair{});
+    off.assign((size_t)(n + 1) * 4, 0);
+    ra = na = rb = nb = cb = 0;
     for (int i = 0; i < n; i++) {
         const brm_csr &a = A[i], &b = B[i];
         if (a.M < 0 || a.N < 0 || b.M < 0 || b.N < 0 || a.nnz < 0 || b.nnz < 0 || a.N != b.M ||
@@ -214,6 +208,53 @@ int brm_batch_precise(brm_context ctx, brm_dtype dtype, int n, const brm_csr *A,
     off[(size_t)3 * (n + 1) + n] = nb;
     if (ra >= INT_MAX || na > INT_MAX || rb >= INT_MAX || nb > INT_MAX || cb > INT_MAX)
         return BRM_ERR_CAPACITY;  // the concatenation must fit int32 indices
+    return BRM_SUCCESS;
+}
+
+// Gathers the pairs' columns and values into the block-diagonal operands.
+void launch_entries(brm_dtype dtype, const brm::BatchPair *dp, int n, const long long *doff,
+                    long long na, long long nb, int *A_col, void *A_val, int *B_col, void *B_val,
+                    int grid, cudaStream_t s)
+{
+    if (dtype == BRM_F64) {
+        brm::k_batch_entries<double><<<grid, 256, 0, s>>>(dp, n, doff + (n + 1), na, 0, A_col,
+                                                          (double *)A_val);
+        brm::count_launch();
+        brm::k_batch_entries<double><<<grid, 256, 0, s>>>(dp, n, doff + 3 * (n + 1), nb, 1, B_col,
+                                                          (double *)B_val);
+        brm::count_launch();
+    } else {
+        brm::k_batch_entries<float><<<grid, 256, 0, s>>>(dp, n, doff + (n + 1), na, 0, A_col,
+                                                         (float *)A_val);
+        brm::count_launch();
+        brm::k_batch_entries<float><<<grid, 256, 0, s>>>(dp, n, doff + 3 * (n + 1), nb, 1, B_col,
+                                                         (float *)B_val);
+        brm::count_launch();
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+int brm_batch_precise(brm_context ctx, brm_dtype dtype, int n, const brm_csr *A, const brm_csr *B,
+                      brm_batch *out)
+{
+    if (!ctx || !out || n < 0 || (n > 0 && (!A || !B)))
+        return BRM_ERR_INVALID_VALUE;
+    if (dtype != BRM_F64 && dtype != BRM_F32)
+        return BRM_ERR_INVALID_VALUE;
+    std::memset(out, 0, sizeof(*out));
+    out->n = n;
+    // offsets of every pair in the block-diagonal operands
+    std::vector<brm::BatchPair> hp;
+    std::vector<long long> off;
+    long long ra = 0, na = 0, rb = 0, nb = 0, cb = 0;
+    {
+        const int st = batch_layout(n, A, B, hp, off, ra, na, rb, nb, cb);
+        if (st != BRM_SUCCESS)
+            return st;
+    }
     out->rows = ra;
     if (n == 0)
         return BRM_SUCCESS;
@@ -349,6 +390,225 @@ int brm_batch_free(brm_context ctx, brm_batch *b)
     std::free(b->row_off);
     std::free(b->nnz_off);
     std::memset(b, 0, sizeof(*b));
+    return st;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Batch with a fixed structure replayed as a CUDA graph.  The block-diagonal
+// structure, the symbolic plan and C's row pointers are made once; the part
+// that depends on the values (gathering every pair's current values into the
+// block-diagonal operands, the numeric phase, shifting C's columns back) is
+// captured once and replayed with one graph launch per recomputation.
+// ---------------------------------------------------------------------------
+struct brm_batch_graph_s {
+    brm_context ctx = nullptr;     // private: its plan belongs to this batch
+    cudaStream_t stream = nullptr;  // the private context's stream
+    cudaStream_t cap = nullptr;     // capture stream
+    brm_dtype dtype = BRM_F64;
+    int n = 0;
+    long long ra = 0, na = 0, rb = 0, nb = 0, cb = 0;
+    void *mem = nullptr;            // pair table, offsets, first entries, A_bd, B_bd
+    brm::BatchPair *dp = nullptr;
+    long long *doff = nullptr, *dfirst = nullptr;
+    brm_csr Abd{}, Bbd{};
+    brm_batch out{};
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+};
+
+namespace {
+
+// Enqueues the value-dependent part on the private context's current stream.
+int batch_graph_values(brm_batch_graph g)
+{
+    cudaStream_t s = brm::context_stream(g->ctx);
+    const int grid = std::max(brm::context_num_sms(g->ctx), 1) * 16;
+    launch_entries(g->dtype, g->dp, g->n, g->doff, g->na, g->nb, (int *)g->Abd.col,
+                   (void *)g->Abd.val, (int *)g->Bbd.col, (void *)g->Bbd.val, grid, s);
+    const int st = brm::numeric_async(g->ctx, g->dtype, &g->Abd, &g->Bbd, g->out.crpt, g->out.ccol,
+                                      g->out.cval);
+    if (st != BRM_SUCCESS)
+        return st;
+    brm::k_batch_unshift<<<grid, 256, 0, s>>>(g->dp, g->n, g->doff, (int)g->ra, g->out.crpt,
+                                              g->out.ccol, g->dfirst);
+    brm::count_launch();
+    return cudaGetLastError() == cudaSuccess ? BRM_SUCCESS : BRM_ERR_CUDA;
+}
+
+}  // namespace
+
+extern "C" {
+
+int brm_batch_graph_destroy(brm_batch_graph g)
+{
+    if (!g)
+        return BRM_SUCCESS;
+    if (g->stream)
+        cudaStreamSynchronize(g->stream);
+    if (g->exec)
+        cudaGraphExecDestroy(g->exec);
+    if (g->graph)
+        cudaGraphDestroy(g->graph);
+    brm_batch_free(g->ctx, &g->out);
+    if (g->mem)
+        cudaFree(g->mem);
+    if (g->ctx)
+        brm_destroy(g->ctx);
+    if (g->cap)
+        cudaStreamDestroy(g->cap);
+    if (g->stream)
+        cudaStreamDestroy(g->stream);
+    (void)cudaGetLastError();
+    delete g;
+    return BRM_SUCCESS;
+}
+
+int brm_batch_graph_create(brm_context ctx, brm_dtype dtype, int n, const brm_csr *A,
+                           const brm_csr *B, brm_batch_graph *out_g, brm_batch *out)
+{
+    if (!ctx || !out_g || !out || n < 1 || !A || !B || (dtype != BRM_F64 && dtype != BRM_F32))
+        return BRM_ERR_INVALID_VALUE;
+    *out_g = nullptr;
+    std::memset(out, 0, sizeof(*out));
+    brm_batch_graph g = new (std::nothrow) brm_batch_graph_s();
+    if (!g)
+        return BRM_ERR_ALLOC;
+    g->dtype = dtype;
+    g->n = n;
+    std::vector<brm::BatchPair> hp;
+    std::vector<long long> off;
+    int st = batch_layout(n, A, B, hp, off, g->ra, g->na, g->rb, g->nb, g->cb);
+    brm_tuning tune;
+    if (st == BRM_SUCCESS)
+        st = brm_get_tuning(ctx, &tune);
+    if (st == BRM_SUCCESS)
+        st = brm_create(&g->ctx);
+    if (st == BRM_SUCCESS)
+        st = brm_set_tuning(g->ctx, &tune);
+    if (st == BRM_SUCCESS &&
+        (cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking) != cudaSuccess ||
+         cudaStreamCreateWithFlags(&g->cap, cudaStreamNonBlocking) != cudaSuccess))
+        st = BRM_ERR_CUDA;
+    if (st == BRM_SUCCESS)
+        st = brm_set_stream(g->ctx, g->stream);
+    const size_t vb = dtype == BRM_F64 ? 8 : 4;
+    const size_t b_pairs = a256(sizeof(brm::BatchPair) * (size_t)n);
+    const size_t b_off = a256(sizeof(long long) * off.size());
+    const size_t b_first = a256(sizeof(long long) * (size_t)(n + 1));
+    const size_t a_rpt = a256(4 * (size_t)(g->ra + 1)), a_col = a256(4 * (size_t)std::max(g->na, 1LL));
+    const size_t a_val = a256(vb * (size_t)std::max(g->na, 1LL));
+    const size_t b_rpt = a256(4 * (size_t)(g->rb + 1)), b_col = a256(4 * (size_t)std::max(g->nb, 1LL));
+    const size_t b_val = a256(vb * (size_t)std::max(g->nb, 1LL));
+    if (st == BRM_SUCCESS &&
+        cudaMalloc(&g->mem, b_pairs + b_off + b_first + a_rpt + a_col + a_val + b_rpt + b_col +
+                                b_val) != cudaSuccess)
+        st = BRM_ERR_ALLOC;
+    if (st != BRM_SUCCESS) {
+        (void)cudaGetLastError();
+        brm_batch_graph_destroy(g);
+        return st;
+    }
+    char *p = (char *)g->mem;
+    g->dp = (brm::BatchPair *)p;
+    g->doff = (long long *)(p += b_pairs);
+    g->dfirst = (long long *)(p += b_off);
+    int *A_rpt = (int *)(p += b_first);
+    int *A_col = (int *)(p += a_rpt);
+    void *A_val = (p += a_col);
+    int *B_rpt = (int *)(p += a_val);
+    int *B_col = (int *)(p += b_rpt);
+    void *B_val = (p += b_col);
+    g->Abd = brm_csr{(int)g->ra, (int)g->rb, (int)g->na, A_rpt, A_col, A_val};
+    g->Bbd = brm_csr{(int)g->rb, (int)g->cb, (int)g->nb, B_rpt, B_col, B_val};
+    cudaStream_t s = g->stream;
+    const int grid = std::max(brm::context_num_sms(g->ctx), 1) * 16;
+    cudaError_t e = cudaMemcpyAsync(g->dp, hp.data(), sizeof(brm::BatchPair) * (size_t)n,
+                                    cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(g->doff, off.data(), sizeof(long long) * off.size(),
+                            cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) {
+        brm::k_batch_rows<<<grid, 256, 0, s>>>(g->dp, n, g->doff, g->ra, 0, A_rpt);
+        brm::count_launch();
+        brm::k_batch_rows<<<grid, 256, 0, s>>>(g->dp, n, g->doff + 2 * (n + 1), g->rb, 1, B_rpt);
+        brm::count_launch();
+        launch_entries(dtype, g->dp, n, g->doff, g->na, g->nb, A_col, A_val, B_col, B_val, grid, s);
+        e = cudaGetLastError();
+    }
+    // structure once: symbolic plan and C's row pointers, C's arrays
+    int cnnz = 0;
+    if (e == cudaSuccess &&
+        cudaMallocAsync((void **)&g->out.crpt, 4 * (size_t)(g->ra + 1), s) != cudaSuccess)
+        e = cudaErrorMemoryAllocation;
+    st = e == cudaSuccess ? brm_symbolic(g->ctx, &g->Abd, &g->Bbd, g->out.crpt, &cnnz)
+                          : BRM_ERR_CUDA;
+    if (st == BRM_SUCCESS &&
+        (cudaMallocAsync((void **)&g->out.ccol, 4 * (size_t)std::max(cnnz, 1), s) != cudaSuccess ||
+         cudaMallocAsync(&g->out.cval, vb * (size_t)std::max(cnnz, 1), s) != cudaSuccess ||
+         cudaMallocAsync((void **)&g->out.rpt_local, 4 * (size_t)(g->ra + n), s) != cudaSuccess))
+        st = BRM_ERR_ALLOC;
+    // first run, uncaptured: sizes every numeric buffer of the plan
+    if (st == BRM_SUCCESS)
+        st = batch_graph_values(g);
+    if (st == BRM_SUCCESS) {
+        brm::k_batch_local_rpt<<<grid, 256, 0, s>>>(n, g->doff, g->ra, g->out.crpt, g->dfirst,
+                                                    g->out.rpt_local);
+        brm::count_launch();
+        st = brm::read_device_error(g->ctx);  // synchronises
+    }
+    g->out.n = n;
+    g->out.rows = g->ra;
+    g->out.nnz = cnnz;
+    g->out.row_off = (long long *)std::malloc(sizeof(long long) * (size_t)(n + 1));
+    g->out.nnz_off = (long long *)std::malloc(sizeof(long long) * (size_t)(n + 1));
+    if (st == BRM_SUCCESS && (!g->out.row_off || !g->out.nnz_off))
+        st = BRM_ERR_ALLOC;
+    if (st == BRM_SUCCESS) {
+        std::memcpy(g->out.row_off, off.data(), sizeof(long long) * (size_t)(n + 1));
+        if (cudaMemcpy(g->out.nnz_off, g->dfirst, sizeof(long long) * (size_t)(n + 1),
+                       cudaMemcpyDeviceToHost) != cudaSuccess)
+            st = BRM_ERR_CUDA;
+    }
+    // capture the value-dependent part on a second stream
+    if (st == BRM_SUCCESS) {
+        brm_set_stream(g->ctx, g->cap);
+        if (cudaStreamBeginCapture(g->cap, cudaStreamCaptureModeRelaxed) != cudaSuccess) {
+            st = BRM_ERR_CUDA;
+        } else {
+            const int st2 = batch_graph_values(g);
+            const cudaError_t e2 = cudaStreamEndCapture(g->cap, &g->graph);
+            st = st2 != BRM_SUCCESS ? st2 : (e2 == cudaSuccess ? BRM_SUCCESS : BRM_ERR_CUDA);
+        }
+        brm_set_stream(g->ctx, g->stream);
+        if (st == BRM_SUCCESS && cudaGraphInstantiate(&g->exec, g->graph, 0) != cudaSuccess)
+            st = BRM_ERR_CUDA;
+    }
+    if (st != BRM_SUCCESS) {
+        (void)cudaGetLastError();
+        brm_batch_graph_destroy(g);
+        std::memset(out, 0, sizeof(*out));
+        return st;
+    }
+    *out = g->out;
+    *out_g = g;
+    return BRM_SUCCESS;
+}
+
+int brm_batch_graph_launch(brm_batch_graph g, void *stream)
+{
+    if (!g || !g->exec)
+        return BRM_ERR_INVALID_VALUE;
+    cudaStream_t s = (cudaStream_t)stream;
+    if (cudaGraphLaunch(g->exec, s) != cudaSuccess) {
+        (void)cudaGetLastError();
+        return BRM_ERR_CUDA;
+    }
+    // the numeric phase's error word, read on the launch stream
+    brm_set_stream(g->ctx, s);
+    const int st = brm::read_device_error(g->ctx);
+    brm_set_stream(g->ctx, g->stream);
     return st;
 }
 

@@ -12,6 +12,14 @@ namespace brm {
 cudaStream_t context_stream(brm_context ctx);
 int context_num_sms(brm_context ctx);
 
+// brm_numeric without its closing synchronisation (it only enqueues work on
+// the context stream, so it can be captured into a CUDA graph once every
+// buffer it needs has been sized by an earlier numeric call on the same
+// plan), and the error-word read that brm_numeric ends with.
+int numeric_async(brm_context ctx, brm_dtype dtype, const brm_csr *A, const brm_csr *B,
+                  const int *crpt, int *ccol, void *cval);
+int read_device_error(brm_context ctx);
+
 // Counts one kernel launch of this library (brm_kernel_launches reports the
 // process-wide total); every launch site calls it right after <<<...>>>.
 void count_launch();

@@ -331,6 +331,11 @@ class Context:
         self._L.brm_batch_free(self._h, C.byref(out))
         return crpt, ccol, cval, roff, noff, lrpt
 
+    def batch_graph(self, pairs) -> "BatchGraph":
+        """brm_batch_graph_create: a batch of fixed structure whose values can
+        be recomputed with one CUDA-graph launch (BatchGraph.launch)."""
+        return BatchGraph(self, pairs)
+
     def batch_precise(self, pairs) -> list:
         """brm_batch_precise: C_i = A_i * B_i for a list of (A_i, B_i)
         DeviceCSR pairs of one value type, in one pipeline.  Returns the C_i
@@ -380,6 +385,62 @@ class _RawDevice:
     def __init__(self, ptr: int, n: int, typestr: str):
         self.__cuda_array_interface__ = {
             "shape": (n,), "typestr": typestr, "data": (ptr, False), "version": 2, "strides": None}
+
+
+class BatchGraph:
+    """A batch of fixed structure (brm_batch_graph_*).  `results` are views
+    of C_i owned by the graph (valid until close); `launch` recomputes them
+    from the pairs' current values with one graph launch."""
+
+    def __init__(self, ctx: "Context", pairs):
+        import torch
+        self._L = _native.lib()
+        self._h = C.c_void_p()
+        self._pairs = list(pairs)  # the graph reads their arrays at every launch
+        n = len(self._pairs)
+        dt = self._pairs[0][0].val.dtype
+        code = _dtype_code(np.float64 if dt == torch.float64 else np.float32)
+        As = (_native.CsrC * n)(*[a.c() for a, _ in self._pairs])
+        Bs = (_native.CsrC * n)(*[b.c() for _, b in self._pairs])
+        out = _native.BatchC()
+        _native.check(self._L.brm_batch_graph_create(ctx._h, code, n, As, Bs, C.byref(self._h),
+                                                     C.byref(out)), "brm_batch_graph_create")
+        dev = self._pairs[0][0].rpt.device
+        vt = "<f8" if dt == torch.float64 else "<f4"
+
+        def view(ptr, m, ts, tdt):
+            if m == 0 or not ptr:
+                return torch.empty(m, dtype=tdt, device=dev)
+            return torch.as_tensor(_RawDevice(ptr, m, ts), device=dev)
+
+        ccol = view(out.ccol, out.nnz, "<i4", torch.int32)
+        cval = view(out.cval, out.nnz, vt, dt)
+        lrpt = view(out.rpt_local, out.rows + n, "<i4", torch.int32)
+        roff = np.ctypeslib.as_array(out.row_off, shape=(n + 1,)).copy()
+        noff = np.ctypeslib.as_array(out.nnz_off, shape=(n + 1,)).copy()
+        self.results = []
+        for i, (a, b) in enumerate(self._pairs):
+            r0, r1, n0, n1 = int(roff[i]), int(roff[i + 1]), int(noff[i]), int(noff[i + 1])
+            self.results.append(DeviceCSR(a.M, b.N, lrpt[r0 + i:r1 + i + 1], ccol[n0:n1],
+                                          cval[n0:n1]))
+
+    def launch(self, stream=None):
+        ptr = None
+        if stream is not None:
+            ptr = stream.cuda_stream if hasattr(stream, "cuda_stream") else int(stream)
+        _native.check(self._L.brm_batch_graph_launch(self._h, ptr), "brm_batch_graph_launch")
+
+    def close(self):
+        if self._h:
+            self.results = []
+            self._L.brm_batch_graph_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class _Ticket:

@@ -229,6 +229,24 @@ int brm_batch_precise(brm_context ctx, brm_dtype dtype, int n, const brm_csr *A,
                       brm_batch *out);
 int brm_batch_free(brm_context ctx, brm_batch *batch);
 
+/* A batch whose structure stays fixed while its values change (the reuse
+ * pattern of iterative methods), replayed as one CUDA graph.  Create makes
+ * the block-diagonal structure, the symbolic plan and every C_i's row
+ * pointers and columns once (in a private context that copies ctx's
+ * tuning), computes the values once, and captures the value-dependent part
+ * (gathering the pairs' current values, the numeric phase, the column
+ * shift) into a graph.  Launch replays it on `stream` (cudaStream_t as void*,
+ * NULL = legacy default stream), waits for it and returns the device-side
+ * error status; the pairs' value arrays are read at launch, so the caller
+ * updates them in place (ordered before the launch) and relaunches.  *out
+ * describes C like brm_batch_precise, owned by the graph: release it only
+ * with brm_batch_graph_destroy.  No counterpart in the reference. */
+typedef struct brm_batch_graph_s *brm_batch_graph;
+int brm_batch_graph_create(brm_context ctx, brm_dtype dtype, int n, const brm_csr *A,
+                           const brm_csr *B, brm_batch_graph *graph, brm_batch *out);
+int brm_batch_graph_launch(brm_batch_graph graph, void *stream);
+int brm_batch_graph_destroy(brm_batch_graph graph);
+
 /* ---- serving: a request loop over batches ---------------------------------- */
 
 /* A server takes C = A * B requests (Precise, device CSR) from any thread.

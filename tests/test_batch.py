@@ -85,3 +85,30 @@ def test_batch_empty_and_rejects_mismatch(ctx):
     B = brm.DeviceCSR.from_host(brm.gen_uniform(65, 10, 3, seed=2))
     with pytest.raises(brm.BrmError):
         ctx.batch_precise([(A, B)])
+
+
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+def test_batch_graph_replays_new_values(ctx, oracle_mod, dtype):
+    """Fixed structure, new values: every graph launch gives what a fresh
+    batch call gives on the current values, bit for bit."""
+    import torch
+    pairs = [(A.astype(dtype), B.astype(dtype)) for A, B in _pairs(seed=3, n=18)]
+    dpairs = [(brm.DeviceCSR.from_host(A), brm.DeviceCSR.from_host(B)) for A, B in pairs]
+    g = ctx.batch_graph(dpairs)
+    for i, (A, B) in enumerate(pairs):
+        assert_same_csr(g.results[i].to_host(), oracle_mod.precise(A, B), f"graph pair {i}")
+    rng = np.random.default_rng(5)
+    for it in range(2):
+        for (A, B), (dA, dB) in zip(pairs, dpairs):
+            A.val = rng.uniform(-1, 1, A.nnz).astype(dtype)
+            B.val = rng.uniform(-1, 1, B.nnz).astype(dtype)
+            dA.val.copy_(torch.from_numpy(A.val))
+            dB.val.copy_(torch.from_numpy(B.val))
+        torch.cuda.synchronize()
+        g.launch()
+        fresh = ctx.batch_precise(dpairs)
+        for i, (A, B) in enumerate(pairs):
+            got = g.results[i].to_host()
+            assert_same_csr(got, oracle_mod.precise(A, B), f"replay {it} pair {i}")
+            assert_same_csr(got, fresh[i].to_host(), f"replay {it} pair {i} vs fresh")
+    g.close()
