@@ -356,6 +356,11 @@ __device__ __forceinline__ void mid_merge_level(int L, const unsigned short *__r
         const int ls = t.loff[l0], le = t.loff[l1], re = t.loff[l2];
         const int stop = min(p1, re);
         if (le == re) {
+            // a run without a right neighbour is copied, unless it is the
+            // slot's only run: a fully merged slot stays in the buffer of
+            // its own last level (the readers pick it by the level parity)
+            if (ns <= (1 << L))
+                p = stop;
             for (; p < stop; p++)
                 dst[p] = src[p];
         } else {
@@ -476,32 +481,42 @@ __global__ void __launch_bounds__(kMidThreads) k_mid_numeric(CsrDev A, CsrDev B,
         if (tid < nslots)
             lev = ceil_log2(t.s_lb[tid + 1] - t.s_lb[tid]);
         const int levels = (int)block_max<NT, long long>(lev, ws);
-        unsigned short *src = idx0, *dst = idx1;
-        for (int lv = 0; lv < levels; lv++) {
-            mid_merge_level(lv, src, dst, col, t, nlists, p0, p1);
-            __syncthreads();
-            unsigned short *x = src;
-            src = dst;
-            dst = x;
+        {
+            unsigned short *src = idx0, *dst = idx1;
+            for (int lv = 0; lv < levels; lv++) {
+                mid_merge_level(lv, src, dst, col, t, nlists, p0, p1);
+                __syncthreads();
+                unsigned short *x = src;
+                src = dst;
+                dst = x;
+            }
         }
+        // A slot with n lists ends its merge after ceil_log2(n) levels, in
+        // idx1 when that count is odd and in idx0 when it is even.  Each
+        // thread walks its positions [p0, p1) slot by slot.
+        int s_cur = -1, s_beg = 0, s_end = 0;
+        const unsigned short *sb = idx0;
+        auto enter = [&](int p) {
+            while (p >= s_end) {
+                s_cur = s_cur < 0 ? t.lslot[last_le(t.loff, nlists, p)] : s_cur + 1;
+                s_beg = t.loff[t.s_lb[s_cur]];
+                s_end = t.loff[t.s_lb[s_cur + 1]];
+                sb = (ceil_log2(t.s_lb[s_cur + 1] - t.s_lb[s_cur]) & 1) ? idx1 : idx0;
+            }
+        };
         // heads: first product of each (row, column) run
         int nh = 0;
         {
-            int prev_s = -1, prev_c = 0;
-            if (p0 > 0 && p0 < p1) {
-                const int e = src[p0 - 1];
-                prev_s = t.lslot[lidx[e]];
-                prev_c = col[e];
-            }
+            int prev_c = 0;
             for (int p = p0; p < p1; p++) {
-                const int e = src[p];
-                const int s = t.lslot[lidx[e]];
-                const int c = col[e];
-                if (s != prev_s || c != prev_c) {
+                enter(p);
+                const int c = col[sb[p]];
+                if (p == p0 && p > s_beg)
+                    prev_c = col[sb[p - 1]];
+                if (p == s_beg || c != prev_c) {
                     atomicOr(&head[p >> 5], 1u << (p & 31));
                     nh++;
                 }
-                prev_s = s;
                 prev_c = c;
             }
         }
@@ -510,11 +525,13 @@ __global__ void __launch_bounds__(kMidThreads) k_mid_numeric(CsrDev A, CsrDev B,
         // head index of each slot's first position
         {
             int h = hx;
+            s_cur = -1;
+            s_end = 0;
             for (int p = p0; p < p1; p++) {
                 if ((head[p >> 5] >> (p & 31)) & 1u) {
-                    const int s = t.lslot[lidx[src[p]]];
-                    if (p == t.loff[t.s_lb[s]])
-                        s_hb[s] = h;
+                    enter(p);
+                    if (p == s_beg)
+                        s_hb[s_cur] = h;
                     h++;
                 }
             }
@@ -522,30 +539,38 @@ __global__ void __launch_bounds__(kMidThreads) k_mid_numeric(CsrDev A, CsrDev B,
                 s_hb[nslots] = (int)htot;
         }
         __syncthreads();
-        // one thread per head: reduce its run in leaf order, store
+        // one thread per head: reduce its run (in leaf order: the merge is
+        // stable) and store it
         {
             int h = hx;
+            s_cur = -1;
+            s_end = 0;
             for (int p = p0; p < p1; p++) {
                 if (!((head[p >> 5] >> (p & 31)) & 1u))
                     continue;
-                const int e = src[p];
-                const int s = t.lslot[lidx[e]];
-                const int row = t.s_row[s];
+                enter(p);
+                const int e = sb[p];
+                const int row = t.s_row[s_cur];
                 const long long base = SCRATCH ? P.mid_pre[row]
                                        : (UPPER ? P.scan_flop[row] : (long long)crpt[row]);
-                const long long o = base + (h - s_hb[s]);
+                const long long o = base + (h - s_hb[s_cur]);
                 int q = p + 1;
-                T v;
-                if (q >= nprod || ((head[q >> 5] >> (q & 31)) & 1u)) {
-                    v = val[e];
-                } else {
-                    ShiftReduce<T> sr;
-                    sr.init(t.lleaf[lidx[e]], val[e]);
-                    for (; q < nprod && !((head[q >> 5] >> (q & 31)) & 1u); q++) {
-                        const int e2 = src[q];
-                        sr.push(t.lleaf[lidx[e2]], val[e2]);
+                T v = val[e];
+                if (q < s_end && !((head[q >> 5] >> (q & 31)) & 1u)) {
+                    const int e1 = sb[q++];
+                    if (!(q < s_end && !((head[q >> 5] >> (q & 31)) & 1u))) {
+                        v = vadd(v, val[e1]);  // two leaves: left + right
+                    } else {
+                        // leaves < 256: at most 8 stack entries below the top
+                        RegShiftReduce<T, 9> sr;
+                        sr.init(t.lleaf[lidx[e]], v);
+                        sr.push(t.lleaf[lidx[e1]], val[e1]);
+                        for (; q < s_end && !((head[q >> 5] >> (q & 31)) & 1u); q++) {
+                            const int e2 = sb[q];
+                            sr.push(t.lleaf[lidx[e2]], val[e2]);
+                        }
+                        v = sr.finish();
                     }
-                    v = sr.finish();
                 }
                 ccol[o] = col[e];
                 cval[o] = v;
