@@ -259,6 +259,55 @@ def upload_pairs(pairs, dev):
     return [(views[2 * i], views[2 * i + 1]) for i in range(len(pairs))], (rpt, col, val)
 
 
+def device_steps(call, dev, stream, flush, steps: int, warmup: int = 2):
+    """Mean CUDA-event time (ms) of `call()` on `stream`, L2 flushed before
+    every timed call; returns (ms, last result)."""
+    import torch
+    out = None
+    for _ in range(warmup):
+        out = call()
+        del out
+    torch.cuda.synchronize(dev)
+    ts = []
+    for i in range(steps):
+        flush.fill_(float(i))
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        out = call()
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        ts.append(e0.elapsed_time(e1))
+        if i + 1 < steps:
+            del out
+    return statistics.mean(ts), out
+
+
+def method_entry(ms: float, products: int, alg_bytes: int, peak: float) -> dict:
+    ach = alg_bytes / (ms / 1e3) / 1e9
+    return {"ms": round(ms, 4), "gflops": round(2 * products / (ms / 1e3) / 1e9, 3),
+            "achieved_gbs": round(ach, 1), "frac": round(ach / peak, 4)}
+
+
+def stencil_section(ctx, dev, stream, flush, steps: int, peak: float):
+    """27-point stencil on 128^3 (C = A*A, a 125-point stencil): Precise and
+    Upper through the one-call device forms."""
+    import brmerge_gb300 as brm
+    S = brm.gen_stencil27(128)
+    products = brm.compute_flop_host(S, S)
+    dS = brm.DeviceCSR.from_host(S, dev)
+    res = {"workload": "stencil27_128^3_AxA", "n": S.M, "nnz_A": int(S.nnz),
+           "products": int(products)}
+    ms, C = device_steps(lambda: ctx.precise_device(dS, dS), dev, stream, flush, steps)
+    res["nnz_C"] = int(C.nnz)
+    alg = 2 * csr_bytes(S.M, S.nnz, 8) + csr_bytes(S.M, C.nnz, 8)
+    del C
+    res["precise"] = method_entry(ms, products, alg, peak)
+    ms, C = device_steps(lambda: ctx.upper(dS, dS), dev, stream, flush, steps)
+    del C
+    res["upper"] = method_entry(ms, products, alg, peak)
+    return res
+
+
 def batched_section(ctx, dev, stream, steps: int):
     """The uneven batch through brm_batch_precise (one pipeline for every
     pair) against a loop of plain per-pair brm_precise_device calls."""
@@ -510,9 +559,15 @@ def run_ours(args):
     e2e_val = 2 * products * args.steps * ws / e2e_s / 1e9
     h2d = csr_bytes(A.M, A.nnz, vb)  # A and B are the same host arrays: copied once
 
-    batched = served = None
+    # BRMerge-Upper on the same workload (one call: C_bar, nnz scan, compaction)
+    del C
+    up_ms, Cu = device_steps(lambda: ctx.upper(dA, dA), dev, stream, flush, args.steps)
+    del Cu
+    upper = method_entry(up_ms, products, alg_bytes, peak)
+
+    batched = served = stencil = None
     if not args.no_batch:
-        del C
+        stencil = stencil_section(ctx, dev, stream, flush, max(1, min(args.steps, 3)), peak)
         batched = batched_section(ctx, dev, stream, steps=max(1, min(args.steps, 3)))
         served = [served_section(dev, rate, args.serve_requests) for rate in (2000.0, 400.0, 150.0)]
     if rank != 0:
@@ -541,8 +596,11 @@ def run_ours(args):
         "clocks": clk.summary(),
         "gpu_launches": int(launches),
     }
+    line["upper"] = dict(upper, call="brm_upper_device (one call)")
     if cpu is not None:
         line["cpu_baseline"] = cpu
+    if stencil is not None:
+        line["stencil"] = stencil
     if batched is not None:
         line["batched"] = batched
     if served is not None:

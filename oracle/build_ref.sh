@@ -2,7 +2,8 @@
 # Builds the reference's BRMerge path unmodified from its own sources into
 # oracle/_ref/libbrm_ref.so (git-ignored).  Needs the reference tree; the
 # default location is /root/reference (override with BRM_REFERENCE_DIR).
-# Only spgemm.h (header-only kernels) and src/Timings.cpp are compiled; two
+# Only spgemm.h (header-only kernels), src/Timings.cpp and src/CSR.cpp (the
+# MatrixMarket reader) are compiled; two
 # small shims in oracle/ref_shim replace TBB malloc and the x86 TSC timer.
 set -euo pipefail
 HERE="$(cd "$(dirname "$0")" && pwd)"
@@ -14,6 +15,6 @@ fi
 mkdir -p "$HERE/_ref"
 g++ -O2 -fopenmp -std=c++17 -DTBB -ffp-contract=off -fPIC -shared \
     -include "$HERE/ref_shim/prelude.h" -I "$HERE/ref_shim" -I "$REF/inc" \
-    "$HERE/ref_wrap.cpp" "$REF/src/Timings.cpp" -o "$HERE/_ref/libbrm_ref.so.tmp"
+    "$HERE/ref_wrap.cpp" "$REF/src/Timings.cpp" "$REF/src/CSR.cpp" -o "$HERE/_ref/libbrm_ref.so.tmp"
 mv "$HERE/_ref/libbrm_ref.so.tmp" "$HERE/_ref/libbrm_ref.so"
 echo "built $HERE/_ref/libbrm_ref.so"
