@@ -308,6 +308,49 @@ def stencil_section(ctx, dev, stream, flush, steps: int, peak: float):
     return res
 
 
+def reader_section(ctx, A, steps: int):
+    """The workload's A written as a MatrixMarket file (real general, 17
+    significant digits) and read back by brm_read_mtx_device; the oracle's
+    reader (numpy restatement of CSR::construct) timed on the same file."""
+    import tempfile
+    import torch
+    import brmerge_gb300 as brm
+    rows = np.repeat(np.arange(A.M, dtype=np.int64), np.diff(A.rpt)) + 1
+    with tempfile.TemporaryDirectory() as td:
+        path = Path(td) / "a.mtx"
+        body = "\n".join(f"{r} {c} {v!r}" for r, c, v in
+                         zip(rows.tolist(), (A.col + 1).tolist(), A.val.tolist()))
+        path.write_text(f"%%MatrixMarket matrix coordinate real general\n{A.M} {A.N} {A.nnz}\n"
+                        f"{body}\n")
+        size = path.stat().st_size
+        ts, tms = [], []
+        X = None
+        for i in range(steps + 1):
+            tm = brm.MtxTiming()
+            t0 = time.perf_counter()
+            X = ctx.read_mtx_device(path, timing=tm)
+            torch.cuda.synchronize()
+            if i:
+                ts.append(time.perf_counter() - t0)
+                tms.append(tm)
+        ok = (X.nnz == A.nnz and np.array_equal(X.col.cpu().numpy(), A.col)
+              and np.array_equal(X.val.cpu().numpy().view(np.int64), A.val.view(np.int64)))
+        sec = statistics.mean(ts)
+        t0 = time.perf_counter()
+        from oracle import mtx as omtx
+        omtx.read(path)
+        cpu_s = time.perf_counter() - t0
+    return {
+        "file": "A as real general .mtx, %r values", "bytes": int(size), "entries": int(A.nnz),
+        "ms": round(sec * 1e3, 3), "mb_per_s": round(size / sec / 1e6, 1),
+        "phases_ms": {k: round(statistics.mean(getattr(t, k) for t in tms) * 1e3, 3)
+                      for k in ("read", "parse", "build")},
+        "matches_input": bool(ok),
+        "cpu_port_ms": round(cpu_s * 1e3, 1),
+        "cpu_port": "oracle/mtx.py (numpy restatement of CSR::construct), 1 core",
+    }
+
+
 def batched_section(ctx, dev, stream, steps: int):
     """The uneven batch through brm_batch_precise (one pipeline for every
     pair) against a loop of plain per-pair brm_precise_device calls."""
@@ -565,8 +608,9 @@ def run_ours(args):
     del Cu
     upper = method_entry(up_ms, products, alg_bytes, peak)
 
-    batched = served = stencil = None
+    batched = served = stencil = reader = None
     if not args.no_batch:
+        reader = reader_section(ctx, A, max(1, min(args.steps, 3)))
         stencil = stencil_section(ctx, dev, stream, flush, max(1, min(args.steps, 3)), peak)
         batched = batched_section(ctx, dev, stream, steps=max(1, min(args.steps, 3)))
         served = [served_section(dev, rate, args.serve_requests) for rate in (2000.0, 400.0, 150.0)]
@@ -601,6 +645,8 @@ def run_ours(args):
         line["cpu_baseline"] = cpu
     if stencil is not None:
         line["stencil"] = stencil
+    if reader is not None:
+        line["mtx_reader"] = reader
     if batched is not None:
         line["batched"] = batched
     if served is not None:

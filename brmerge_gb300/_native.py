@@ -61,6 +61,11 @@ class ServerResultC(C.Structure):
                 ("queued_s", C.c_double), ("latency_s", C.c_double), ("batch_size", C.c_int)]
 
 
+class MtxTimingC(C.Structure):
+    """Mirror of brm_mtx_timing."""
+    _fields_ = [(n, C.c_double) for n in ("read", "parse", "build", "total")]
+
+
 class HostCsrC(C.Structure):
     """Mirror of brm_host_csr (generator output)."""
     _fields_ = [("M", C.c_int), ("N", C.c_int), ("nnz", C.c_int),
@@ -139,6 +144,12 @@ def lib() -> C.CDLL:
         _decl(L.brm_upper_bound, C.c_int,
               [vp, C.c_int, csrp, csrp, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)])
         _decl(L.brm_validate, C.c_int, [vp, csrp, C.c_int, c_int_p])
+        _decl(L.brm_read_mtx_device, C.c_int,
+              [vp, C.c_int, C.c_char_p, c_int_p, c_int_p, c_int_p, ctxp, ctxp, ctxp,
+               C.POINTER(MtxTimingC)])
+        _decl(L.brm_read_mtx, C.c_int,
+              [C.c_char_p, C.c_int, c_int_p, c_int_p, c_int_p, ctxp, ctxp, ctxp,
+               C.POINTER(MtxTimingC)])
         _lib = L
     return _lib
 
@@ -161,6 +172,10 @@ def host() -> C.CDLL:
         _decl(H.brm_gen_lognormal, C.c_int, [C.c_int, C.c_int, C.c_double, C.c_double,
                                               C.c_int, C.c_ulonglong, hp])
         _decl(H.brm_gen_uniform, C.c_int, [C.c_int, C.c_int, C.c_int, C.c_ulonglong, hp])
+        _decl(H.brm_parse_int_token, C.c_int, [C.c_char_p, C.c_int, C.POINTER(C.c_longlong)])
+        _decl(H.brm_parse_real_token, C.c_int, [C.c_char_p, C.c_int, c_double_p])
+        _decl(H.brm_parse_real_tokens, None,
+              [C.c_void_p, C.c_void_p, C.c_void_p, C.c_longlong, C.c_void_p, C.c_void_p])
         _host = H
     return _host
 

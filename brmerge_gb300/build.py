@@ -32,8 +32,9 @@ CUDA_SOURCES = [
     "brm_hostpool.cu",
     "brm_batch.cu",
     "brm_server.cu",
+    "brm_mtx.cu",
 ]
-HOST_SOURCES = ["host/gen.cpp"]
+HOST_SOURCES = ["host/gen.cpp", "host/numparse.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -92,9 +93,10 @@ def build_host() -> Path:
     cxx = shutil.which("g++") or "g++"
     out = PKG / "libbrm_host.so"
     srcs = [CSRC / s for s in HOST_SOURCES]
-    if _newer(out, srcs + [INCLUDE / "brm_gen.h"]):
+    if _newer(out, srcs + [INCLUDE / "brm_gen.h", CSRC / "brm_numparse.h", CSRC / "brm_pow5.h"]):
         tmp = out.with_suffix(".so.tmp")
-        _run([cxx, "-O2", "-std=c++17", "-fPIC", "-shared", "-Wall", "-I", str(INCLUDE)]
+        _run([cxx, "-O2", "-std=c++17", "-fPIC", "-shared", "-Wall", "-ffp-contract=off",
+              "-I", str(INCLUDE), "-I", str(CSRC)]
              + [str(s) for s in srcs] + ["-o", str(tmp)])
         os.replace(tmp, out)
     return out

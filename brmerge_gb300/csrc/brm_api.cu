@@ -707,6 +707,10 @@ int brm::numeric_async(brm_context ctx, brm_dtype dtype, const brm_csr *A, const
 
 int brm::read_device_error(brm_context ctx) { return read_err(ctx); }
 
+std::mutex &brm::shared_context_mutex() { return g_mu; }
+
+int brm::shared_context(brm_context *out) { return default_ctx(out); }
+
 extern "C" {
 
 const char *brm_status_string(int status)
@@ -723,6 +727,8 @@ const char *brm_status_string(int status)
     case BRM_ERR_TIMEOUT: return "bounded device wait expired";
     case BRM_ERR_NO_DEVICE: return "no CUDA device";
     case BRM_ERR_CAPACITY: return "request exceeds a fixed capacity";
+    case BRM_ERR_FORMAT: return "malformed MatrixMarket file";
+    case BRM_ERR_IO: return "file cannot be opened or read";
     default: return "unknown status";
     }
 }

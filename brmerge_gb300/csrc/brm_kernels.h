@@ -1,6 +1,8 @@
 // brm_kernels.h -- host-side launchers of the BRMerge kernels (one GPU, one stream).
 #pragma once
 
+#include <mutex>
+
 #include <cuda_runtime.h>
 
 #include "brm_plan.h"
@@ -19,6 +21,11 @@ int context_num_sms(brm_context ctx);
 int numeric_async(brm_context ctx, brm_dtype dtype, const brm_csr *A, const brm_csr *B,
                   const int *crpt, int *ccol, void *cval);
 int read_device_error(brm_context ctx);
+
+// The process-wide context of the host drop-ins (created on first use) and
+// the mutex that serialises its users.
+std::mutex &shared_context_mutex();
+int shared_context(brm_context *out);
 
 // Counts one kernel launch of this library (brm_kernel_launches reports the
 // process-wide total); every launch site calls it right after <<<...>>>.

@@ -151,6 +151,32 @@ def brmerge_upper(A: CSR, B: CSR, C_out: CSR | None = None,
     return _host_call("brm_upper", "brm_upper_f32", A, B, C_out, timing, UpperTiming)
 
 
+class MtxTiming(_Timing):
+    """Phase times (seconds) of a MatrixMarket read (brm_mtx_timing)."""
+    _c = _native.MtxTimingC
+
+
+def read_mtx(path, dtype=np.float64, timing: MtxTiming | None = None) -> CSR:
+    """Reads a MatrixMarket coordinate file into a host CSR (brm_read_mtx;
+    the reference's CSR::construct, CSR.cpp:259-479), parsing it on the GPU.
+    Raises BrmError (BRM_ERR_FORMAT / BRM_ERR_IO) on a bad file."""
+    code = _dtype_code(dtype)
+    L = _native.lib()
+    M, N, n = C.c_int(), C.c_int(), C.c_int()
+    pr, pc, pv = C.c_void_p(), C.c_void_p(), C.c_void_p()
+    tc = _native.MtxTimingC()
+    _native.check(L.brm_read_mtx(str(path).encode(), code, C.byref(M), C.byref(N), C.byref(n),
+                                 C.byref(pr), C.byref(pc), C.byref(pv), C.byref(tc)),
+                  "brm_read_mtx")
+    vt = C.c_double if code == F64 else C.c_float
+    rpt = _owned(L, pr.value, M.value + 1, C.c_int, np.int32)
+    col = _owned(L, pc.value, n.value, C.c_int, np.int32)
+    val = _owned(L, pv.value, n.value, vt, np.float64 if code == F64 else np.float32)
+    if timing is not None:
+        timing._load(tc)
+    return CSR(M.value, N.value, rpt, col, val)
+
+
 # ---------------------------------------------------------------------------
 # device-resident form
 # ---------------------------------------------------------------------------
@@ -349,6 +375,25 @@ class Context:
             r0, r1, n0, n1 = int(roff[i]), int(roff[i + 1]), int(noff[i]), int(noff[i + 1])
             res.append(DeviceCSR(a.M, b.N, lrpt[r0 + i:r1 + i + 1], ccol[n0:n1], cval[n0:n1]))
         return res
+
+    def read_mtx_device(self, path, dtype=np.float64, timing: MtxTiming | None = None,
+                        device="cuda") -> DeviceCSR:
+        """brm_read_mtx_device: a MatrixMarket file straight into device CSR."""
+        code = _dtype_code(dtype)
+        M, N, n = C.c_int(), C.c_int(), C.c_int()
+        pr, pc, pv = C.c_void_p(), C.c_void_p(), C.c_void_p()
+        tc = _native.MtxTimingC()
+        _native.check(self._L.brm_read_mtx_device(self._h, code, str(path).encode(), C.byref(M),
+                                                  C.byref(N), C.byref(n), C.byref(pr),
+                                                  C.byref(pc), C.byref(pv), C.byref(tc)),
+                      "brm_read_mtx_device")
+        vt = "<f8" if code == F64 else "<f4"
+        rpt = _device_tensor(self._L, pr.value, M.value + 1, "<i4", device)
+        col = _device_tensor(self._L, pc.value, n.value, "<i4", device)
+        val = _device_tensor(self._L, pv.value, n.value, vt, device)
+        if timing is not None:
+            timing._load(tc)
+        return DeviceCSR(M.value, N.value, rpt, col, val)
 
     def upper(self, A: DeviceCSR, B: DeviceCSR, timing=None) -> DeviceCSR:
         """brm_upper_device: one call, callee-allocated outputs (no copy)."""

@@ -48,6 +48,15 @@ int brm_gen_lognormal(int M, int N, double mu, double sigma, int cap,
  * uniform random distinct columns in [0, N), values U[-1,1]. */
 int brm_gen_uniform(int M, int N, int max_per_row, unsigned long long seed, brm_host_csr *out);
 
+/* Host builds of the device MatrixMarket token parsers (brm_read_mtx*), for
+ * testing them without a GPU.  Status 0: converted (correctly rounded);
+ * 1: valid, but the device defers the value to an exact host conversion;
+ * -1: not a number of the reader's grammar. */
+int brm_parse_int_token(const char *s, int len, long long *out);
+int brm_parse_real_token(const char *s, int len, double *out);
+void brm_parse_real_tokens(const char *buf, const long long *off, const int *len, long long n,
+                           double *out, int *status);
+
 #ifdef __cplusplus
 }
 #endif

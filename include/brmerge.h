@@ -42,7 +42,9 @@ typedef enum brm_status {
     BRM_ERR_INTERNAL = 7,      /* a device-side invariant failed */
     BRM_ERR_TIMEOUT = 8,       /* a bounded device wait expired */
     BRM_ERR_NO_DEVICE = 9,     /* no CUDA device */
-    BRM_ERR_CAPACITY = 10      /* request larger than a fixed capacity */
+    BRM_ERR_CAPACITY = 10,     /* request larger than a fixed capacity */
+    BRM_ERR_FORMAT = 11,       /* malformed MatrixMarket file (brm_read_mtx*) */
+    BRM_ERR_IO = 12            /* a file cannot be opened or read */
 } brm_status;
 
 typedef enum brm_dtype { BRM_F64 = 0, BRM_F32 = 1 } brm_dtype;
@@ -292,6 +294,48 @@ int brm_server_release(brm_server srv, long long ticket);
 /* Finishes the queued requests, then frees everything (unreleased results
  * included). */
 int brm_server_destroy(brm_server srv);
+
+/* ---- MatrixMarket reader ------------------------------------------------------ */
+
+/* Phase times in seconds of a read: read = file to device (overlapped
+ * reads and host-to-device copies), parse = tokenising and number
+ * conversion on the device (plus the exact host conversion of the rare
+ * tokens the device defers), build = symmetric expansion, sort by (row,
+ * column) and row pointers, total = the whole call. */
+typedef struct brm_mtx_timing {
+    double read;
+    double parse;
+    double build;
+    double total;
+} brm_mtx_timing;
+
+/* Reads a MatrixMarket coordinate file into CSR with the semantics of the
+ * reference's CSR::construct (BRMerge-SpGEMM/src/CSR.cpp:259-479): banner
+ * "%%MatrixMarket matrix coordinate <real|integer|pattern|complex>
+ * <general|symmetric|skew-symmetric>", '%' comment lines, the size line
+ * "M N nnz" (nnz > 0), then nnz entries read as whitespace-separated tokens
+ * (line breaks do not matter; surplus tokens are ignored).  Indices become
+ * 0-based, symmetric entries are mirrored off the diagonal (negated for
+ * skew-symmetric), pattern values are 1, complex values keep their real
+ * part, rows are sorted by column; values are converted with correct
+ * rounding (f32 output: the double rounded to float).  Errors: BRM_ERR_IO,
+ * BRM_ERR_FORMAT (banner, size line, a token that is not a number, fewer
+ * entries than declared, an index out of range, a repeated (row, column),
+ * a value that overflows a double), BRM_ERR_OVERFLOW (more than INT_MAX
+ * entries after mirroring).  Where the reference reads out of bounds or
+ * moves an out-of-range column to another row, these return
+ * BRM_ERR_FORMAT.  The body is tokenised and converted on the device.
+ *
+ * Device form: *rpt (M+1), *col and *val (nnz) come from the context's
+ * stream-ordered pool; release each with brm_device_free.  timing may be
+ * NULL. */
+int brm_read_mtx_device(brm_context ctx, brm_dtype dtype, const char *path, int *M, int *N,
+                        int *nnz, int **rpt, int **col, void **val, brm_mtx_timing *timing);
+
+/* Host form (what CSR::construct fills): arrays from the page-locked host
+ * cache, released with brm_free; uses the process-wide context. */
+int brm_read_mtx(const char *path, brm_dtype dtype, int *M, int *N, int *nnz, int **rpt,
+                 int **col, void **val, brm_mtx_timing *timing);
 
 /* ---- helpers ---------------------------------------------------------------- */
 

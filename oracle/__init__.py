@@ -6,9 +6,11 @@ package brmerge_gb300 never imports it.
 
 * ``precise`` / ``upper``: the C restatement (brm_oracle.c, built here and on
   the GPU host by ``build()``), bit-for-bit pinned against the reference.
-* ``ref_precise`` / ``ref_upper``: the reference's own brmerge_precise /
-  brmerge_upper compiled from its sources by build_ref.sh into _ref/ when the
-  reference tree is present (not on the GPU host).
+* ``mtx``: the MatrixMarket reader (CSR::construct) restated with numpy.
+* ``ref_precise`` / ``ref_upper`` / ``ref_read_mtx``: the reference's own
+  brmerge_precise / brmerge_upper / MatrixMarket reader compiled from its
+  sources by build_ref.sh into _ref/ when the reference tree is present (not
+  on the GPU host).
 """
 from __future__ import annotations
 
@@ -86,8 +88,26 @@ def ref():
         R.ref_free_int.argtypes = [vp]
         R.ref_free_double.restype = None
         R.ref_free_double.argtypes = [vp]
+        ip = C.POINTER(C.c_int)
+        _sig(R.ref_read_mtx, [C.c_char_p, ip, ip, ip, pp, pp, pp, C.c_char_p, C.c_int])
         _ref = R
     return _ref
+
+
+def ref_read_mtx(path):
+    """The reference's own MatrixMarket reader (CSR::construct); returns the
+    CSR or raises ValueError with the reader's message.  Only for inputs the
+    reference reads without reaching an assert or undefined behaviour."""
+    R = ref()
+    M, N, nnz = C.c_int(), C.c_int(), C.c_int()
+    pr, pc, pv = C.c_void_p(), C.c_void_p(), C.c_void_p()
+    msg = C.create_string_buffer(256)
+    st = R.ref_read_mtx(str(path).encode(), C.byref(M), C.byref(N), C.byref(nnz), C.byref(pr),
+                        C.byref(pc), C.byref(pv), msg, 256)
+    if st != 0:
+        raise ValueError(msg.value.decode(errors="replace"))
+    return _unpack(M.value, N.value, pr, pc, pv, nnz.value, np.float64, R.ref_free_int,
+                   R.ref_free_double)
 
 
 def _arrays(A, B):

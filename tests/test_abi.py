@@ -40,7 +40,7 @@ def test_gen_exports_all_declared(built):
 def test_status_strings(built):
     from brmerge_gb300 import _native
     L = _native.lib()
-    for s in range(11):
+    for s in range(13):
         assert L.brm_status_string(s)
     assert L.brm_status_string(0) == b"success"
 
