@@ -305,6 +305,9 @@ def stencil_section(ctx, dev, stream, flush, steps: int, peak: float):
     ms, C = device_steps(lambda: ctx.upper(dS, dS), dev, stream, flush, steps)
     del C
     res["upper"] = method_entry(ms, products, alg, peak)
+    ms, C = device_steps(lambda: ctx.hash_device(dS, dS), dev, stream, flush, steps)
+    del C
+    res["hash_comparator"] = method_entry(ms, products, alg, peak)
     return res
 
 
@@ -607,6 +610,10 @@ def run_ours(args):
     up_ms, Cu = device_steps(lambda: ctx.upper(dA, dA), dev, stream, flush, args.steps)
     del Cu
     upper = method_entry(up_ms, products, alg_bytes, peak)
+    # the hash SpGEMM comparator: same structure, values in hardware order
+    h_ms, Ch = device_steps(lambda: ctx.hash_device(dA, dA), dev, stream, flush, args.steps)
+    del Ch
+    hashc = method_entry(h_ms, products, alg_bytes, peak)
 
     batched = served = stencil = reader = None
     if not args.no_batch:
@@ -641,6 +648,7 @@ def run_ours(args):
         "gpu_launches": int(launches),
     }
     line["upper"] = dict(upper, call="brm_upper_device (one call)")
+    line["hash_comparator"] = dict(hashc, call="brm_hash_device (values not in merge order)")
     if cpu is not None:
         line["cpu_baseline"] = cpu
     if stencil is not None:

@@ -144,6 +144,8 @@ def lib() -> C.CDLL:
         _decl(L.brm_upper_bound, C.c_int,
               [vp, C.c_int, csrp, csrp, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)])
         _decl(L.brm_validate, C.c_int, [vp, csrp, C.c_int, c_int_p])
+        _decl(L.brm_hash_device, C.c_int,
+              [vp, C.c_int, csrp, csrp, ctxp, ctxp, ctxp, c_int_p])
         _decl(L.brm_read_mtx_device, C.c_int,
               [vp, C.c_int, C.c_char_p, c_int_p, c_int_p, c_int_p, ctxp, ctxp, ctxp,
                C.POINTER(MtxTimingC)])

@@ -33,6 +33,7 @@ CUDA_SOURCES = [
     "brm_batch.cu",
     "brm_server.cu",
     "brm_mtx.cu",
+    "brm_hash.cu",
 ]
 HOST_SOURCES = ["host/gen.cpp", "host/numparse.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

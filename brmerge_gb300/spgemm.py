@@ -376,6 +376,24 @@ class Context:
             res.append(DeviceCSR(a.M, b.N, lrpt[r0 + i:r1 + i + 1], ccol[n0:n1], cval[n0:n1]))
         return res
 
+    def hash_device(self, A: DeviceCSR, B: DeviceCSR) -> DeviceCSR:
+        """brm_hash_device: the hash SpGEMM comparator (same structure as
+        Precise, values summed in hardware order)."""
+        import torch
+        code = _dtype_code(np.float64 if A.val.dtype == torch.float64 else np.float32)
+        pr, pc, pv = C.c_void_p(), C.c_void_p(), C.c_void_p()
+        cnnz = C.c_int(0)
+        a, b = A.c(), B.c()
+        _native.check(self._L.brm_hash_device(self._h, code, C.byref(a), C.byref(b), C.byref(pr),
+                                              C.byref(pc), C.byref(pv), C.byref(cnnz)),
+                      "brm_hash_device")
+        n = cnnz.value
+        dev = A.rpt.device
+        vt = "<f8" if A.val.dtype == torch.float64 else "<f4"
+        return DeviceCSR(A.M, B.N, _device_tensor(self._L, pr.value, A.M + 1, "<i4", dev),
+                         _device_tensor(self._L, pc.value, n, "<i4", dev),
+                         _device_tensor(self._L, pv.value, n, vt, dev))
+
     def read_mtx_device(self, path, dtype=np.float64, timing: MtxTiming | None = None,
                         device="cuda") -> DeviceCSR:
         """brm_read_mtx_device: a MatrixMarket file straight into device CSR."""

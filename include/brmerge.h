@@ -295,6 +295,19 @@ int brm_server_release(brm_server srv, long long ticket);
  * included). */
 int brm_server_destroy(brm_server srv);
 
+/* ---- hash SpGEMM comparator ----------------------------------------------------- */
+
+/* C = A*B by binned hash SpGEMM with sorted rows (Nagasaka et al., the
+ * comparator of the BRMerge paper: Existing-SpGEMM/inc/hash_mult.h:1028-1057,
+ * HashSpGEMM<sortOutput = true>).  The structure of C (crpt, ccol) is
+ * identical to brm_precise_device; the values are summed in an order the
+ * hardware picks, so they equal the merge-tree values only to rounding (the
+ * reference compares such results with |d| < 1e-9 or |d| < 1e-9 |v|,
+ * BRMerge-SpGEMM/src/CSR.cpp:214-253).  Outputs as brm_precise_device
+ * (release with brm_device_free). */
+int brm_hash_device(brm_context ctx, brm_dtype dtype, const brm_csr *A, const brm_csr *B,
+                    int **crpt, int **ccol, void **cval, int *cnnz);
+
 /* ---- MatrixMarket reader ------------------------------------------------------ */
 
 /* Phase times in seconds of a read: read = file to device (overlapped
