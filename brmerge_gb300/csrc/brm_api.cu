@@ -52,7 +52,7 @@ struct brm_context_s {
     int *d_bad = nullptr;
     brm::Counters *h_cnt = nullptr;  // pinned mirror of the device counters
     int *h_bad = nullptr;            // pinned
-    long long *h_mid = nullptr;      // pinned: entries of the mid-row scratch
+    long long *h_mid = nullptr;      // pinned: entries of the mid-row scratch (batched, warp)
     // per-A-entry list metadata (B-row start and length)
     DevBuf ameta;
     // heavy-row segments: descriptors + written list, the split table and the
@@ -152,6 +152,8 @@ size_t workspace_bytes(int M)
     b += a256(8 * (m + 1));                 // scan_flop
     b += a256(4 * m);                       // mid_flop
     b += a256(8 * (m + 1));                 // mid_pre
+    b += a256(4 * m);                       // mw_flop
+    b += a256(8 * (m + 1));                 // mw_pre
     b += a256(4 * (m + 1));                 // batch_start
     b += a256(8 * m);                       // seg_base
     b += a256(4 * m);                       // seg_n
@@ -195,6 +197,8 @@ int ensure_workspace(brm_context ctx, int M)
     P.scan_flop = (long long *)take(8 * (m + 1));
     P.mid_flop = (int *)take(4 * m);
     P.mid_pre = (long long *)take(8 * (m + 1));
+    P.mw_flop = (int *)take(4 * m);
+    P.mw_pre = (long long *)take(8 * (m + 1));
     P.batch_start = (int *)take(4 * (m + 1));
     P.seg_base = (unsigned long long *)take(8 * m);
     P.seg_n = (int *)take(4 * m);
@@ -314,12 +318,17 @@ int plan_phase(brm_context ctx, const brm_csr *A, const brm_csr *B, int *crpt, b
     // the segment descriptors of heavy rows are sized by the analysis
     BRM_CK(cudaGetLastError());
     BRM_CK(cudaMemcpyAsync(ctx->h_cnt, P.cnt, sizeof(brm::Counters), cudaMemcpyDeviceToHost, s));
-    if (fused)
+    if (fused) {
         BRM_CK(cudaMemcpyAsync(ctx->h_mid, P.mid_pre + A->M, sizeof(long long),
                                cudaMemcpyDeviceToHost, s));
+        BRM_CK(cudaMemcpyAsync(ctx->h_mid + 1, P.mw_pre + A->M, sizeof(long long),
+                               cudaMemcpyDeviceToHost, s));
+    }
     BRM_CK(cudaStreamSynchronize(s));
     if (fused) {
-        const size_t n = (size_t)(*ctx->h_mid > 0 ? *ctx->h_mid : 1);
+        // batched mid rows at mid_pre[row], warp mid rows after them
+        const long long tot = ctx->h_mid[0] + ctx->h_mid[1];
+        const size_t n = (size_t)(tot > 0 ? tot : 1);
         const size_t b_col = a256(4 * n);
         BRM_TRY(grow(ctx->midbuf, b_col + vsize((brm_dtype)fused_dtype) * n));
         ctx->mid_col = (int *)ctx->midbuf.p;
@@ -752,7 +761,7 @@ int brm_create(brm_context *out)
     if (e == cudaSuccess)
         e = cudaMallocHost(&ctx->h_bad, sizeof(int));
     if (e == cudaSuccess)
-        e = cudaMallocHost(&ctx->h_mid, sizeof(long long));
+        e = cudaMallocHost(&ctx->h_mid, 2 * sizeof(long long));
     for (int i = 0; i < kNumEvents && e == cudaSuccess; i++)
         e = cudaEventCreate(&ctx->ev[i]);
     for (int i = 0; i < brm::kMaxParts && e == cudaSuccess; i++)

@@ -608,9 +608,10 @@ __global__ void __launch_bounds__(256) k_batch_starts(PlanDev P, int M)
         P.cnt->n_batch = (int)((hi + W - 1) / W);
 }
 
-// Moves the mid rows written by k_mid_numeric<..., SCRATCH> from the
-// scratch (row at P.mid_pre[row], P.nnz[row] entries) to C at crpt[row].
-// One warp per row; rows that are not mid rows are skipped.
+// Moves the mid rows written by k_mid_numeric<..., SCRATCH> (row at
+// P.mid_pre[row]) and k_mid_warp<..., kMwScratch> (row at P.mid_pre[M] +
+// P.mw_pre[row]), P.nnz[row] entries each, from the scratch to C at
+// crpt[row].  One warp per row; rows that are not mid rows are skipped.
 template <typename T>
 __global__ void __launch_bounds__(256) k_mid_compact(PlanDev P, int M, const int *__restrict__ scol,
                                                      const T *__restrict__ sval, const int *crpt,
@@ -621,9 +622,13 @@ __global__ void __launch_bounds__(256) k_mid_compact(PlanDev P, int M, const int
     const int r1 = min(M, P.r_hi);
     for (int row = P.r_lo + ((blockIdx.x * blockDim.x + threadIdx.x) >> 5); row < r1;
          row += nwarps) {
-        if (P.mid_flop[row] == 0)
+        long long src;
+        if (P.mid_flop[row] != 0)
+            src = P.mid_pre[row];
+        else if (P.mw_flop[row] != 0)
+            src = P.mid_pre[M] + P.mw_pre[row];
+        else
             continue;
-        const long long src = P.mid_pre[row];
         const long long dst = crpt[row];
         const int n = P.nnz[row];
         for (int i = lane; i < n; i += 32) {

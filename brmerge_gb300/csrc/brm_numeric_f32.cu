@@ -1,6 +1,7 @@
 // brm_numeric_f32.cu -- numeric phase launchers for float values.
 #include "brm_kernels.h"
 #include "brm_mid.cuh"
+#include "brm_midwarp.cuh"
 #include "brm_seg.cuh"
 #include "brm_rows.cuh"
 
@@ -21,6 +22,8 @@ static void numeric_f32(const CsrDev &A, const CsrDev &B, const PlanDev &P, cons
                                                           crpt, ccol, cval);
         count_launch();
     } else {
+        launch_mid_warp<float, UPPER ? kMwUpper : kMwPrecise>(A, B, P, crpt, ccol, cval, num_sms,
+                                                          s);
         const size_t msm = MidNumLayout<float>::bytes;
         cudaFuncSetAttribute(k_mid_numeric<float, UPPER>,
                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)msm);
@@ -75,6 +78,7 @@ void launch_mid_scratch_f32(const CsrDev &A, const CsrDev &B, const PlanDev &P, 
     k_mid_numeric<float, false, true><<<num_sms * 2, kMidThreads, msm, s>>>(
         A, B, P, nullptr, mid_col, (float *)mid_val);
     count_launch();
+    launch_mid_warp<float, kMwScratch>(A, B, P, nullptr, mid_col, (float *)mid_val, num_sms, s);
 }
 
 }  // namespace brm

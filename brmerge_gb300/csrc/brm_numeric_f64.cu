@@ -1,6 +1,7 @@
 // brm_numeric_f64.cu -- numeric phase launchers for double values.
 #include "brm_kernels.h"
 #include "brm_mid.cuh"
+#include "brm_midwarp.cuh"
 #include "brm_seg.cuh"
 #include "brm_rows.cuh"
 
@@ -21,6 +22,8 @@ static void numeric_f64(const CsrDev &A, const CsrDev &B, const PlanDev &P, cons
                                                           crpt, ccol, cval);
         count_launch();
     } else {
+        launch_mid_warp<double, UPPER ? kMwUpper : kMwPrecise>(A, B, P, crpt, ccol, cval, num_sms,
+                                                          s);
         const size_t msm = MidNumLayout<double>::bytes;
         cudaFuncSetAttribute(k_mid_numeric<double, UPPER>,
                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)msm);
@@ -75,6 +78,7 @@ void launch_mid_scratch_f64(const CsrDev &A, const CsrDev &B, const PlanDev &P, 
     k_mid_numeric<double, false, true><<<num_sms * 2, kMidThreads, msm, s>>>(
         A, B, P, nullptr, mid_col, (double *)mid_val);
     count_launch();
+    launch_mid_warp<double, kMwScratch>(A, B, P, nullptr, mid_col, (double *)mid_val, num_sms, s);
 }
 
 }  // namespace brm

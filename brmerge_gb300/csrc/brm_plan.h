@@ -33,6 +33,12 @@ constexpr int kMidMaxLists = kMidCap / 2;
 constexpr int kMidMaxK = 255;
 constexpr int kMidMaxRows = kMidCap / (kWarpMaxFlop + 1) + 2;
 
+// Warp mid rows: more than kWarpMaxFlop and at most kMwF products, at most
+// kMidMaxK A entries, columns within a range below 2^kMwRangeBits; one warp
+// each (they take precedence over the batched mid rows).
+constexpr int kMwF = 768;
+constexpr int kMwRangeBits = 22;
+
 // Segmented heavy rows: a row that is not a mid row is cut, at 32-column word
 // (or, inside very dense words, column) boundaries, into column segments of at
 // most kSegCap products within one planning chunk of kPlanBits columns.  The
@@ -68,7 +74,8 @@ enum RowBin : int {
     kBinHeavy = 3,  // row CTA, scheduled first
     kBinMid = 4,    // row CTA
     kBinBatch = 5,  // batched mid-row kernels (no row list: row-order batches)
-    kNumBins = 6,
+    kBinMidWarp = 6,  // one warp per row (brm_midwarp.cuh)
+    kNumBins = 7,
 };
 
 // Device counters (one struct in device memory, zeroed per phase).
@@ -155,6 +162,8 @@ struct PlanDev {
     int *alen;             // [nnz(A)] length of B row acol[j] (0 if acol[j] is out of range)
     int *mid_flop;         // [M] products of batched mid rows, 0 for other rows
     long long *mid_pre;    // [M+1] exclusive scan of mid_flop
+    int *mw_flop;          // [M] products of warp mid rows, 0 for other rows
+    long long *mw_pre;     // [M+1] exclusive scan of mw_flop (one-call scratch after mid_pre[M])
     int *batch_start;      // [M+1] first row of each mid batch
     unsigned long long *seg_base;  // [M] first descriptor slot of each heavy row
     int *seg_n;            // [M] segments of each heavy row (0: not segmented)

@@ -1,6 +1,7 @@
 // brm_symbolic.cu -- symbolic phase launchers (exact row nnz, spill routing).
 #include "brm_kernels.h"
 #include "brm_mid.cuh"
+#include "brm_midwarp.cuh"
 #include "brm_rows.cuh"
 #include "brm_seg.cuh"
 
@@ -11,6 +12,7 @@ void launch_batches(const PlanDev &P, int M, void *tmp, cudaStream_t s)
     if (M <= 0)
         return;
     launch_scan_i64(P.mid_flop, P.mid_pre, M, tmp, s);
+    launch_scan_i64(P.mw_flop, P.mw_pre, M, tmp, s);
     k_batch_starts<0><<<(M + 1 + 255) / 256, 256, 0, s>>>(P, M);
     count_launch();
 }
@@ -29,6 +31,7 @@ void launch_symbolic(const CsrDev &A, const CsrDev &B, const PlanDev &P, int num
                                  (int)msm);
             k_mid_symbolic<0><<<num_sms * 2, kMidThreads, msm, s>>>(A, B, P);
             count_launch();
+            launch_mid_warp<double, kMwSymbolic>(A, B, P, nullptr, nullptr, nullptr, num_sms, s);
         }
     }
     // heavy rows: exact nnz and segment plan (both Precise and Upper)
