@@ -1,4 +1,4 @@
-// brm_midwarp.cuh -- one warp per mid row: radix-ordered products, no block barriers.
+// brm_midwarp.cuh -- one warp per mid row: merged product keys, no block barriers.
 //
 // Rows with at most kMwF products (and at most kMidMaxK A entries, column
 // range below 2^kMwRangeBits) are the bulk of regular products (a 27-point
@@ -9,9 +9,9 @@
 //   2. every product as a 32-bit key ((column - cmin) << 10 | product index)
 //      in list-major order, i.e. leaf order (BRMerge-SpGEMM/inc/spgemm.h:
 //      618-624: list l holds the l-th A entry's scaled B row);
-//   3. a stable LSD radix sort of the keys on the column bits (at most 9
-//      bits a pass; a warp ranks equal digits in lane order from one ballot
-//      per digit bit, so equal columns keep leaf order);
+//   3. a bottom-up merge of the sorted lists by key, ceil(log2 lists)
+//      levels (merge path: every lane a contiguous share of the output), so
+//      equal columns end in leaf order;
 //   4. the runs of one column are listed and lane i reduces runs i, i + 32,
 //      ... with the merge-tree rule (adjacent leaves join at their split
 //      level: closed forms up to four leaves, a register shift-reduce beyond,
@@ -31,23 +31,19 @@ namespace brm {
 
 enum MidWarpMode : int { kMwSymbolic = 0, kMwPrecise = 1, kMwUpper = 2, kMwScratch = 3 };
 
-constexpr int kMwWarps = 8;
+constexpr int kMwWarps = 12;
 constexpr int kMwThreads = kMwWarps * 32;
 constexpr int kMwIdxBits = 10;  // product index in the key (kMwF <= 1024)
-constexpr int kMwDigit = 9;     // radix digit width at most
-constexpr int kMwBins = 1 << kMwDigit;
 static_assert(kMwF <= (1 << kMwIdxBits), "product index must fit the key");
 static_assert(kMwRangeBits + kMwIdxBits <= 32, "keys are 32-bit");
 
 struct MidWarpLayout {
-    // keys (sorted in place between k0 and k1; the free one then lists the
-    // runs, up to kMwF + 1 entries)
+    // keys, merged back and forth between k0 and k1; the free one then lists
+    // the runs (up to kMwF + 1 entries)
     static constexpr size_t o_k0 = 0;
     static constexpr size_t o_k1 = o_k0 + mid_a16((kMwF + 1) * 4);
-    static constexpr size_t o_addr = o_k1 + mid_a16((kMwF + 1) * 4);   // B position per product
-    static constexpr size_t o_leaf = o_addr + kMwF * 4;                // leaf per product
-    static constexpr size_t o_hist = o_leaf + mid_a16(kMwF);           // digit counts
-    static constexpr size_t o_loff = o_hist + kMwBins * 4;             // list product offsets
+    static constexpr size_t o_plist = o_k1 + mid_a16((kMwF + 1) * 4);  // list of each product
+    static constexpr size_t o_loff = o_plist + mid_a16(kMwF);           // list product offsets
     static constexpr size_t o_lbs = o_loff + mid_a16((kMidMaxK + 2) * 2);
     static constexpr size_t o_lleaf = o_lbs + (kMidMaxK + 1) * 4;
     static constexpr size_t per_warp = mid_a16(o_lleaf + kMidMaxK + 1);
@@ -74,6 +70,63 @@ __device__ __forceinline__ T mw_run_value(int n, const GetLeaf &leaf, const GetV
     return sr.finish();
 }
 
+// One level of the warp's bottom-up merge: runs of 2^L consecutive lists;
+// runs 2m and 2m+1 merge into dst, a run without a right neighbour is
+// copied.  The lane writes output positions [p0, p1).  Keys are unique
+// (they hold the product index), so the merge is a plain merge of keys.
+__device__ __forceinline__ void mw_merge_level(int L, const unsigned *__restrict__ src,
+                                               unsigned *__restrict__ dst,
+                                               const unsigned short *loff, int nl, int p0, int p1)
+{
+    if (p0 >= p1)
+        return;
+    int lo = 0, hi = nl - 1;  // list holding position p0
+    while (lo < hi) {
+        const int m = (lo + hi + 1) >> 1;
+        if (loff[m] <= p0)
+            lo = m;
+        else
+            hi = m - 1;
+    }
+    int j = lo;
+    int p = p0;
+    while (p < p1) {
+        const int pg = (j >> L) & ~1;
+        const int l0 = pg << L;
+        const int l1 = min((pg + 1) << L, nl);
+        const int l2 = min((pg + 2) << L, nl);
+        const int ls = loff[l0], le = loff[l1], re = loff[l2];
+        const int stop = min(p1, re);
+        if (le == re) {
+            for (; p < stop; p++)
+                dst[p] = src[p];
+        } else {
+            const int na = le - ls, nb = re - le, d = p - ls;
+            int a = max(0, d - nb), b = min(d, na);
+            while (a < b) {
+                const int m = (a + b) >> 1;
+                if (src[ls + m] < src[le + d - 1 - m])
+                    a = m + 1;
+                else
+                    b = m;
+            }
+            int ia = a, ib = d - a;
+            unsigned ka = ia < na ? src[ls + ia] : 0xffffffffu;
+            unsigned kb = ib < nb ? src[le + ib] : 0xffffffffu;
+            for (; p < stop; p++) {
+                if (ka < kb) {
+                    dst[p] = ka;
+                    ka = ++ia < na ? src[ls + ia] : 0xffffffffu;
+                } else {
+                    dst[p] = kb;
+                    kb = ++ib < nb ? src[le + ib] : 0xffffffffu;
+                }
+            }
+        }
+        j = l2;
+    }
+}
+
 template <typename T, int MODE>
 __global__ void __launch_bounds__(kMwThreads) k_mid_warp(CsrDev A, CsrDev B, PlanDev P,
                                                          const int *crpt, int *ccol, T *cval)
@@ -83,9 +136,7 @@ __global__ void __launch_bounds__(kMwThreads) k_mid_warp(CsrDev A, CsrDev B, Pla
     unsigned char *ws = smem + (size_t)wid * MidWarpLayout::per_warp;
     unsigned *k0 = (unsigned *)(ws + MidWarpLayout::o_k0);
     unsigned *k1 = (unsigned *)(ws + MidWarpLayout::o_k1);
-    int *paddr = (int *)(ws + MidWarpLayout::o_addr);
-    unsigned char *pleaf = ws + MidWarpLayout::o_leaf;
-    int *hist = (int *)(ws + MidWarpLayout::o_hist);
+    unsigned char *plist = ws + MidWarpLayout::o_plist;
     unsigned short *loff = (unsigned short *)(ws + MidWarpLayout::o_loff);
     int *lbs = (int *)(ws + MidWarpLayout::o_lbs);
     unsigned char *lleaf = ws + MidWarpLayout::o_lleaf;
@@ -132,7 +183,7 @@ __global__ void __launch_bounds__(kMwThreads) k_mid_warp(CsrDev A, CsrDev B, Pla
         if (lane == 0)
             loff[nl] = (unsigned short)F;
         __syncwarp();
-        // 2. keys in list-major (leaf) order
+        // 2. keys in list-major (leaf) order: each list is sorted by key
         {
             int lo = 0, hi = nl - 1;  // list of product `lane`
             while (lo < hi) {
@@ -146,73 +197,20 @@ __global__ void __launch_bounds__(kMwThreads) k_mid_warp(CsrDev A, CsrDev B, Pla
             for (int e = lane; e < F; e += 32) {
                 while (e >= loff[j + 1])
                     j++;
-                const int addr = lbs[j] + (e - loff[j]);
-                const int c = bcol[addr];
+                const int c = bcol[lbs[j] + (e - loff[j])];
                 k0[e] = ((unsigned)(c - cmin) << kMwIdxBits) | (unsigned)e;
-                paddr[e] = addr;
-                pleaf[e] = lleaf[j];
+                plist[e] = (unsigned char)j;
             }
         }
         __syncwarp();
-        // 3. stable radix sort on the column bits
-        const int rb = cr.y > cmin ? 32 - __clz(cr.y - cmin) : 0;
+        // 3. bottom-up merge of the sorted lists (ceil(log2 nl) levels)
         unsigned *src = k0, *dst = k1;
-        if (rb > 0) {
-            const int passes = (rb + kMwDigit - 1) / kMwDigit;
-            const int width = (rb + passes - 1) / passes;
-            const unsigned dmask = (1u << width) - 1u;
-            const int nbins = 1 << width;
-            for (int ps = 0; ps < passes; ps++) {
-                const int shift = kMwIdxBits + ps * width;
-                for (int b = lane; b < nbins; b += 32)
-                    hist[b] = 0;
-                __syncwarp();
-                for (int e = lane; e < F; e += 32)
-                    atomicAdd(&hist[(src[e] >> shift) & dmask], 1);
-                __syncwarp();
-                {
-                    // exclusive scan of the counts: lane owns bins [lane*per, +per)
-                    const int per = nbins >> 5 > 0 ? nbins >> 5 : 1;
-                    int s = 0;
-                    for (int q = 0; q < per; q++) {
-                        const int b = lane * per + q;
-                        if (b < nbins)
-                            s += hist[b];
-                    }
-                    int run = warp_incl_scan(s) - s;
-                    for (int q = 0; q < per; q++) {
-                        const int b = lane * per + q;
-                        if (b < nbins) {
-                            const int c = hist[b];
-                            hist[b] = run;
-                            run += c;
-                        }
-                    }
-                }
-                __syncwarp();
-                for (int eb = 0; eb < F; eb += 32) {
-                    const int e = eb + lane;
-                    const bool ok = e < F;
-                    const unsigned key = ok ? src[e] : 0u;
-                    const int d = ok ? (int)((key >> shift) & dmask) : 0;
-                    // lanes with the same digit: one ballot per digit bit
-                    // (several times the throughput of __match_any_sync here)
-                    unsigned peers = __ballot_sync(kFull, ok);
-                    for (int b = 0; b < width; b++) {
-                        const bool bit = (d >> b) & 1;
-                        const unsigned m = __ballot_sync(kFull, bit);
-                        peers &= bit ? m : ~m;
-                    }
-                    int pos = 0;
-                    if (ok)
-                        pos = hist[d] + __popc(peers & lt);
-                    __syncwarp();
-                    if (ok && (peers >> lane) == 1u)  // last lane of its digit group
-                        hist[d] += __popc(peers);
-                    __syncwarp();
-                    if (ok)
-                        dst[pos] = key;
-                }
+        {
+            const int per = (F + 31) >> 5;
+            const int p0 = min(lane * per, F), p1 = min(p0 + per, F);
+            const int levels = 32 - __clz(nl - 1);  // nl >= 2
+            for (int L = 0; L < levels; L++) {
+                mw_merge_level(L, src, dst, loff, nl, p0, p1);
                 __syncwarp();
                 unsigned *x = src;
                 src = dst;
@@ -258,10 +256,11 @@ __global__ void __launch_bounds__(kMwThreads) k_mid_warp(CsrDev A, CsrDev B, Pla
         for (int h = lane; h < len; h += 32) {
             const int p = (int)dst[h], m = (int)dst[h + 1] - p;
             const unsigned *run = src + p;
-            auto leaf = [&](int i) { return (int)pleaf[run[i] & imask]; };
+            auto leaf = [&](int i) { return (int)lleaf[plist[run[i] & imask]]; };
             auto val = [&](int i) {
                 const int e = (int)(run[i] & imask);
-                return vmul(arow[pleaf[e]], bval[paddr[e]]);
+                const int j = plist[e];
+                return vmul(arow[lleaf[j]], bval[lbs[j] + (e - loff[j])]);
             };
             // leaves below 32 need at most 5 stack entries below the top
             const T v = k <= 32 ? mw_run_value<T, 6>(m, leaf, val) : mw_run_value<T, 9>(m, leaf, val);
