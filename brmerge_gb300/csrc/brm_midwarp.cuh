@@ -1,9 +1,10 @@
-// brm_midwarp.cuh -- one warp per mid row: merged product keys, no block barriers.
+// brm_midwarp.cuh -- one warp (or four) per mid row: merged product keys, no block barriers.
 //
-// Rows with at most kMwF products (and at most kMidMaxK A entries, column
-// range below 2^kMwRangeBits) are the bulk of regular products (a 27-point
-// stencil squared: 729 products, 27 lists, 125 outputs per row) and of small
-// uneven batches.  A warp takes a row at a time:
+// Rows with at most kMgF products (and at most kMidMaxK A entries, a column
+// range below 2^kMwRangeBits / 2^kMgRangeBits) are the bulk of regular
+// products (a 27-point stencil squared: 729 products, 27 lists, 125 outputs
+// per row) and of uneven batches.  A warp (rows up to kMwF products) or a
+// group of four warps takes a row at a time:
 //
 //   1. its nonempty lists (leaf order) into a warp-private table;
 //   2. every product as a 32-bit key ((column - cmin) << 10 | product index)
@@ -31,24 +32,83 @@ namespace brm {
 
 enum MidWarpMode : int { kMwSymbolic = 0, kMwPrecise = 1, kMwUpper = 2, kMwScratch = 3 };
 
-constexpr int kMwWarps = 12;
-constexpr int kMwThreads = kMwWarps * 32;
-constexpr int kMwIdxBits = 10;  // product index in the key (kMwF <= 1024)
-static_assert(kMwF <= (1 << kMwIdxBits), "product index must fit the key");
-static_assert(kMwRangeBits + kMwIdxBits <= 32, "keys are 32-bit");
+// A group of G warps works on one row at a time: G = 1 for rows of at most
+// kMwF products, G = 4 (named barriers) up to kMgF.  Keys are (column -
+// cmin) << IDX | product index.
+template <int G>
+struct MwShape;
+template <>
+struct MwShape<1> {
+    static constexpr int F = kMwF;
+    static constexpr int IDX = 10;
+    static constexpr int RANGE = kMwRangeBits;
+    static constexpr int GROUPS = 12;
+    static constexpr int BIN = kBinMidWarp;
+};
+template <>
+struct MwShape<4> {
+    static constexpr int F = kMgF;
+    static constexpr int IDX = 12;
+    static constexpr int RANGE = kMgRangeBits;
+    static constexpr int GROUPS = 3;
+    static constexpr int BIN = kBinMidGroup;
+};
+constexpr int kMwThreads = 384;  // both shapes: 12 x 1 and 3 x 4 warps
+static_assert(MwShape<1>::F <= (1 << MwShape<1>::IDX) && MwShape<1>::RANGE + MwShape<1>::IDX <= 32,
+              "warp keys are 32-bit");
+static_assert(MwShape<4>::F <= (1 << MwShape<4>::IDX) && MwShape<4>::RANGE + MwShape<4>::IDX <= 32,
+              "group keys are 32-bit");
 
+template <int G>
 struct MidWarpLayout {
+    static constexpr int FM = MwShape<G>::F;
     // keys, merged back and forth between k0 and k1; the free one then lists
-    // the runs (up to kMwF + 1 entries)
+    // the runs (up to FM + 1 entries)
     static constexpr size_t o_k0 = 0;
-    static constexpr size_t o_k1 = o_k0 + mid_a16((kMwF + 1) * 4);
-    static constexpr size_t o_plist = o_k1 + mid_a16((kMwF + 1) * 4);  // list of each product
-    static constexpr size_t o_loff = o_plist + mid_a16(kMwF);           // list product offsets
+    static constexpr size_t o_k1 = o_k0 + mid_a16((FM + 1) * 4);
+    static constexpr size_t o_plist = o_k1 + mid_a16((FM + 1) * 4);  // list of each product
+    static constexpr size_t o_loff = o_plist + mid_a16(FM);           // list product offsets
     static constexpr size_t o_lbs = o_loff + mid_a16((kMidMaxK + 2) * 2);
     static constexpr size_t o_lleaf = o_lbs + (kMidMaxK + 1) * 4;
-    static constexpr size_t per_warp = mid_a16(o_lleaf + kMidMaxK + 1);
-    static constexpr size_t bytes = per_warp * kMwWarps;
+    static constexpr size_t o_gs = o_lleaf + mid_a16(kMidMaxK + 1);    // group scan scratch
+    static constexpr size_t per_group = mid_a16(o_gs + 4 * (G + 1));
+    static constexpr size_t bytes = per_group * MwShape<G>::GROUPS;
 };
+
+template <int G>
+__device__ __forceinline__ void grp_sync(int gid)
+{
+    if (G == 1)
+        __syncwarp();
+    else
+        asm volatile("bar.sync %0, %1;" ::"r"(gid + 1), "r"(G * 32) : "memory");
+}
+
+// Exclusive scan of one int per thread of the group; *total gets the sum.
+template <int G>
+__device__ __forceinline__ int grp_excl_scan(int v, int *gs, int gid, int *total)
+{
+    const int lane = threadIdx.x & 31;
+    const int inc = warp_incl_scan(v);
+    if (G == 1) {
+        *total = __shfl_sync(kFull, inc, 31);
+        return inc - v;
+    }
+    const int w = (threadIdx.x >> 5) % G;
+    grp_sync<G>(gid);  // gs may still be read by a previous scan
+    if (lane == 31)
+        gs[w] = inc;
+    grp_sync<G>(gid);
+    int off = 0, tot = 0;
+#pragma unroll
+    for (int i = 0; i < G; i++) {
+        const int x = gs[i];
+        off += i < w ? x : 0;
+        tot += x;
+    }
+    *total = tot;
+    return off + inc - v;
+}
 
 // Merge-tree value of a run of n >= 1 products in leaf order (leaves below
 // 2^(D-1)).
@@ -70,9 +130,9 @@ __device__ __forceinline__ T mw_run_value(int n, const GetLeaf &leaf, const GetV
     return sr.finish();
 }
 
-// One level of the warp's bottom-up merge: runs of 2^L consecutive lists;
+// One level of the group's bottom-up merge: runs of 2^L consecutive lists;
 // runs 2m and 2m+1 merge into dst, a run without a right neighbour is
-// copied.  The lane writes output positions [p0, p1).  Keys are unique
+// copied.  The thread writes output positions [p0, p1).  Keys are unique
 // (they hold the product index), so the merge is a plain merge of keys.
 __device__ __forceinline__ void mw_merge_level(int L, const unsigned *__restrict__ src,
                                                unsigned *__restrict__ dst,
@@ -127,29 +187,33 @@ __device__ __forceinline__ void mw_merge_level(int L, const unsigned *__restrict
     }
 }
 
-template <typename T, int MODE>
+template <typename T, int MODE, int G>
 __global__ void __launch_bounds__(kMwThreads) k_mid_warp(CsrDev A, CsrDev B, PlanDev P,
                                                          const int *crpt, int *ccol, T *cval)
 {
+    using S = MwShape<G>;
+    using L = MidWarpLayout<G>;
+    constexpr int NT = 32 * G;
+    constexpr int IDX = S::IDX;
     extern __shared__ __align__(16) unsigned char smem[];
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    unsigned char *ws = smem + (size_t)wid * MidWarpLayout::per_warp;
-    unsigned *k0 = (unsigned *)(ws + MidWarpLayout::o_k0);
-    unsigned *k1 = (unsigned *)(ws + MidWarpLayout::o_k1);
-    unsigned char *plist = ws + MidWarpLayout::o_plist;
-    unsigned short *loff = (unsigned short *)(ws + MidWarpLayout::o_loff);
-    int *lbs = (int *)(ws + MidWarpLayout::o_lbs);
-    unsigned char *lleaf = ws + MidWarpLayout::o_lleaf;
-    const unsigned lt = lanemask_lt();
+    const int gid = threadIdx.x / NT, t = threadIdx.x % NT;
+    unsigned char *ws = smem + (size_t)gid * L::per_group;
+    unsigned *k0 = (unsigned *)(ws + L::o_k0);
+    unsigned *k1 = (unsigned *)(ws + L::o_k1);
+    unsigned char *plist = ws + L::o_plist;
+    unsigned short *loff = (unsigned short *)(ws + L::o_loff);
+    int *lbs = (int *)(ws + L::o_lbs);
+    unsigned char *lleaf = ws + L::o_lleaf;
+    int *gs = (int *)(ws + L::o_gs);
     const int M = A.M;
-    const int n = P.cnt->bin_count[kBinMidWarp];
-    const int *rows = P.rows + (size_t)kBinMidWarp * M;
+    const int n = P.cnt->bin_count[S::BIN];
+    const int *rows = P.rows + (size_t)S::BIN * M;
     const int *__restrict__ bcol = B.col;
     const T *__restrict__ bval = (const T *)B.val;
     const T *__restrict__ aval = (const T *)A.val;
-    const int gw = (blockIdx.x * kMwThreads + threadIdx.x) >> 5;
-    const int nw = (gridDim.x * kMwThreads) >> 5;
-    for (int it = gw; it < n; it += nw) {
+    const int g0 = blockIdx.x * S::GROUPS + gid;
+    const int ng = gridDim.x * S::GROUPS;
+    for (int it = g0; it < n; it += ng) {
         const int row = rows[it];
         if (row < P.r_lo || row >= P.r_hi)
             continue;
@@ -157,103 +221,101 @@ __global__ void __launch_bounds__(kMwThreads) k_mid_warp(CsrDev A, CsrDev B, Pla
         const int k = A.rpt[row + 1] - a0;
         const int2 cr = P.crange[row];
         const int cmin = cr.x;
-        // 1. nonempty lists in leaf order
+        // 1. nonempty lists in leaf order (count << 16 | products, scanned)
         int nl = 0, F = 0;
-        for (int jb = 0; jb < k; jb += 32) {
-            const int j = jb + lane;
+        for (int jb = 0; jb < k; jb += NT) {
+            const int j = jb + t;
             const int len = j < k ? P.alen[a0 + j] : 0;
-            const bool ne = len > 0;
-            const unsigned nem = __ballot_sync(kFull, ne);
-            const int inc = warp_incl_scan(len);
-            const int tot = __shfl_sync(kFull, inc, 31);
-            if (ne) {
-                const int li = nl + __popc(nem & lt);
-                loff[li] = (unsigned short)(F + inc - len);
+            const int x = len > 0 ? (1 << 16) + len : 0;
+            int tot;
+            const int ex = grp_excl_scan<G>(x, gs, gid, &tot);
+            if (len > 0) {
+                const int li = nl + (ex >> 16);
+                loff[li] = (unsigned short)(F + (ex & 0xffff));
                 lbs[li] = P.abs[a0 + j];
                 lleaf[li] = (unsigned char)j;
             }
-            nl += __popc(nem);
-            F += tot;
+            nl += tot >> 16;
+            F += tot & 0xffff;
         }
-        if (F > kMwF || cr.y - cmin >= (1 << kMwRangeBits)) {  // the analysis bins prevent this
-            if (lane == 0)
+        if (F > S::F || cr.y - cmin >= (1 << S::RANGE)) {  // the analysis bins prevent this
+            if (t == 0)
                 atomicOr(&P.cnt->err, kErrWindowOverflow);
+            grp_sync<G>(gid);
             continue;
         }
-        if (lane == 0)
+        if (t == 0)
             loff[nl] = (unsigned short)F;
-        __syncwarp();
+        grp_sync<G>(gid);
         // 2. keys in list-major (leaf) order: each list is sorted by key
         {
-            int lo = 0, hi = nl - 1;  // list of product `lane`
+            int lo = 0, hi = nl - 1;  // list of product t
             while (lo < hi) {
                 const int m = (lo + hi + 1) >> 1;
-                if (loff[m] <= lane)
+                if (loff[m] <= t)
                     lo = m;
                 else
                     hi = m - 1;
             }
             int j = lo;
-            for (int e = lane; e < F; e += 32) {
+            for (int e = t; e < F; e += NT) {
                 while (e >= loff[j + 1])
                     j++;
                 const int c = bcol[lbs[j] + (e - loff[j])];
-                k0[e] = ((unsigned)(c - cmin) << kMwIdxBits) | (unsigned)e;
+                k0[e] = ((unsigned)(c - cmin) << IDX) | (unsigned)e;
                 plist[e] = (unsigned char)j;
             }
         }
-        __syncwarp();
-        // 3. bottom-up merge of the sorted lists (ceil(log2 nl) levels)
+        grp_sync<G>(gid);
+        // 3. bottom-up merge of the sorted lists (ceil(log2 nl) levels, nl >= 2)
         unsigned *src = k0, *dst = k1;
+        const int per = (F + NT - 1) / NT;
+        const int p0 = min(t * per, F), p1 = min(p0 + per, F);
         {
-            const int per = (F + 31) >> 5;
-            const int p0 = min(lane * per, F), p1 = min(p0 + per, F);
-            const int levels = 32 - __clz(nl - 1);  // nl >= 2
-            for (int L = 0; L < levels; L++) {
-                mw_merge_level(L, src, dst, loff, nl, p0, p1);
-                __syncwarp();
+            const int levels = 32 - __clz(nl - 1);
+            for (int lv = 0; lv < levels; lv++) {
+                mw_merge_level(lv, src, dst, loff, nl, p0, p1);
+                grp_sync<G>(gid);
                 unsigned *x = src;
                 src = dst;
                 dst = x;
             }
         }
-        // 4. runs of one column: the heads (first product of each run) are
-        //    listed in order, then lane i reduces runs i, i + 32, ... (its
-        //    output goes to the row's position i: coalesced stores)
-        int len = 0;
-        for (int pb = 0; pb < F; pb += 32) {
-            const int p = pb + lane;
-            bool head = false;
-            if (p < F)
-                head = p == 0 || (src[p] >> kMwIdxBits) != (src[p - 1] >> kMwIdxBits);
-            const unsigned hm = __ballot_sync(kFull, head);
-            if (head)
-                dst[len + __popc(hm & lt)] = (unsigned)p;
-            len += __popc(hm);
-        }
-        if (lane == 0)
+        // 4. runs of one column: each thread finds the heads (first products
+        //    of runs) in its share, they are listed in order, and thread i
+        //    reduces runs i, i + NT, ... (coalesced stores)
+        int nh = 0;
+        for (int p = p0; p < p1; p++)
+            nh += p == 0 || (src[p] >> IDX) != (src[p - 1] >> IDX);
+        int len;
+        int hx = grp_excl_scan<G>(nh, gs, gid, &len);
+        for (int p = p0; p < p1; p++)
+            if (p == 0 || (src[p] >> IDX) != (src[p - 1] >> IDX))
+                dst[hx++] = (unsigned)p;
+        if (t == 0)
             dst[len] = (unsigned)F;
-        __syncwarp();
+        grp_sync<G>(gid);
         if (MODE == kMwSymbolic) {
-            if (lane == 0)
+            if (t == 0)
                 P.nnz[row] = len;
+            grp_sync<G>(gid);
             continue;
         }
         long long base;
         if (MODE == kMwPrecise) {
             base = crpt[row];
-            if (lane == 0 && len != crpt[row + 1] - crpt[row])
+            if (t == 0 && len != crpt[row + 1] - crpt[row])
                 atomicOr(&P.cnt->err, kErrNnzMismatch);
         } else if (MODE == kMwUpper) {
             base = P.scan_flop[row];
         } else {
             base = P.mid_pre[M] + P.mw_pre[row];
         }
-        if ((MODE == kMwUpper || MODE == kMwScratch) && lane == 0)
+        if ((MODE == kMwUpper || MODE == kMwScratch) && t == 0)
             P.nnz[row] = len;
         const T *arow = aval + a0;
-        constexpr unsigned imask = (1u << kMwIdxBits) - 1u;
-        for (int h = lane; h < len; h += 32) {
+        constexpr unsigned imask = (1u << IDX) - 1u;
+        for (int h = t; h < len; h += NT) {
             const int p = (int)dst[h], m = (int)dst[h + 1] - p;
             const unsigned *run = src + p;
             auto leaf = [&](int i) { return (int)lleaf[plist[run[i] & imask]]; };
@@ -264,22 +326,31 @@ __global__ void __launch_bounds__(kMwThreads) k_mid_warp(CsrDev A, CsrDev B, Pla
             };
             // leaves below 32 need at most 5 stack entries below the top
             const T v = k <= 32 ? mw_run_value<T, 6>(m, leaf, val) : mw_run_value<T, 9>(m, leaf, val);
-            ccol[base + h] = cmin + (int)(run[0] >> kMwIdxBits);
+            ccol[base + h] = cmin + (int)(run[0] >> IDX);
             cval[base + h] = v;
         }
-        __syncwarp();
+        grp_sync<G>(gid);
     }
 }
 
+template <typename T, int MODE, int G>
+inline void launch_mid_group(const CsrDev &A, const CsrDev &B, const PlanDev &P, const int *crpt,
+                             int *ccol, T *cval, int num_sms, cudaStream_t s)
+{
+    const size_t sm = MidWarpLayout<G>::bytes;
+    cudaFuncSetAttribute(k_mid_warp<T, MODE, G>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)sm);
+    k_mid_warp<T, MODE, G><<<num_sms * 2, kMwThreads, sm, s>>>(A, B, P, crpt, ccol, cval);
+    count_launch();
+}
+
+// The warp rows and the 4-warp group rows of one mode.
 template <typename T, int MODE>
 inline void launch_mid_warp(const CsrDev &A, const CsrDev &B, const PlanDev &P, const int *crpt,
                             int *ccol, T *cval, int num_sms, cudaStream_t s)
 {
-    const size_t sm = MidWarpLayout::bytes;
-    cudaFuncSetAttribute(k_mid_warp<T, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)sm);
-    k_mid_warp<T, MODE><<<num_sms * 2, kMwThreads, sm, s>>>(A, B, P, crpt, ccol, cval);
-    count_launch();
+    launch_mid_group<T, MODE, 1>(A, B, P, crpt, ccol, cval, num_sms, s);
+    launch_mid_group<T, MODE, 4>(A, B, P, crpt, ccol, cval, num_sms, s);
 }
 
 }  // namespace brm

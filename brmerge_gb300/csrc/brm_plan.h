@@ -35,9 +35,13 @@ constexpr int kMidMaxRows = kMidCap / (kWarpMaxFlop + 1) + 2;
 
 // Warp mid rows: more than kWarpMaxFlop and at most kMwF products, at most
 // kMidMaxK A entries, columns within a range below 2^kMwRangeBits; one warp
-// each (they take precedence over the batched mid rows).
+// each.  Group rows: up to kMgF products, range below 2^kMgRangeBits, four
+// warps each.  Both take precedence over the batched mid rows and over the
+// segmented heavy rows.
 constexpr int kMwF = 768;
 constexpr int kMwRangeBits = 22;
+constexpr int kMgF = 3072;
+constexpr int kMgRangeBits = 20;
 
 // Segmented heavy rows: a row that is not a mid row is cut, at 32-column word
 // (or, inside very dense words, column) boundaries, into column segments of at
@@ -75,7 +79,8 @@ enum RowBin : int {
     kBinMid = 4,    // row CTA
     kBinBatch = 5,  // batched mid-row kernels (no row list: row-order batches)
     kBinMidWarp = 6,  // one warp per row (brm_midwarp.cuh)
-    kNumBins = 7,
+    kBinMidGroup = 7, // four warps per row (brm_midwarp.cuh)
+    kNumBins = 8,
 };
 
 // Device counters (one struct in device memory, zeroed per phase).
