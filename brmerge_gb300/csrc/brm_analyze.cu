@@ -14,7 +14,7 @@ namespace brm {
 // global atomic per bin.
 // ---------------------------------------------------------------------------
 constexpr int kAnaThreads = 256;
-constexpr int kAnaRowsPerWarp = 8;
+constexpr int kAnaRowsPerWarp = 2;
 
 __global__ void __launch_bounds__(kAnaThreads) k_analyze(CsrDev A, CsrDev B, PlanDev P)
 {
