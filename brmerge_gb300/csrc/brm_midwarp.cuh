@@ -170,17 +170,17 @@ __device__ __forceinline__ void mw_merge_level(int L, const unsigned *__restrict
                 else
                     b = m;
             }
-            int ia = a, ib = d - a;
-            unsigned ka = ia < na ? src[ls + ia] : 0xffffffffu;
-            unsigned kb = ib < nb ? src[le + ib] : 0xffffffffu;
+            int ia = ls + a, ib = le + d - a;  // next positions in src
+            unsigned ka = ia < le ? src[ia] : 0xffffffffu;
+            unsigned kb = ib < re ? src[ib] : 0xffffffffu;
             for (; p < stop; p++) {
-                if (ka < kb) {
-                    dst[p] = ka;
-                    ka = ++ia < na ? src[ls + ia] : 0xffffffffu;
-                } else {
-                    dst[p] = kb;
-                    kb = ++ib < nb ? src[le + ib] : 0xffffffffu;
-                }
+                // branch-free step: one load, lanes stay converged
+                const bool ta = ka < kb;
+                dst[p] = ta ? ka : kb;
+                const int nx = ta ? ++ia : ++ib;
+                const unsigned kn = nx < (ta ? le : re) ? src[nx] : 0xffffffffu;
+                ka = ta ? kn : ka;
+                kb = ta ? kb : kn;
             }
         }
         j = l2;
