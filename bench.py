@@ -46,7 +46,7 @@ def csr_bytes(M: int, nnz: int, vbytes: int) -> int:
     return 4 * (M + 1) + nnz * (4 + vbytes)
 
 
-def make_workload(name: str):
+def make_workload(name: str, stencil_n: int = 128):
     import brmerge_gb300 as brm
     if name == "rmat":
         n = 1 << RMAT_SCALE
@@ -57,8 +57,8 @@ def make_workload(name: str):
         A = brm.gen_er(16384, 8, seed=0)
         desc = {"workload": "er_n16384_8perrow_AxA", "n": 16384, "seed": 0}
     elif name == "stencil":
-        A = brm.gen_stencil27(128)
-        desc = {"workload": "stencil27_128^3_AxA", "n": 128 ** 3}
+        A = brm.gen_stencil27(stencil_n)
+        desc = {"workload": f"stencil27_{stencil_n}^3_AxA", "n": stencil_n ** 3}
     else:
         raise SystemExit(f"unknown workload {name}")
     return A, desc
@@ -190,7 +190,7 @@ def run_reference(args):
         return
     import oracle
     oracle.build(with_ref=False)
-    A, desc = make_workload(args.workload)
+    A, desc = make_workload(args.workload, args.stencil_n)
     use_ref = oracle.ref_available()
     nt = oracle.max_threads()
     flop = oracle.compute_flop(A, A)
@@ -538,7 +538,7 @@ def run_ours(args):
         dist.init_process_group("nccl")
     dev = torch.device("cuda", local if ws > 1 else 0)
     torch.cuda.set_device(dev)
-    A, desc = make_workload(args.workload)
+    A, desc = make_workload(args.workload, args.stencil_n)
     products = brm.compute_flop_host(A, A)
     stream = torch.cuda.current_stream(dev)
     ctx = brm.Context(stream=stream)
@@ -672,6 +672,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=["rmat", "er", "stencil"], default="rmat")
+    ap.add_argument("--stencil-n", type=int, default=128,
+                    help="grid side of the stencil workload (profiling uses a smaller one)")
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batch", action="store_true",
