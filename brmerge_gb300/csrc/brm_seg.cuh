@@ -566,25 +566,42 @@ __global__ void __launch_bounds__(kSegThreads) k_seg_numeric(CsrDev A, CsrDev B,
         const int nsum = (span + 1023) >> 10;
         const int *sp0 = P.split + d.tab + (long long)d.bidx * k;
         const int *sp1 = sp0 + k;
-        // nonempty sub-lists of the segment, in leaf order
+        // nonempty sub-lists of the segment, in leaf order (a thread takes
+        // four consecutive lists per pass: hub rows have thousands of lists
+        // and few products of each in one segment)
+        constexpr int LPT = 4;
         int lcarry = 0, pcarry = 0;
-        for (int lb = 0; lb < k; lb += NT) {
-            const int l = lb + tid;
-            int st = 0, len = 0;
-            if (l < k) {
-                st = sp0[l];
-                len = sp1[l] - st;
+        for (int lb = 0; lb < k; lb += NT * LPT) {
+            int st[LPT], len[LPT];
+            int cnt = 0, psum = 0;
+#pragma unroll
+            for (int q = 0; q < LPT; q++) {
+                const int l = lb + tid * LPT + q;
+                st[q] = 0;
+                len[q] = 0;
+                if (l < k) {
+                    st[q] = sp0[l];
+                    len[q] = sp1[l] - st[q];
+                }
+                cnt += len[q] > 0;
+                psum += len[q];
             }
-            const bool ne = len > 0;
             long long tot;
             const long long ex = block_excl_scan<NT, long long>(
-                ((long long)(ne ? 1 : 0) << 32) | (long long)len, ws, &tot);
-            const int li = lcarry + (int)(ex >> 32);
-            const int po = pcarry + (int)(ex & 0xffffffffLL);
-            if (ne && li < kSegCap) {
-                loff[li] = po;
-                lbs[li] = st;
-                lleaf[li] = (unsigned short)l;
+                ((long long)cnt << 32) | (long long)psum, ws, &tot);
+            int li = lcarry + (int)(ex >> 32);
+            int po = pcarry + (int)(ex & 0xffffffffLL);
+#pragma unroll
+            for (int q = 0; q < LPT; q++) {
+                if (len[q] > 0) {
+                    if (li < kSegCap) {
+                        loff[li] = po;
+                        lbs[li] = st[q];
+                        lleaf[li] = (unsigned short)(lb + tid * LPT + q);
+                    }
+                    li++;
+                    po += len[q];
+                }
             }
             lcarry += (int)(tot >> 32);
             pcarry += (int)(tot & 0xffffffffLL);
