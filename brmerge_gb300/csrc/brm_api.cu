@@ -492,7 +492,7 @@ int numeric_by_parts(brm_context ctx, brm_dtype dtype, const brm_csr *A, const b
     const int *d_rpt = (const int *)ctx->io_crpt.p;
     BRM_CK(cudaMemcpyAsync(h_rpt, d_rpt, 4 * ((size_t)M + 1), cudaMemcpyDeviceToHost, s));
     // parts: one per 32 MB of C, at most kHostParts
-    constexpr int kHostParts = 4;
+    constexpr int kHostParts = 8;
     const long long bytes = (long long)cnnz * (long long)(4 + vb);
     const int nparts = (int)std::min<long long>(kHostParts, std::max<long long>(1, bytes >> 25));
     if (nparts <= 1) {
