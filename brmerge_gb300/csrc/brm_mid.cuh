@@ -615,7 +615,7 @@ __global__ void __launch_bounds__(256) k_batch_starts(PlanDev P, int M)
 template <typename T>
 __global__ void __launch_bounds__(256) k_mid_compact(PlanDev P, int M, const int *__restrict__ scol,
                                                      const T *__restrict__ sval, const int *crpt,
-                                                     int *ccol, T *cval)
+                                                     int *__restrict__ ccol, T *__restrict__ cval)
 {
     const int lane = threadIdx.x & 31;
     const int nwarps = (gridDim.x * blockDim.x) >> 5;
@@ -631,7 +631,23 @@ __global__ void __launch_bounds__(256) k_mid_compact(PlanDev P, int M, const int
             continue;
         const long long dst = crpt[row];
         const int n = P.nnz[row];
-        for (int i = lane; i < n; i += 32) {
+        // four elements per lane in flight before the stores
+        int i = lane;
+        for (; i + 96 < n; i += 128) {
+            int c[4];
+            T v[4];
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                c[u] = scol[src + i + 32 * u];
+                v[u] = sval[src + i + 32 * u];
+            }
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                ccol[dst + i + 32 * u] = c[u];
+                cval[dst + i + 32 * u] = v[u];
+            }
+        }
+        for (; i < n; i += 32) {
             ccol[dst + i] = scol[src + i];
             cval[dst + i] = sval[src + i];
         }

@@ -791,7 +791,8 @@ __global__ void __launch_bounds__(256) k_warp_numeric(CsrDev A, CsrDev B, PlanDe
 // ---------------------------------------------------------------------------
 template <typename T, bool UPPER>
 __global__ void __launch_bounds__(256) k_copy_numeric(CsrDev A, CsrDev B, PlanDev P,
-                                                      const int *crpt, int *ccol, T *cval)
+                                                      const int *crpt, int *__restrict__ ccol,
+                                                      T *__restrict__ cval)
 {
     const int lane = threadIdx.x & 31;
     const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -807,9 +808,27 @@ __global__ void __launch_bounds__(256) k_copy_numeric(CsrDev A, CsrDev B, PlanDe
         const T a = ((const T *)A.val)[j];
         const int s = B.rpt[b], len = B.rpt[b + 1] - s;
         const long long base = UPPER ? P.scan_flop[row] : (long long)crpt[row];
-        for (int q = lane; q < len; q += 32) {
-            ccol[base + q] = B.col[s + q];
-            cval[base + q] = vmul(a, ((const T *)B.val)[s + q]);
+        const int *__restrict__ bcol = B.col;
+        const T *__restrict__ bval = (const T *)B.val;
+        // four elements per lane in flight before the stores
+        int q = lane;
+        for (; q + 96 < len; q += 128) {
+            int c[4];
+            T v[4];
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                c[u] = bcol[s + q + 32 * u];
+                v[u] = bval[s + q + 32 * u];
+            }
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                ccol[base + q + 32 * u] = c[u];
+                cval[base + q + 32 * u] = vmul(a, v[u]);
+            }
+        }
+        for (; q < len; q += 32) {
+            ccol[base + q] = bcol[s + q];
+            cval[base + q] = vmul(a, bval[s + q]);
         }
     }
 }
