@@ -618,17 +618,29 @@ __global__ void __launch_bounds__(256) k_mid_compact(PlanDev P, int M, const int
                                                      int *__restrict__ ccol, T *__restrict__ cval)
 {
     const int lane = threadIdx.x & 31;
+    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nwarps = (gridDim.x * blockDim.x) >> 5;
     const int r1 = min(M, P.r_hi);
-    for (int row = P.r_lo + ((blockIdx.x * blockDim.x + threadIdx.x) >> 5); row < r1;
-         row += nwarps) {
+    // warp and group rows from their row lists, then (only when there are
+    // batches) the batched mid rows by a sweep over the rows
+    const int nw1 = P.cnt->bin_count[kBinMidWarp];
+    const int nw4 = P.cnt->bin_count[kBinMidGroup];
+    const int nsweep = P.cnt->n_batch > 0 ? r1 - P.r_lo : 0;
+    for (int it = gw; it < nw1 + nw4 + nsweep; it += nwarps) {
+        int row;
         long long src;
-        if (P.mid_flop[row] != 0)
-            src = P.mid_pre[row];
-        else if (P.mw_flop[row] != 0)
+        if (it < nw1 + nw4) {
+            row = it < nw1 ? P.rows[(size_t)kBinMidWarp * M + it]
+                           : P.rows[(size_t)kBinMidGroup * M + (it - nw1)];
+            if (row < P.r_lo || row >= r1)
+                continue;
             src = P.mid_pre[M] + P.mw_pre[row];
-        else
-            continue;
+        } else {
+            row = P.r_lo + (it - nw1 - nw4);
+            if (P.mid_flop[row] == 0)
+                continue;
+            src = P.mid_pre[row];
+        }
         const long long dst = crpt[row];
         const int n = P.nnz[row];
         // four elements per lane in flight before the stores
