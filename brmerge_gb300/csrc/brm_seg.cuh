@@ -941,6 +941,34 @@ __global__ void __launch_bounds__(kSegThreads) k_seg_numeric(CsrDev A, CsrDev B,
 //    pass with the stack in registers (leaves below 2^16: at most 16 entries
 //    below the top).
 // ---------------------------------------------------------------------------
+// Sequential trie of the elements [b, e) of a long column (leaves in
+// increasing order, below 2^(D-1)).
+template <typename T, int D>
+__device__ __forceinline__ T long_run(const unsigned short *__restrict__ lleaf,
+                                      const T *__restrict__ lval, long long b, long long e)
+{
+    RegShiftReduce<T, D> sr;
+    sr.init(lleaf[b], lval[b]);
+    // elements in groups of kGatherBatch independent loads, so a long
+    // column does not wait for one load per element
+    for (long long j0 = b + 1; j0 < e; j0 += kGatherBatch) {
+        int lf[kGatherBatch];
+        T lv[kGatherBatch];
+#pragma unroll
+        for (int q = 0; q < kGatherBatch; q++) {
+            if (j0 + q < e) {
+                lf[q] = lleaf[j0 + q];
+                lv[q] = lval[j0 + q];
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < kGatherBatch; q++)
+            if (j0 + q < e)
+                sr.push(lf[q], lv[q]);
+    }
+    return sr.finish();
+}
+
 template <typename T>
 __global__ void __launch_bounds__(128) k_long_reduce(PlanDev P, int *ccol, T *cval)
 {
@@ -948,32 +976,25 @@ __global__ void __launch_bounds__(128) k_long_reduce(PlanDev P, int *ccol, T *cv
     const long long n = min((long long)(used >> 40), P.long_cap_cols);
     const T *__restrict__ lval = (const T *)P.long_val;
     const unsigned short *__restrict__ lleaf = P.long_leaf;
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-         i += (long long)gridDim.x * blockDim.x) {
-        const LongCol c = P.long_col[i];
-        if (c.len <= 0)
-            continue;
-        RegShiftReduce<T, 17> sr;
-        sr.init(lleaf[c.off], lval[c.off]);
-        // elements in groups of kGatherBatch independent loads, so a long
-        // column does not wait for one load per element
-        for (int j0 = 1; j0 < c.len; j0 += kGatherBatch) {
-            int lf[kGatherBatch];
-            T lv[kGatherBatch];
-#pragma unroll
-            for (int q = 0; q < kGatherBatch; q++) {
-                if (j0 + q < c.len) {
-                    lf[q] = lleaf[c.off + j0 + q];
-                    lv[q] = lval[c.off + j0 + q];
-                }
+    for (long long i0 = (long long)blockIdx.x * blockDim.x; i0 < n;
+         i0 += (long long)gridDim.x * blockDim.x) {
+        const long long i = i0 + threadIdx.x;
+        LongCol c;
+        c.len = 0;
+        if (i < n)
+            c = P.long_col[i];
+        // the stack depth follows the largest leaf (the last one); the warp
+        // takes the shallow stack when all of its columns allow it
+        const bool shallow = c.len <= 0 || lleaf[c.off + c.len - 1] < 256;
+        if (__all_sync(kFull, shallow)) {
+            if (c.len > 0) {
+                ccol[c.out] = c.col;
+                cval[c.out] = long_run<T, 9>(lleaf, lval, c.off, c.off + c.len);
             }
-#pragma unroll
-            for (int q = 0; q < kGatherBatch; q++)
-                if (j0 + q < c.len)
-                    sr.push(lf[q], lv[q]);
+        } else if (c.len > 0) {
+            ccol[c.out] = c.col;
+            cval[c.out] = long_run<T, 17>(lleaf, lval, c.off, c.off + c.len);
         }
-        ccol[c.out] = c.col;
-        cval[c.out] = sr.finish();
     }
 }
 
