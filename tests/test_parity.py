@@ -351,3 +351,69 @@ def test_repeat_calls_identical(ctx):
     C1 = ctx.precise(dA, dA).to_host()
     C2 = ctx.precise(dA, dA).to_host()
     assert_same_csr(C1, C2, "repeat")
+
+
+# ---------------------------------------------------------------------------
+# warp and four-warp mid rows: class boundaries and fallbacks
+# ---------------------------------------------------------------------------
+
+def _rows_with_products(rng, targets, K, N, blen_lo=1, blen_hi=6, span=None):
+    """B with K rows of blen_lo..blen_hi columns (within [0, span) when given)
+    and one A row per target product count (A rows pick B rows greedily,
+    longest first, so the short rows fill the remainder exactly)."""
+    span = N if span is None else span
+    blens = rng.integers(blen_lo, blen_hi + 1, K)
+    Brows = [sorted(rng.choice(span, int(b), replace=False)) for b in blens]
+    Arows = []
+    for t in targets:
+        order = rng.permutation(K)
+        order = order[np.argsort(-blens[order], kind="stable")]
+        row, f = [], 0
+        for b in order:
+            if f + blens[b] <= t:
+                row.append(int(b))
+                f += int(blens[b])
+            if f == t:
+                break
+        Arows.append(sorted(row))
+    return _csr(Arows, K, 1), _csr(Brows, N, 2)
+
+
+def test_mid_row_class_boundaries(ctx, oracle_mod):
+    """Rows of 33, 768, 769, 3072 and 3073 products (warp, group and
+    segmented classes on either side of each boundary)."""
+    rng = np.random.default_rng(41)
+    A, B = _rows_with_products(rng, [33, 767, 768, 769, 1500, 3071, 3072, 3073, 5000],
+                               K=3000, N=20000, blen_lo=1, blen_hi=30)
+    R = oracle_mod.precise(A, B)
+    assert_same_csr(gpu_precise(ctx, A, B), R, "boundaries split")
+    assert_same_csr(gpu_precise_one_call(ctx, A, B), R, "boundaries one call")
+    assert_same_csr(gpu_upper(ctx, A, B), R, "boundaries upper")
+
+
+def test_mid_rows_wide_column_range(ctx, oracle_mod):
+    """Mid-size rows whose columns span more than 2^20 / 2^22 columns take the
+    batched or segmented paths instead of the warp kernels."""
+    rng = np.random.default_rng(42)
+    N = 6_000_000
+    A, B = _rows_with_products(rng, [100, 700, 2000, 3000], K=2000, N=N, blen_lo=1, blen_hi=30)
+    R = oracle_mod.precise(A, B)
+    assert_same_csr(gpu_precise(ctx, A, B), R, "wide split")
+    assert_same_csr(gpu_precise_one_call(ctx, A, B), R, "wide one call")
+    assert_same_csr(gpu_upper(ctx, A, B), R, "wide upper")
+
+
+def test_mid_rows_list_counts(ctx, oracle_mod):
+    """Warp rows with 31, 32, 33 and 255 lists (register stack of 6 or 9
+    levels), many repeated columns so that long runs are reduced."""
+    rng = np.random.default_rng(43)
+    K, N = 400, 60
+    Brows = [sorted(rng.choice(N, int(rng.integers(1, 4)), replace=False)) for _ in range(K)]
+    Arows = [sorted(rng.choice(K, k, replace=False)) for k in (31, 32, 33, 100, 255)]
+    A, B = _csr(Arows, K, 3), _csr(Brows, N, 4)
+    R = oracle_mod.precise(A, B)
+    assert_same_csr(gpu_precise(ctx, A, B), R, "list counts")
+    assert_same_csr(gpu_precise_one_call(ctx, A, B), R, "list counts one call")
+    assert_same_csr(gpu_upper(ctx, A, B), R, "list counts upper")
+    C32 = gpu_precise(ctx, A.astype(np.float32), B.astype(np.float32))
+    assert_same_csr(C32, oracle_mod.precise(A.astype(np.float32), B.astype(np.float32)), "f32")
