@@ -2,13 +2,13 @@
 //
 // The reference multiplies one pair per call (BRMerge-SpGEMM/inc/spgemm.h:
 // 468-735).  Rows of C depend only on their own A row and the B rows it
-// names, so a batch of n pairs is one product of block-diagonal matrices:
-// A_bd = diag(A_1 .. A_n) and B_bd = diag(B_1 .. B_n), with A_i's columns
-// shifted by the B rows before it and B_i's columns by the B columns before
-// it.  Every row of C_bd is the merge of exactly the lists of its own pair,
-// in the same leaf order, so each C_i is bit-identical to a separate call.
-// The batch runs as one Precise pipeline (about twenty kernel launches for
-// all pairs together); C_i's columns are shifted back afterwards.
+// names, so a batch of n pairs is one product of stacked operands: A_bd =
+// diag(A_1 .. A_n) (A_i's columns shifted by the B rows before it) and B_bd
+// = the B_i stacked row-wise with their own columns (N_bd = max N_i).  Every
+// row of C_bd is the merge of exactly the lists of its own pair, in the same
+// leaf order, over B_i's own columns, so each C_i is bit-identical to a
+// separate call and needs no column shift.  The batch runs as one Precise
+// pipeline (about thirty kernel launches for all pairs together).
 #include <algorithm>
 #include <climits>
 #include <cstdlib>
@@ -21,13 +21,12 @@
 
 namespace brm {
 
-// One pair on the device: its input views and its offsets in the
-// block-diagonal operands (A rows, A entries, B rows = A columns, B entries,
-// B columns = C columns).
+// One pair on the device: its input views and its offsets in the stacked
+// operands (A rows, A entries, B rows = A columns, B entries).
 struct BatchPair {
     const int *arpt, *acol, *brpt, *bcol;
     const void *aval, *bval;
-    long long row_a, nnz_a, row_b, nnz_b, col_b;
+    long long row_a, nnz_a, row_b, nnz_b;
     int M, K, N, nnzA, nnzB;
 };
 
@@ -68,9 +67,10 @@ __global__ void __launch_bounds__(256) k_batch_rows(const BatchPair *pairs, int 
     }
 }
 
-// Columns and values of A_bd (which = 0) or B_bd (which = 1): one thread per
-// entry of the concatenation.
-template <typename T>
+// Columns (COLS) and values of A_bd (which = 0) or B_bd (which = 1): one
+// thread per entry of the concatenation.  A replay of a fixed structure
+// gathers the values alone.
+template <typename T, bool COLS>
 __global__ void __launch_bounds__(256) k_batch_entries(const BatchPair *pairs, int n,
                                                        const long long *nnz_off, long long nnz,
                                                        int which, int *col, T *val)
@@ -81,34 +81,22 @@ __global__ void __launch_bounds__(256) k_batch_entries(const BatchPair *pairs, i
         const BatchPair &q = pairs[i];
         if (which == 0) {
             const long long j = e - q.nnz_a;
-            col[e] = (int)(q.acol[j] + q.row_b);
+            if (COLS)
+                col[e] = (int)(q.acol[j] + q.row_b);
             val[e] = ((const T *)q.aval)[j];
         } else {
             const long long j = e - q.nnz_b;
-            col[e] = (int)(q.bcol[j] + q.col_b);
+            if (COLS)
+                col[e] = q.bcol[j];
             val[e] = ((const T *)q.bval)[j];
         }
     }
 }
 
-// C_bd -> the pairs' own columns, and each pair's first entry in C_bd.  One
-// warp per row.
-__global__ void __launch_bounds__(256) k_batch_unshift(const BatchPair *pairs, int n,
-                                                       const long long *row_off, int rows,
-                                                       const int *crpt, int *ccol,
-                                                       long long *nnz_first)
+// Each pair's first entry in C_bd (every pair, including empty ones).
+__global__ void __launch_bounds__(256) k_batch_first(const BatchPair *pairs, int n, int rows,
+                                                     const int *crpt, long long *nnz_first)
 {
-    const int lane = threadIdx.x & 31;
-    const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
-    for (long long r = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < rows;
-         r += nwarps) {
-        const int i = pair_of(row_off, n, r);
-        const int shift = (int)pairs[i].col_b;
-        const int s = crpt[r], e = crpt[r + 1];
-        for (int j = s + lane; j < e; j += 32)
-            ccol[j] -= shift;
-    }
-    // pair starts (every pair, including empty ones)
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i <= n;
          i += (long long)gridDim.x * blockDim.x)
         nnz_first[i] = crpt[i < n ? pairs[i].row_a : rows];
@@ -158,9 +146,9 @@ int grow_buf(Buf &b, size_t bytes, cudaStream_t s)
 
 size_t a256(size_t x) { return (x + 255) & ~size_t(255); }
 
-// Offsets of every pair in the block-diagonal operands: hp[i] and, in off,
-// four arrays of n + 1 prefixes (A rows, A entries, B rows, B entries); the
-// totals in ra, na, rb, nb and cb (B columns).  BRM_ERR_INVALID_VALUE for a
+// Offsets of every pair in the stacked operands: hp[i] and, in off, four
+// arrays of n + 1 prefixes (A rows, A entries, B rows, B entries); the
+// totals in ra, na, rb, nb, and cb = the largest B column count.  BRM_ERR_INVALID_VALUE for a
 // malformed pair, BRM_ERR_CAPACITY when a total does not fit int32.
 int batch_layout(int n, const brm_csr *A, const brm_csr *B, std::vector<brm::BatchPair> &hp,
                  std::vector<long long> &off, long long &ra, long long &na, long long &rb,
@@ -191,7 +179,6 @@ int batch_layout(int n, const brm_csr *A, const brm_csr *B, std::vector<brm::Bat
         q.nnz_a = na;
         q.row_b = rb;
         q.nnz_b = nb;
-        q.col_b = cb;
         off[(size_t)i] = ra;
         off[(size_t)(n + 1) + i] = na;
         off[(size_t)2 * (n + 1) + i] = rb;
@@ -200,7 +187,7 @@ int batch_layout(int n, const brm_csr *A, const brm_csr *B, std::vector<brm::Bat
         na += a.nnz;
         rb += a.N;
         nb += b.nnz;
-        cb += b.N;
+        cb = std::max<long long>(cb, b.N);
     }
     off[(size_t)n] = ra;
     off[(size_t)(n + 1) + n] = na;
@@ -211,26 +198,37 @@ int batch_layout(int n, const brm_csr *A, const brm_csr *B, std::vector<brm::Bat
     return BRM_SUCCESS;
 }
 
-// Gathers the pairs' columns and values into the block-diagonal operands.
-void launch_entries(brm_dtype dtype, const brm::BatchPair *dp, int n, const long long *doff,
-                    long long na, long long nb, int *A_col, void *A_val, int *B_col, void *B_val,
-                    int grid, cudaStream_t s)
+// Gathers the pairs' columns (cols) and values into the stacked operands.
+template <bool COLS>
+void launch_entries_t(brm_dtype dtype, const brm::BatchPair *dp, int n, const long long *doff,
+                      long long na, long long nb, int *A_col, void *A_val, int *B_col,
+                      void *B_val, int grid, cudaStream_t s)
 {
     if (dtype == BRM_F64) {
-        brm::k_batch_entries<double><<<grid, 256, 0, s>>>(dp, n, doff + (n + 1), na, 0, A_col,
-                                                          (double *)A_val);
+        brm::k_batch_entries<double, COLS><<<grid, 256, 0, s>>>(dp, n, doff + (n + 1), na, 0,
+                                                                A_col, (double *)A_val);
         brm::count_launch();
-        brm::k_batch_entries<double><<<grid, 256, 0, s>>>(dp, n, doff + 3 * (n + 1), nb, 1, B_col,
-                                                          (double *)B_val);
+        brm::k_batch_entries<double, COLS><<<grid, 256, 0, s>>>(dp, n, doff + 3 * (n + 1), nb, 1,
+                                                                B_col, (double *)B_val);
         brm::count_launch();
     } else {
-        brm::k_batch_entries<float><<<grid, 256, 0, s>>>(dp, n, doff + (n + 1), na, 0, A_col,
-                                                         (float *)A_val);
+        brm::k_batch_entries<float, COLS><<<grid, 256, 0, s>>>(dp, n, doff + (n + 1), na, 0,
+                                                               A_col, (float *)A_val);
         brm::count_launch();
-        brm::k_batch_entries<float><<<grid, 256, 0, s>>>(dp, n, doff + 3 * (n + 1), nb, 1, B_col,
-                                                         (float *)B_val);
+        brm::k_batch_entries<float, COLS><<<grid, 256, 0, s>>>(dp, n, doff + 3 * (n + 1), nb, 1,
+                                                               B_col, (float *)B_val);
         brm::count_launch();
     }
+}
+
+void launch_entries(brm_dtype dtype, const brm::BatchPair *dp, int n, const long long *doff,
+                    long long na, long long nb, int *A_col, void *A_val, int *B_col, void *B_val,
+                    int grid, cudaStream_t s, bool cols = true)
+{
+    if (cols)
+        launch_entries_t<true>(dtype, dp, n, doff, na, nb, A_col, A_val, B_col, B_val, grid, s);
+    else
+        launch_entries_t<false>(dtype, dp, n, doff, na, nb, A_col, A_val, B_col, B_val, grid, s);
 }
 
 }  // namespace
@@ -246,7 +244,7 @@ int brm_batch_precise(brm_context ctx, brm_dtype dtype, int n, const brm_csr *A,
         return BRM_ERR_INVALID_VALUE;
     std::memset(out, 0, sizeof(*out));
     out->n = n;
-    // offsets of every pair in the block-diagonal operands
+    // offsets of every pair in the stacked operands
     std::vector<brm::BatchPair> hp;
     std::vector<long long> off;
     long long ra = 0, na = 0, rb = 0, nb = 0, cb = 0;
@@ -301,21 +299,7 @@ int brm_batch_precise(brm_context ctx, brm_dtype dtype, int n, const brm_csr *A,
         brm::count_launch();
         brm::k_batch_rows<<<g, 256, 0, s>>>(dp, n, doff + 2 * (n + 1), rb, 1, B_rpt);
         brm::count_launch();
-        if (dtype == BRM_F64) {
-            brm::k_batch_entries<double><<<g, 256, 0, s>>>(dp, n, doff + (n + 1), na, 0, A_col,
-                                                           (double *)A_val);
-            brm::count_launch();
-            brm::k_batch_entries<double><<<g, 256, 0, s>>>(dp, n, doff + 3 * (n + 1), nb, 1,
-                                                           B_col, (double *)B_val);
-            brm::count_launch();
-        } else {
-            brm::k_batch_entries<float><<<g, 256, 0, s>>>(dp, n, doff + (n + 1), na, 0, A_col,
-                                                          (float *)A_val);
-            brm::count_launch();
-            brm::k_batch_entries<float><<<g, 256, 0, s>>>(dp, n, doff + 3 * (n + 1), nb, 1,
-                                                          B_col, (float *)B_val);
-            brm::count_launch();
-        }
+        launch_entries(dtype, dp, n, doff, na, nb, A_col, A_val, B_col, B_val, g, s);
         e = cudaGetLastError();
     }
     if (e != cudaSuccess) {
@@ -323,7 +307,7 @@ int brm_batch_precise(brm_context ctx, brm_dtype dtype, int n, const brm_csr *A,
         cleanup();
         return BRM_ERR_CUDA;
     }
-    // one Precise call on the block-diagonal operands
+    // one Precise call on the stacked operands
     brm_csr Abd{(int)ra, (int)rb, (int)na, A_rpt, A_col, A_val};
     brm_csr Bbd{(int)rb, (int)cb, (int)nb, B_rpt, B_col, B_val};
     int *crpt = nullptr, *ccol = nullptr;
@@ -338,7 +322,7 @@ int brm_batch_precise(brm_context ctx, brm_dtype dtype, int n, const brm_csr *A,
     e = cudaMallocAsync((void **)&lrpt, sizeof(int) * (size_t)(ra + n), s);
     if (e == cudaSuccess) {
         const int g = std::max(sms, 1) * 16;
-        brm::k_batch_unshift<<<g, 256, 0, s>>>(dp, n, doff, (int)ra, crpt, ccol, dfirst);
+        brm::k_batch_first<<<g, 256, 0, s>>>(dp, n, (int)ra, crpt, dfirst);
         brm::count_launch();
         brm::k_batch_local_rpt<<<g, 256, 0, s>>>(n, doff, ra, crpt, dfirst, lrpt);
         brm::count_launch();
@@ -396,11 +380,11 @@ int brm_batch_free(brm_context ctx, brm_batch *b)
 }  // extern "C"
 
 // ---------------------------------------------------------------------------
-// Batch with a fixed structure replayed as a CUDA graph.  The block-diagonal
+// Batch with a fixed structure replayed as a CUDA graph.  The stacked
 // structure, the symbolic plan and C's row pointers are made once; the part
 // that depends on the values (gathering every pair's current values into the
-// block-diagonal operands, the numeric phase, shifting C's columns back) is
-// captured once and replayed with one graph launch per recomputation.
+// stacked operands and the numeric phase) is captured once and replayed with
+// one graph launch per recomputation.
 // ---------------------------------------------------------------------------
 struct brm_batch_graph_s {
     brm_context ctx = nullptr;     // private: its plan belongs to this batch
@@ -420,20 +404,19 @@ struct brm_batch_graph_s {
 
 namespace {
 
-// Enqueues the value-dependent part on the private context's current stream.
+// Enqueues the value-dependent part on the private context's current
+// stream: the pairs' current values into the stacked operands (their
+// columns are fixed), then the numeric phase straight into C.
 int batch_graph_values(brm_batch_graph g)
 {
     cudaStream_t s = brm::context_stream(g->ctx);
     const int grid = std::max(brm::context_num_sms(g->ctx), 1) * 16;
     launch_entries(g->dtype, g->dp, g->n, g->doff, g->na, g->nb, (int *)g->Abd.col,
-                   (void *)g->Abd.val, (int *)g->Bbd.col, (void *)g->Bbd.val, grid, s);
+                   (void *)g->Abd.val, (int *)g->Bbd.col, (void *)g->Bbd.val, grid, s, false);
     const int st = brm::numeric_async(g->ctx, g->dtype, &g->Abd, &g->Bbd, g->out.crpt, g->out.ccol,
                                       g->out.cval);
     if (st != BRM_SUCCESS)
         return st;
-    brm::k_batch_unshift<<<grid, 256, 0, s>>>(g->dp, g->n, g->doff, (int)g->ra, g->out.crpt,
-                                              g->out.ccol, g->dfirst);
-    brm::count_launch();
     return cudaGetLastError() == cudaSuccess ? BRM_SUCCESS : BRM_ERR_CUDA;
 }
 
@@ -553,6 +536,8 @@ int brm_batch_graph_create(brm_context ctx, brm_dtype dtype, int n, const brm_cs
     if (st == BRM_SUCCESS)
         st = batch_graph_values(g);
     if (st == BRM_SUCCESS) {
+        brm::k_batch_first<<<grid, 256, 0, s>>>(g->dp, n, (int)g->ra, g->out.crpt, g->dfirst);
+        brm::count_launch();
         brm::k_batch_local_rpt<<<grid, 256, 0, s>>>(n, g->doff, g->ra, g->out.crpt, g->dfirst,
                                                     g->out.rpt_local);
         brm::count_launch();

@@ -5,7 +5,7 @@
 // non-blocking stream, take whatever is queued (same value type, in arrival
 // order), admit requests while the summed upper-bound bytes of everything
 // admitted and not yet released stay under the memory cap, and run them as
-// one batch (brm_batch_precise: one block-diagonal pipeline).  Requests that
+// one batch (brm_batch_precise: one stacked-operand pipeline).  Requests that
 // arrive while batches are on the GPU wait for the next free worker, so the
 // batches of different workers overlap on the device.  A result stays in
 // the batch's device arrays until the caller releases it; the batch's memory

@@ -524,7 +524,7 @@ class _ServerBlock(_RawDevice):
 
 class Server:
     """brm_server: C = A * B requests from any thread, batched by worker
-    threads under a memory cap (one block-diagonal pipeline per batch)."""
+    threads under a memory cap (one stacked-operand pipeline per batch)."""
 
     def __init__(self, mem_cap_bytes: int = 0, max_batch: int = 0, workers: int = 0):
         self._L = _native.lib()

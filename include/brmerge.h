@@ -222,22 +222,22 @@ typedef struct brm_batch {
 
 /* C_i = A_i * B_i (BRMerge-Precise) for n independent pairs of device CSR
  * matrices of one value type, in one pipeline: the pairs form one product of
- * block-diagonal matrices, so the kernels see every row of every pair at
- * once.  Each C_i is bit-identical to brm_precise_device(A_i, B_i).  No
- * counterpart in the reference (one pair per call).  The concatenated rows,
- * entries and columns must each fit int32 (else BRM_ERR_CAPACITY); nnz of
- * all C_i together must fit int32 (else BRM_ERR_OVERFLOW). */
+ * stacked operands (A block-diagonal, the B_i stacked row-wise with their own
+ * columns), so the kernels see every row of every pair at once.  Each C_i is
+ * bit-identical to brm_precise_device(A_i, B_i).  No counterpart in the
+ * reference (one pair per call).  The concatenated rows and entries must
+ * each fit int32 (else BRM_ERR_CAPACITY); nnz of all C_i together must fit
+ * int32 (else BRM_ERR_OVERFLOW). */
 int brm_batch_precise(brm_context ctx, brm_dtype dtype, int n, const brm_csr *A, const brm_csr *B,
                       brm_batch *out);
 int brm_batch_free(brm_context ctx, brm_batch *batch);
 
 /* A batch whose structure stays fixed while its values change (the reuse
  * pattern of iterative methods), replayed as one CUDA graph.  Create makes
- * the block-diagonal structure, the symbolic plan and every C_i's row
- * pointers and columns once (in a private context that copies ctx's
- * tuning), computes the values once, and captures the value-dependent part
- * (gathering the pairs' current values, the numeric phase, the column
- * shift) into a graph.  Launch replays it on `stream` (cudaStream_t as void*,
+ * the stacked structure, the symbolic plan and every C_i's row pointers and
+ * columns once (in a private context that copies ctx's tuning), computes the
+ * values once, and captures the value-dependent part (gathering the pairs'
+ * current values, the numeric phase) into a graph.  Launch replays it on `stream` (cudaStream_t as void*,
  * NULL = legacy default stream), waits for it and returns the device-side
  * error status; the pairs' value arrays are read at launch, so the caller
  * updates them in place (ordered before the launch) and relaunches.  *out
