@@ -10,9 +10,11 @@
 //   2. every product as a 32-bit key ((column - cmin) << 10 | product index)
 //      in list-major order, i.e. leaf order (BRMerge-SpGEMM/inc/spgemm.h:
 //      618-624: list l holds the l-th A entry's scaled B row);
-//   3. a bottom-up merge of the sorted lists by key, ceil(log2 lists)
-//      levels (merge path: every lane a contiguous share of the output), so
-//      equal columns end in leaf order;
+//   3. the keys sorted: up to 128 products in registers by a bitonic
+//      network across the warp, more by a bottom-up merge of the sorted
+//      lists, ceil(log2 lists) levels (merge path: every lane a contiguous
+//      share of the output); the keys are unique and equal columns end in
+//      leaf order;
 //   4. the runs of one column are listed and lane i reduces runs i, i + 32,
 //      ... with the merge-tree rule (adjacent leaves join at their split
 //      level: closed forms up to four leaves, a register shift-reduce beyond,
@@ -187,8 +189,65 @@ __device__ __forceinline__ void mw_merge_level(int L, const unsigned *__restrict
     }
 }
 
+// Sorts the warp's 32 * KPL keys in registers (bitonic network; key i =
+// lane * KPL + q), ascending.
+template <int KPL>
+__device__ __forceinline__ void warp_bitonic_keys(unsigned (&key)[KPL])
+{
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int k = 2; k <= 32 * KPL; k <<= 1) {
+#pragma unroll
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            if (j >= KPL) {
+                const int lj = j / KPL;
+#pragma unroll
+                for (int q = 0; q < KPL; q++) {
+                    const unsigned o = __shfl_xor_sync(kFull, key[q], lj);
+                    const int i = lane * KPL + q;
+                    const bool up = (i & k) == 0, lower = (i & j) == 0;
+                    key[q] = (lower == up) ? min(key[q], o) : max(key[q], o);
+                }
+            } else {
+#pragma unroll
+                for (int q = 0; q < KPL; q++) {
+                    if (q & j)
+                        continue;
+                    const int i = lane * KPL + q;
+                    const bool up = (i & k) == 0;
+                    const unsigned a = key[q], b = key[q | j];
+                    key[q] = up ? min(a, b) : max(a, b);
+                    key[q | j] = up ? max(a, b) : min(a, b);
+                }
+            }
+        }
+    }
+}
+
+// Sorts keys[0, F) (F <= 32 * KPL) of a warp in place through registers.
+template <int KPL>
+__device__ __forceinline__ void warp_sort_small(unsigned *keys, int F)
+{
+    const int lane = threadIdx.x & 31;
+    unsigned key[KPL];
+#pragma unroll
+    for (int q = 0; q < KPL; q++) {
+        const int i = lane * KPL + q;
+        key[q] = i < F ? keys[i] : 0xffffffffu;
+    }
+    __syncwarp();
+    warp_bitonic_keys<KPL>(key);
+#pragma unroll
+    for (int q = 0; q < KPL; q++) {
+        const int i = lane * KPL + q;
+        if (i < F)
+            keys[i] = key[q];
+    }
+    __syncwarp();
+}
+
 template <typename T, int MODE, int G>
-__global__ void __launch_bounds__(kMwThreads) k_mid_warp(CsrDev A, CsrDev B, PlanDev P,
+__global__ void __launch_bounds__(kMwThreads, 2) k_mid_warp(CsrDev A, CsrDev B, PlanDev P,
                                                          const int *crpt, int *ccol, T *cval)
 {
     using S = MwShape<G>;
@@ -267,11 +326,17 @@ __global__ void __launch_bounds__(kMwThreads) k_mid_warp(CsrDev A, CsrDev B, Pla
             }
         }
         grp_sync<G>(gid);
-        // 3. bottom-up merge of the sorted lists (ceil(log2 nl) levels, nl >= 2)
+        // 3. sort by key: small rows of one warp in registers (bitonic),
+        //    others by a bottom-up merge of the sorted lists (ceil(log2 nl)
+        //    levels, nl >= 2)
         unsigned *src = k0, *dst = k1;
         const int per = (F + NT - 1) / NT;
         const int p0 = min(t * per, F), p1 = min(p0 + per, F);
-        {
+        if (G == 1 && F <= 64) {
+            warp_sort_small<2>(src, F);
+        } else if (G == 1 && F <= 128) {
+            warp_sort_small<4>(src, F);
+        } else {
             const int levels = 32 - __clz(nl - 1);
             for (int lv = 0; lv < levels; lv++) {
                 mw_merge_level(lv, src, dst, loff, nl, p0, p1);
