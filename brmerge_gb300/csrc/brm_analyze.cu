@@ -1,4 +1,5 @@
 // brm_analyze.cu -- row analysis, device scans, Upper compaction, validation.
+#include <algorithm>
 #include <climits>
 
 #include "brm_common.cuh"
@@ -10,16 +11,55 @@ namespace brm {
 // Row analysis.  Replaces compute_flop (spgemm.h:31-56) and the flop-balanced
 // static row ranges (spgemm.h:496-503): on the GPU the balance comes from
 // binning rows by their product count and handing heavy rows out first.
-// One warp per row; each block appends its rows to the bin lists with one
+// A group of lanes per row; each block appends its rows to the bin lists with one
 // global atomic per bin.
 // ---------------------------------------------------------------------------
 constexpr int kAnaThreads = 256;
-constexpr int kAnaRowsPerWarp = 2;
+constexpr int kAnaRowsPerGroup = 2;
 
+// Reductions over a group of TW lanes (TW a power of two <= 32, the group
+// aligned in the warp); `gm` is the group's lane mask.
+template <int TW, typename T>
+__device__ __forceinline__ T grp_sum(T v, unsigned gm)
+{
+#pragma unroll
+    for (int o = TW / 2; o > 0; o >>= 1)
+        v += __shfl_xor_sync(gm, v, o);
+    return v;
+}
+template <int TW, typename T>
+__device__ __forceinline__ T grp_max(T v, unsigned gm)
+{
+#pragma unroll
+    for (int o = TW / 2; o > 0; o >>= 1) {
+        const T n = __shfl_xor_sync(gm, v, o);
+        v = n > v ? n : v;
+    }
+    return v;
+}
+template <int TW, typename T>
+__device__ __forceinline__ T grp_min(T v, unsigned gm)
+{
+#pragma unroll
+    for (int o = TW / 2; o > 0; o >>= 1) {
+        const T n = __shfl_xor_sync(gm, v, o);
+        v = n < v ? n : v;
+    }
+    return v;
+}
+
+// A group of TW lanes per row (TW = 8 when rows are short, 32 otherwise),
+// kAnaRowsPerGroup rows per group.  With TW = 8, rows of more than
+// kAnaLongK entries are listed and left to a second, warp-wide pass
+// (LISTED: the rows are P.longk_rows[0 .. n_longk)).
+constexpr int kAnaLongK = 64;
+
+template <int TW, bool LISTED>
 __global__ void __launch_bounds__(kAnaThreads) k_analyze(CsrDev A, CsrDev B, PlanDev P)
 {
     constexpr int NW = kAnaThreads / 32;
-    constexpr int RPB = NW * kAnaRowsPerWarp;
+    constexpr int NGR = kAnaThreads / TW;  // groups per block
+    constexpr int RPB = NGR * kAnaRowsPerGroup;
     __shared__ int s_cnt[kNumBins];
     __shared__ int s_base[kNumBins];
     __shared__ int s_bin[RPB];
@@ -27,23 +67,34 @@ __global__ void __launch_bounds__(kAnaThreads) k_analyze(CsrDev A, CsrDev B, Pla
     __shared__ unsigned long long s_flop[NW];
     __shared__ int s_maxk[NW];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int gl = threadIdx.x & (TW - 1);    // lane in the group
+    const int grp = threadIdx.x / TW;         // group in the block
+    const unsigned gm = TW == 32 ? kFull : (((1u << TW) - 1u) << (lane & ~(TW - 1)));
     if (threadIdx.x < kNumBins)
         s_cnt[threadIdx.x] = 0;
     __syncthreads();
     const int M = A.M, K = B.M;
+    const int nrows = LISTED ? P.cnt->n_longk : M;
     const int row0 = blockIdx.x * RPB;
-    unsigned long long wflop = 0;
-    int wmaxk = 0;
-    for (int r = 0; r < kAnaRowsPerWarp; r++) {
-        const int slot = w * kAnaRowsPerWarp + r;
-        const int row = row0 + slot;
-        if (row >= M) {
-            if (lane == 0)
+    unsigned long long gflop = 0;
+    int gmaxk = 0;
+    for (int r = 0; r < kAnaRowsPerGroup; r++) {
+        const int slot = grp * kAnaRowsPerGroup + r;
+        if (row0 + slot >= nrows) {
+            if (gl == 0)
                 s_bin[slot] = -1;
             continue;
         }
+        const int row = LISTED ? P.longk_rows[row0 + slot] : row0 + slot;
         int a0 = A.rpt[row];
         int a1 = A.rpt[row + 1];
+        if (TW < 32 && a1 - a0 > kAnaLongK && a0 >= 0 && a1 <= A.nnz) {
+            if (gl == 0) {
+                P.longk_rows[atomicAdd(&P.cnt->n_longk, 1)] = row;
+                s_bin[slot] = -1;
+            }
+            continue;
+        }
         long long f = 0;
         int nl = 0, leaf = -1;
         bool bad = false;
@@ -51,31 +102,50 @@ __global__ void __launch_bounds__(kAnaThreads) k_analyze(CsrDev A, CsrDev B, Pla
             bad = true;
             a0 = a1 = 0;
         }
-        for (int j = a0 + lane; j < a1; j += 32) {
-            int b = A.col[j];
-            int len = 0, bs = 0;
-            if ((unsigned)b < (unsigned)K) {
-                bs = B.rpt[b];
-                len = B.rpt[b + 1] - bs;
-            } else {
-                bad = true;
+        // four entries a lane in flight (long rows on narrow groups)
+        for (int jb = a0 + gl; jb < a1; jb += 4 * TW) {
+            int b[4], bs[4], be[4];
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                const int j = jb + u * TW;
+                b[u] = j < a1 ? A.col[j] : -1;
             }
-            P.abs[j] = bs;
-            P.alen[j] = len;
-            f += len;
-            if (len > 0) {
-                nl++;
-                leaf = j - a0;
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                const int j = jb + u * TW;
+                bs[u] = be[u] = 0;
+                if (j < a1) {
+                    if ((unsigned)b[u] < (unsigned)K) {
+                        bs[u] = B.rpt[b[u]];
+                        be[u] = B.rpt[b[u] + 1];
+                    } else {
+                        bad = true;
+                    }
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                const int j = jb + u * TW;
+                if (j < a1) {
+                    const int len = be[u] - bs[u];
+                    P.abs[j] = bs[u];
+                    P.alen[j] = len;
+                    f += len;
+                    if (len > 0) {
+                        nl++;
+                        leaf = max(leaf, j - a0);
+                    }
+                }
             }
         }
-        f = warp_sum(f);
-        nl = warp_sum(nl);
-        leaf = warp_max(leaf);
-        bad = __any_sync(kFull, bad);
+        f = grp_sum<TW>(f, gm);
+        nl = grp_sum<TW>(nl, gm);
+        leaf = grp_max<TW>(leaf, gm);
+        bad = (__ballot_sync(gm, bad) & gm) != 0u;
         const bool ovf = f > INT_MAX;
         if (ovf)
             f = INT_MAX;
-        // row class (f, nl, a0, a1 are warp-uniform)
+        // row class (f, nl, a0, a1 are uniform in the group)
         int bin;
         if (f == 0)
             bin = kBinEmpty;
@@ -95,17 +165,31 @@ __global__ void __launch_bounds__(kAnaThreads) k_analyze(CsrDev A, CsrDev B, Pla
             // column range of the row for the segment planning and the warp
             // mid rows' keys: the first and last column of every nonempty list
             int mn = INT_MAX, mx = -1;
-            for (int j = a0 + lane; j < a1; j += 32) {
-                const int len = P.alen[j];
-                if (len > 0) {
-                    const int bs = P.abs[j];
-                    mn = min(mn, B.col[bs]);
-                    mx = max(mx, B.col[bs + len - 1]);
+            for (int jb = a0 + gl; jb < a1; jb += 4 * TW) {
+                int c0[4], c1[4];
+#pragma unroll
+                for (int u = 0; u < 4; u++) {
+                    const int j = jb + u * TW;
+                    c0[u] = INT_MAX;
+                    c1[u] = -1;
+                    if (j < a1) {
+                        const int len = P.alen[j];
+                        if (len > 0) {
+                            const int bs = P.abs[j];
+                            c0[u] = B.col[bs];
+                            c1[u] = B.col[bs + len - 1];
+                        }
+                    }
+                }
+#pragma unroll
+                for (int u = 0; u < 4; u++) {
+                    mn = min(mn, c0[u]);
+                    mx = max(mx, c1[u]);
                 }
             }
-            mn = warp_min(mn);
-            mx = warp_max(mx);
-            if (lane == 0)
+            mn = grp_min<TW>(mn, gm);
+            mx = grp_max<TW>(mx, gm);
+            if (gl == 0)
                 P.crange[row] = make_int2(mn, mx);
             if ((bin == kBinMidWarp && (long long)mx - mn >= (1ll << kMwRangeBits)) ||
                 (bin == kBinMidGroup && (long long)mx - mn >= (1ll << kMgRangeBits)))
@@ -113,7 +197,7 @@ __global__ void __launch_bounds__(kAnaThreads) k_analyze(CsrDev A, CsrDev B, Pla
             if (bin == kBinHeavy && a1 - a0 > kSegMaxK)
                 bin = kBinMid;
         }
-        if (lane == 0) {
+        if (gl == 0) {
             if (bad)
                 atomicOr(&P.cnt->err, kErrBadInput);
             if (ovf)
@@ -139,13 +223,18 @@ __global__ void __launch_bounds__(kAnaThreads) k_analyze(CsrDev A, CsrDev B, Pla
             }
             s_bin[slot] = bin;
             s_idx[slot] = (bin < 0 || bin == kBinEmpty || bin == kBinBatch) ? 0 : atomicAdd(&s_cnt[bin], 1);
-            wflop += (unsigned long long)f;
-            wmaxk = max(wmaxk, a1 - a0);
+            gflop += (unsigned long long)f;
+            gmaxk = max(gmaxk, a1 - a0);
         }
     }
-    if (lane == 0) {
-        s_flop[w] = wflop;
-        s_maxk[w] = wmaxk;
+    // per warp: the groups' totals (held by their first lanes)
+    {
+        unsigned long long wf = grp_sum<32>(gflop, kFull);
+        int wk = grp_max<32>(gmaxk, kFull);
+        if (lane == 0) {
+            s_flop[w] = wf;
+            s_maxk[w] = wk;
+        }
     }
     __syncthreads();
     if (threadIdx.x < kNumBins)
@@ -166,7 +255,8 @@ __global__ void __launch_bounds__(kAnaThreads) k_analyze(CsrDev A, CsrDev B, Pla
     for (int slot = threadIdx.x; slot < RPB; slot += kAnaThreads) {
         int bin = s_bin[slot];
         if (bin > kBinEmpty && bin != kBinBatch)
-            P.rows[(size_t)bin * M + s_base[bin] + s_idx[slot]] = row0 + slot;
+            P.rows[(size_t)bin * M + s_base[bin] + s_idx[slot]] =
+                LISTED ? P.longk_rows[row0 + slot] : row0 + slot;
     }
 }
 
@@ -174,9 +264,19 @@ void launch_analyze(const CsrDev &A, const CsrDev &B, const PlanDev &P, cudaStre
 {
     if (A.M <= 0)
         return;
-    constexpr int RPB = (kAnaThreads / 32) * kAnaRowsPerWarp;
-    int grid = (A.M + RPB - 1) / RPB;
-    k_analyze<<<grid, kAnaThreads, 0, s>>>(A, B, P);
+    constexpr int RPB32 = (kAnaThreads / 32) * kAnaRowsPerGroup;
+    // eight lanes a row when rows average at most 12 entries; the few long
+    // rows then go to a warp-wide pass over their list (at most all rows)
+    if ((long long)A.nnz <= 12ll * A.M) {
+        constexpr int RPB = (kAnaThreads / 8) * kAnaRowsPerGroup;
+        k_analyze<8, false><<<(A.M + RPB - 1) / RPB, kAnaThreads, 0, s>>>(A, B, P);
+        count_launch();
+        const long long most = std::min<long long>(A.M, (long long)A.nnz / (kAnaLongK + 1));
+        const int g = (int)std::max<long long>(1, (most + RPB32 - 1) / RPB32);
+        k_analyze<32, true><<<g, kAnaThreads, 0, s>>>(A, B, P);
+    } else {
+        k_analyze<32, false><<<(A.M + RPB32 - 1) / RPB32, kAnaThreads, 0, s>>>(A, B, P);
+    }
     count_launch();
 }
 

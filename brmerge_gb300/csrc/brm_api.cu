@@ -154,6 +154,7 @@ size_t workspace_bytes(int M)
     b += a256(8 * (m + 1));                 // mid_pre
     b += a256(4 * m);                       // mw_flop
     b += a256(8 * (m + 1));                 // mw_pre
+    b += a256(4 * m);                       // longk_rows
     b += a256(4 * (m + 1));                 // batch_start
     b += a256(8 * m);                       // seg_base
     b += a256(4 * m);                       // seg_n
@@ -199,6 +200,7 @@ int ensure_workspace(brm_context ctx, int M)
     P.mid_pre = (long long *)take(8 * (m + 1));
     P.mw_flop = (int *)take(4 * m);
     P.mw_pre = (long long *)take(8 * (m + 1));
+    P.longk_rows = (int *)take(4 * m);
     P.batch_start = (int *)take(4 * (m + 1));
     P.seg_base = (unsigned long long *)take(8 * m);
     P.seg_n = (int *)take(4 * m);

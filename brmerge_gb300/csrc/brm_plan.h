@@ -103,7 +103,7 @@ struct Counters {
     int n_seg;         // segments written by the planning
     int work_plan;     // dynamic row counter of the heavy-row planning
     int n_huge;        // heavy rows above kHugeFlop products (listed from the end)
-    int pad;
+    int n_longk;       // rows the narrow analysis left to the warp-wide pass
     // long columns of the segment kernel handed to the column reducer:
     // (columns << 40) | elements reserved so far
     unsigned long long long_used;
@@ -169,6 +169,7 @@ struct PlanDev {
     long long *mid_pre;    // [M+1] exclusive scan of mid_flop
     int *mw_flop;          // [M] products of warp mid rows, 0 for other rows
     long long *mw_pre;     // [M+1] exclusive scan of mw_flop (one-call scratch after mid_pre[M])
+    int *longk_rows;       // [M] rows with many A entries, analysed by whole warps
     int *batch_start;      // [M+1] first row of each mid batch
     unsigned long long *seg_base;  // [M] first descriptor slot of each heavy row
     int *seg_n;            // [M] segments of each heavy row (0: not segmented)
