@@ -625,18 +625,21 @@ __global__ void __launch_bounds__(256) k_mid_compact(PlanDev P, int M, const int
     // batches) the batched mid rows by a sweep over the rows
     const int nw1 = P.cnt->bin_count[kBinMidWarp];
     const int nw4 = P.cnt->bin_count[kBinMidGroup];
+    const int nwt = P.cnt->bin_count[kBinMidTile];
+    const int nlist = nw1 + nw4 + nwt;
     const int nsweep = P.cnt->n_batch > 0 ? r1 - P.r_lo : 0;
-    for (int it = gw; it < nw1 + nw4 + nsweep; it += nwarps) {
+    for (int it = gw; it < nlist + nsweep; it += nwarps) {
         int row;
         long long src;
-        if (it < nw1 + nw4) {
-            row = it < nw1 ? P.rows[(size_t)kBinMidWarp * M + it]
-                           : P.rows[(size_t)kBinMidGroup * M + (it - nw1)];
+        if (it < nlist) {
+            row = it < nw1        ? P.rows[(size_t)kBinMidWarp * M + it]
+                  : it < nw1 + nw4 ? P.rows[(size_t)kBinMidGroup * M + (it - nw1)]
+                                  : P.rows[(size_t)kBinMidTile * M + (it - nw1 - nw4)];
             if (row < P.r_lo || row >= r1)
                 continue;
             src = P.mid_pre[M] + P.mw_pre[row];
         } else {
-            row = P.r_lo + (it - nw1 - nw4);
+            row = P.r_lo + (it - nlist);
             if (P.mid_flop[row] == 0)
                 continue;
             src = P.mid_pre[row];

@@ -398,6 +398,216 @@ __global__ void __launch_bounds__(kMwThreads, 2) k_mid_warp(CsrDev A, CsrDev B, 
     }
 }
 
+// ---------------------------------------------------------------------------
+// Tile rows: at most kMtF products, half a warp (16 lanes) each, four keys a
+// lane sorted by a bitonic network that stays inside the half warp, so a
+// warp works on two rows at once.
+// ---------------------------------------------------------------------------
+constexpr int kMtTW = 16;                 // lanes per row
+constexpr int kMtKPL = kMtF / kMtTW;      // keys per lane
+constexpr int kMtIdx = 6;                 // product index bits (kMtF = 64)
+static_assert(kMtF <= (1 << kMtIdx) && kMtRangeBits + kMtIdx <= 32, "tile keys are 32-bit");
+
+struct MidTileLayout {
+    static constexpr size_t o_key = 0;                            // sorted keys
+    static constexpr size_t o_head = o_key + kMtF * 4;             // run starts, + 1
+    static constexpr size_t o_lbs = o_head + (kMtF + 1) * 4;       // list B starts
+    static constexpr size_t o_loff = o_lbs + kMtF * 4;             // list product offsets
+    static constexpr size_t o_plist = o_loff + mid_a16((kMtF + 1) * 2);
+    static constexpr size_t o_lleaf = o_plist + kMtF;
+    static constexpr size_t per_tile = mid_a16(o_lleaf + kMtF);
+};
+
+template <typename T, int MODE>
+__global__ void __launch_bounds__(kMwThreads, 2) k_mid_tile(CsrDev A, CsrDev B, PlanDev P,
+                                                         const int *crpt, int *ccol, T *cval)
+{
+    constexpr int TW = kMtTW, KPL = kMtKPL, IDX = kMtIdx;
+    __shared__ __align__(16) unsigned char smem[(kMwThreads / TW) * MidTileLayout::per_tile];
+    const int lane = threadIdx.x & 31;
+    const int lt = lane & (TW - 1);
+    const int tb = lane & ~(TW - 1);                      // tile's first lane
+    const unsigned gm = ((1u << TW) - 1u) << tb;          // tile's lanes
+    const unsigned ltm = (1u << lt) - 1u;                 // tile lanes below this one
+    const int tile = threadIdx.x / TW;
+    unsigned char *ws = smem + (size_t)tile * MidTileLayout::per_tile;
+    unsigned *skey = (unsigned *)(ws + MidTileLayout::o_key);
+    unsigned *shead = (unsigned *)(ws + MidTileLayout::o_head);
+    int *lbs = (int *)(ws + MidTileLayout::o_lbs);
+    unsigned short *loff = (unsigned short *)(ws + MidTileLayout::o_loff);
+    unsigned char *plist = ws + MidTileLayout::o_plist;
+    unsigned char *lleaf = ws + MidTileLayout::o_lleaf;
+    const int M = A.M;
+    const int n = P.cnt->bin_count[kBinMidTile];
+    const int *rows = P.rows + (size_t)kBinMidTile * M;
+    const int *__restrict__ bcol = B.col;
+    const T *__restrict__ bval = (const T *)B.val;
+    const T *__restrict__ aval = (const T *)A.val;
+    const int t0 = blockIdx.x * (kMwThreads / TW) + tile;
+    const int nt = gridDim.x * (kMwThreads / TW);
+    // both tiles of a warp run the same number of iterations, so the sort
+    // network (full-warp shuffles) always has every lane
+    for (int itb = t0 - (tile & 1); itb < n; itb += nt) {
+        const int it = itb + (tile & 1);
+        const bool live = it < n;
+        const int row = live ? rows[it] : 0;
+        const bool act = live && row >= P.r_lo && row < P.r_hi;
+        int a0 = 0, k = 0, cmin = 0;
+        if (act) {
+            a0 = A.rpt[row];
+            k = A.rpt[row + 1] - a0;
+            cmin = P.crange[row].x;
+        }
+        // 1. nonempty lists in leaf order
+        int nl = 0, F = 0;
+        for (int jb = 0; jb < k; jb += TW) {
+            const int j = jb + lt;
+            const int len = j < k ? P.alen[a0 + j] : 0;
+            const unsigned nem = (__ballot_sync(gm, len > 0) >> tb) & ((1u << TW) - 1u);
+            int inc = len;
+#pragma unroll
+            for (int o = 1; o < TW; o <<= 1) {
+                const int x = __shfl_up_sync(gm, inc, o, TW);
+                if (lt >= o)
+                    inc += x;
+            }
+            const int tot = __shfl_sync(gm, inc, TW - 1, TW);
+            if (len > 0 && F + inc <= kMtF) {
+                const int li = nl + __popc(nem & ltm);
+                loff[li] = (unsigned short)(F + inc - len);
+                lbs[li] = P.abs[a0 + j];
+                lleaf[li] = (unsigned char)j;
+            }
+            nl += __popc(nem);
+            F += tot;
+        }
+        const bool ok = act && F <= kMtF && nl >= 1;
+        if (act && !ok && lt == 0)
+            atomicOr(&P.cnt->err, kErrWindowOverflow);  // the analysis bins prevent this
+        if (lt == 0 && ok)
+            loff[nl] = (unsigned short)F;
+        __syncwarp(gm);
+        // 2. keys into registers: key q of lane lt is product lt * KPL + q
+        unsigned key[KPL];
+#pragma unroll
+        for (int q = 0; q < KPL; q++) {
+            const int i = lt * KPL + q;
+            key[q] = 0xffffffffu;
+            if (ok && i < F) {
+                int lo = 0, hi = nl - 1;
+                while (lo < hi) {
+                    const int m = (lo + hi + 1) >> 1;
+                    if (loff[m] <= i)
+                        lo = m;
+                    else
+                        hi = m - 1;
+                }
+                const int c = bcol[lbs[lo] + (i - loff[lo])];
+                key[q] = ((unsigned)(c - cmin) << IDX) | (unsigned)i;
+                plist[i] = (unsigned char)lo;
+            }
+        }
+        // 3. bitonic sort of the tile's TW * KPL keys (partners stay in the tile)
+#pragma unroll
+        for (int kk = 2; kk <= TW * KPL; kk <<= 1) {
+#pragma unroll
+            for (int j = kk >> 1; j > 0; j >>= 1) {
+                if (j >= KPL) {
+                    const int lj = j / KPL;
+#pragma unroll
+                    for (int q = 0; q < KPL; q++) {
+                        const unsigned o = __shfl_xor_sync(kFull, key[q], lj);
+                        const int i = lt * KPL + q;
+                        const bool up = (i & kk) == 0, lower = (i & j) == 0;
+                        key[q] = (lower == up) ? min(key[q], o) : max(key[q], o);
+                    }
+                } else {
+#pragma unroll
+                    for (int q = 0; q < KPL; q++) {
+                        if (q & j)
+                            continue;
+                        const int i = lt * KPL + q;
+                        const bool up = (i & kk) == 0;
+                        const unsigned a = key[q], b = key[q | j];
+                        key[q] = up ? min(a, b) : max(a, b);
+                        key[q | j] = up ? max(a, b) : min(a, b);
+                    }
+                }
+            }
+        }
+        if (!ok)
+            continue;
+#pragma unroll
+        for (int q = 0; q < KPL; q++) {
+            const int i = lt * KPL + q;
+            if (i < F)
+                skey[i] = key[q];
+        }
+        __syncwarp(gm);
+        // 4. runs of one column (heads listed in order), lane i reduces runs
+        //    i, i + TW, ...
+        int nh = 0;
+#pragma unroll
+        for (int q = 0; q < KPL; q++) {
+            const int p = lt * KPL + q;
+            if (p < F)
+                nh += p == 0 || (skey[p] >> IDX) != (skey[p - 1] >> IDX);
+        }
+        int hx = nh;
+#pragma unroll
+        for (int o = 1; o < TW; o <<= 1) {
+            const int x = __shfl_up_sync(gm, hx, o, TW);
+            if (lt >= o)
+                hx += x;
+        }
+        const int len = __shfl_sync(gm, hx, TW - 1, TW);
+        hx -= nh;
+#pragma unroll
+        for (int q = 0; q < KPL; q++) {
+            const int p = lt * KPL + q;
+            if (p < F && (p == 0 || (skey[p] >> IDX) != (skey[p - 1] >> IDX)))
+                shead[hx++] = (unsigned)p;
+        }
+        if (lt == 0)
+            shead[len] = (unsigned)F;
+        __syncwarp(gm);
+        if (MODE == kMwSymbolic) {
+            if (lt == 0)
+                P.nnz[row] = len;
+            __syncwarp(gm);
+            continue;
+        }
+        long long base;
+        if (MODE == kMwPrecise) {
+            base = crpt[row];
+            if (lt == 0 && len != crpt[row + 1] - crpt[row])
+                atomicOr(&P.cnt->err, kErrNnzMismatch);
+        } else if (MODE == kMwUpper) {
+            base = P.scan_flop[row];
+        } else {
+            base = P.mid_pre[M] + P.mw_pre[row];
+        }
+        if ((MODE == kMwUpper || MODE == kMwScratch) && lt == 0)
+            P.nnz[row] = len;
+        const T *arow = aval + a0;
+        constexpr unsigned imask = (1u << IDX) - 1u;
+        for (int h = lt; h < len; h += TW) {
+            const int p = (int)shead[h], m = (int)shead[h + 1] - p;
+            const unsigned *run = skey + p;
+            auto leaf = [&](int i) { return (int)lleaf[plist[run[i] & imask]]; };
+            auto val = [&](int i) {
+                const int e = (int)(run[i] & imask);
+                const int j = plist[e];
+                return vmul(arow[lleaf[j]], bval[lbs[j] + (e - loff[j])]);
+            };
+            const T v = k <= 32 ? mw_run_value<T, 6>(m, leaf, val) : mw_run_value<T, 9>(m, leaf, val);
+            ccol[base + h] = cmin + (int)(run[0] >> IDX);
+            cval[base + h] = v;
+        }
+        __syncwarp(gm);
+    }
+}
+
 template <typename T, int MODE, int G>
 inline void launch_mid_group(const CsrDev &A, const CsrDev &B, const PlanDev &P, const int *crpt,
                              int *ccol, T *cval, int num_sms, cudaStream_t s)
@@ -409,13 +619,15 @@ inline void launch_mid_group(const CsrDev &A, const CsrDev &B, const PlanDev &P,
     count_launch();
 }
 
-// The warp rows and the 4-warp group rows of one mode.
+// The warp rows, the four-warp group rows and the tile rows of one mode.
 template <typename T, int MODE>
 inline void launch_mid_warp(const CsrDev &A, const CsrDev &B, const PlanDev &P, const int *crpt,
                             int *ccol, T *cval, int num_sms, cudaStream_t s)
 {
     launch_mid_group<T, MODE, 1>(A, B, P, crpt, ccol, cval, num_sms, s);
     launch_mid_group<T, MODE, 4>(A, B, P, crpt, ccol, cval, num_sms, s);
+    k_mid_tile<T, MODE><<<num_sms * 4, kMwThreads, 0, s>>>(A, B, P, crpt, ccol, cval);
+    count_launch();
 }
 
 }  // namespace brm

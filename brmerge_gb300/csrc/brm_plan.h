@@ -40,6 +40,8 @@ constexpr int kMidMaxRows = kMidCap / (kWarpMaxFlop + 1) + 2;
 // segmented heavy rows.
 constexpr int kMwF = 768;
 constexpr int kMwRangeBits = 22;
+constexpr int kMtF = 64;          // tile rows: at most 64 products, half a warp each
+constexpr int kMtRangeBits = 26;
 constexpr int kMgF = 3072;
 constexpr int kMgRangeBits = 20;
 
@@ -80,7 +82,8 @@ enum RowBin : int {
     kBinBatch = 5,  // batched mid-row kernels (no row list: row-order batches)
     kBinMidWarp = 6,  // one warp per row (brm_midwarp.cuh)
     kBinMidGroup = 7, // four warps per row (brm_midwarp.cuh)
-    kNumBins = 8,
+    kBinMidTile = 8,  // half a warp per row, products sorted in registers (brm_midwarp.cuh)
+    kNumBins = 9,
 };
 
 // Device counters (one struct in device memory, zeroed per phase).
