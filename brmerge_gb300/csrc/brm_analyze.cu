@@ -154,14 +154,18 @@ __global__ void __launch_bounds__(kAnaThreads) k_analyze(CsrDev A, CsrDev B, Pla
         else if (f <= kWarpMaxFlop)
             bin = kBinWarp;
         else if (f <= kMgF && a1 - a0 <= kMidMaxK)  // unless the column range is too wide
-            bin = f <= kMtF ? kBinMidTile : f <= kMwF ? kBinMidWarp : kBinMidGroup;
+            bin = f <= kMtF    ? kBinMidTile
+                  : f <= kMt2F ? kBinMidTile2
+                  : f <= kMwF  ? kBinMidWarp
+                               : kBinMidGroup;
         else if (f <= P.mid_limit && 2 * nl <= P.mid_limit && a1 - a0 <= kMidMaxK)
             bin = kBinBatch;
         else if (a1 - a0 <= kSegMaxK)
             bin = kBinHeavy;  // segmented (brm_seg.cuh)
         else
             bin = kBinMid;    // row CTA / spill path
-        if (bin == kBinHeavy || bin == kBinMidWarp || bin == kBinMidGroup || bin == kBinMidTile) {
+        if (bin == kBinHeavy || bin == kBinMidWarp || bin == kBinMidGroup || bin == kBinMidTile ||
+            bin == kBinMidTile2) {
             // column range of the row for the segment planning and the warp
             // mid rows' keys: the first and last column of every nonempty list
             int mn = INT_MAX, mx = -1;
@@ -193,7 +197,8 @@ __global__ void __launch_bounds__(kAnaThreads) k_analyze(CsrDev A, CsrDev B, Pla
                 P.crange[row] = make_int2(mn, mx);
             if ((bin == kBinMidWarp && (long long)mx - mn >= (1ll << kMwRangeBits)) ||
                 (bin == kBinMidGroup && (long long)mx - mn >= (1ll << kMgRangeBits)) ||
-                (bin == kBinMidTile && (long long)mx - mn >= (1ll << kMtRangeBits)))
+                ((bin == kBinMidTile || bin == kBinMidTile2) &&
+                 (long long)mx - mn >= (1ll << kMtRangeBits)))
                 bin = (f <= P.mid_limit && 2 * nl <= P.mid_limit) ? kBinBatch : kBinHeavy;
             if (bin == kBinHeavy && a1 - a0 > kSegMaxK)
                 bin = kBinMid;
@@ -208,7 +213,10 @@ __global__ void __launch_bounds__(kAnaThreads) k_analyze(CsrDev A, CsrDev B, Pla
                 P.seg_base[row] = atomicAdd(&P.cnt->seg_cap, seg_bound(f, B.N, P.seg_cut));
             P.mid_flop[row] = bin == kBinBatch ? max((int)f, 2 * nl) : 0;  // batch weight
             P.mw_flop[row] =
-                (bin == kBinMidWarp || bin == kBinMidGroup || bin == kBinMidTile) ? (int)f : 0;
+                (bin == kBinMidWarp || bin == kBinMidGroup || bin == kBinMidTile ||
+                 bin == kBinMidTile2)
+                    ? (int)f
+                    : 0;
             P.spill[row] = 0;
             if (bin == kBinEmpty)
                 P.nnz[row] = 0;

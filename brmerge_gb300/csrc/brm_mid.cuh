@@ -626,15 +626,17 @@ __global__ void __launch_bounds__(256) k_mid_compact(PlanDev P, int M, const int
     const int nw1 = P.cnt->bin_count[kBinMidWarp];
     const int nw4 = P.cnt->bin_count[kBinMidGroup];
     const int nwt = P.cnt->bin_count[kBinMidTile];
-    const int nlist = nw1 + nw4 + nwt;
+    const int nwt2 = P.cnt->bin_count[kBinMidTile2];
+    const int nlist = nw1 + nw4 + nwt + nwt2;
     const int nsweep = P.cnt->n_batch > 0 ? r1 - P.r_lo : 0;
     for (int it = gw; it < nlist + nsweep; it += nwarps) {
         int row;
         long long src;
         if (it < nlist) {
-            row = it < nw1        ? P.rows[(size_t)kBinMidWarp * M + it]
-                  : it < nw1 + nw4 ? P.rows[(size_t)kBinMidGroup * M + (it - nw1)]
-                                  : P.rows[(size_t)kBinMidTile * M + (it - nw1 - nw4)];
+            row = it < nw1              ? P.rows[(size_t)kBinMidWarp * M + it]
+                  : it < nw1 + nw4       ? P.rows[(size_t)kBinMidGroup * M + (it - nw1)]
+                  : it < nw1 + nw4 + nwt ? P.rows[(size_t)kBinMidTile * M + (it - nw1 - nw4)]
+                                         : P.rows[(size_t)kBinMidTile2 * M + (it - nw1 - nw4 - nwt)];
             if (row < P.r_lo || row >= r1)
                 continue;
             src = P.mid_pre[M] + P.mw_pre[row];

@@ -403,43 +403,61 @@ __global__ void __launch_bounds__(kMwThreads, 2) k_mid_warp(CsrDev A, CsrDev B, 
 // lane sorted by a bitonic network that stays inside the half warp, so a
 // warp works on two rows at once.
 // ---------------------------------------------------------------------------
-constexpr int kMtTW = 16;                 // lanes per row
-constexpr int kMtKPL = kMtF / kMtTW;      // keys per lane
-constexpr int kMtIdx = 6;                 // product index bits (kMtF = 64)
-static_assert(kMtF <= (1 << kMtIdx) && kMtRangeBits + kMtIdx <= 32, "tile keys are 32-bit");
+constexpr int kMtTW = 16;  // lanes per row
 
+// Shape of a tile class: KPL keys a lane, FM = 16 * KPL products at most.
+template <int KPL>
+struct MtShape;
+template <>
+struct MtShape<4> {
+    static constexpr int FM = kMtF;
+    static constexpr int IDX = 6;
+    static constexpr int BIN = kBinMidTile;
+};
+template <>
+struct MtShape<8> {
+    static constexpr int FM = kMt2F;
+    static constexpr int IDX = 7;
+    static constexpr int BIN = kBinMidTile2;
+};
+static_assert(kMtF == kMtTW * 4 && kMt2F == kMtTW * 8, "tile shapes");
+static_assert(kMtRangeBits + 7 <= 32, "tile keys are 32-bit");
+
+template <int FM>
 struct MidTileLayout {
     static constexpr size_t o_key = 0;                            // sorted keys
-    static constexpr size_t o_head = o_key + kMtF * 4;             // run starts, + 1
-    static constexpr size_t o_lbs = o_head + (kMtF + 1) * 4;       // list B starts
-    static constexpr size_t o_loff = o_lbs + kMtF * 4;             // list product offsets
-    static constexpr size_t o_plist = o_loff + mid_a16((kMtF + 1) * 2);
-    static constexpr size_t o_lleaf = o_plist + kMtF;
-    static constexpr size_t per_tile = mid_a16(o_lleaf + kMtF);
+    static constexpr size_t o_head = o_key + FM * 4;               // run starts, + 1
+    static constexpr size_t o_lbs = o_head + (FM + 1) * 4;         // list B starts
+    static constexpr size_t o_loff = o_lbs + FM * 4;               // list product offsets
+    static constexpr size_t o_plist = o_loff + mid_a16((FM + 1) * 2);
+    static constexpr size_t o_lleaf = o_plist + FM;
+    static constexpr size_t per_tile = mid_a16(o_lleaf + FM);
 };
 
-template <typename T, int MODE>
+template <typename T, int MODE, int KPL>
 __global__ void __launch_bounds__(kMwThreads, 2) k_mid_tile(CsrDev A, CsrDev B, PlanDev P,
                                                          const int *crpt, int *ccol, T *cval)
 {
-    constexpr int TW = kMtTW, KPL = kMtKPL, IDX = kMtIdx;
-    __shared__ __align__(16) unsigned char smem[(kMwThreads / TW) * MidTileLayout::per_tile];
+    using S = MtShape<KPL>;
+    using TL = MidTileLayout<S::FM>;
+    constexpr int TW = kMtTW, IDX = S::IDX, kMtF = S::FM;
+    extern __shared__ __align__(16) unsigned char smem[];
     const int lane = threadIdx.x & 31;
     const int lt = lane & (TW - 1);
     const int tb = lane & ~(TW - 1);                      // tile's first lane
     const unsigned gm = ((1u << TW) - 1u) << tb;          // tile's lanes
     const unsigned ltm = (1u << lt) - 1u;                 // tile lanes below this one
     const int tile = threadIdx.x / TW;
-    unsigned char *ws = smem + (size_t)tile * MidTileLayout::per_tile;
-    unsigned *skey = (unsigned *)(ws + MidTileLayout::o_key);
-    unsigned *shead = (unsigned *)(ws + MidTileLayout::o_head);
-    int *lbs = (int *)(ws + MidTileLayout::o_lbs);
-    unsigned short *loff = (unsigned short *)(ws + MidTileLayout::o_loff);
-    unsigned char *plist = ws + MidTileLayout::o_plist;
-    unsigned char *lleaf = ws + MidTileLayout::o_lleaf;
+    unsigned char *ws = smem + (size_t)tile * TL::per_tile;
+    unsigned *skey = (unsigned *)(ws + TL::o_key);
+    unsigned *shead = (unsigned *)(ws + TL::o_head);
+    int *lbs = (int *)(ws + TL::o_lbs);
+    unsigned short *loff = (unsigned short *)(ws + TL::o_loff);
+    unsigned char *plist = ws + TL::o_plist;
+    unsigned char *lleaf = ws + TL::o_lleaf;
     const int M = A.M;
-    const int n = P.cnt->bin_count[kBinMidTile];
-    const int *rows = P.rows + (size_t)kBinMidTile * M;
+    const int n = P.cnt->bin_count[S::BIN];
+    const int *rows = P.rows + (size_t)S::BIN * M;
     const int *__restrict__ bcol = B.col;
     const T *__restrict__ bval = (const T *)B.val;
     const T *__restrict__ aval = (const T *)A.val;
@@ -619,6 +637,17 @@ inline void launch_mid_group(const CsrDev &A, const CsrDev &B, const PlanDev &P,
     count_launch();
 }
 
+template <typename T, int MODE, int KPL>
+inline void launch_mid_tile(const CsrDev &A, const CsrDev &B, const PlanDev &P, const int *crpt,
+                            int *ccol, T *cval, int num_sms, cudaStream_t s)
+{
+    const size_t sm = (size_t)(kMwThreads / kMtTW) * MidTileLayout<MtShape<KPL>::FM>::per_tile;
+    cudaFuncSetAttribute(k_mid_tile<T, MODE, KPL>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)sm);
+    k_mid_tile<T, MODE, KPL><<<num_sms * 4, kMwThreads, sm, s>>>(A, B, P, crpt, ccol, cval);
+    count_launch();
+}
+
 // The warp rows, the four-warp group rows and the tile rows of one mode.
 template <typename T, int MODE>
 inline void launch_mid_warp(const CsrDev &A, const CsrDev &B, const PlanDev &P, const int *crpt,
@@ -626,8 +655,8 @@ inline void launch_mid_warp(const CsrDev &A, const CsrDev &B, const PlanDev &P, 
 {
     launch_mid_group<T, MODE, 1>(A, B, P, crpt, ccol, cval, num_sms, s);
     launch_mid_group<T, MODE, 4>(A, B, P, crpt, ccol, cval, num_sms, s);
-    k_mid_tile<T, MODE><<<num_sms * 4, kMwThreads, 0, s>>>(A, B, P, crpt, ccol, cval);
-    count_launch();
+    launch_mid_tile<T, MODE, 8>(A, B, P, crpt, ccol, cval, num_sms, s);
+    launch_mid_tile<T, MODE, 4>(A, B, P, crpt, ccol, cval, num_sms, s);
 }
 
 }  // namespace brm

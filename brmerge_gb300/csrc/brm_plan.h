@@ -41,7 +41,8 @@ constexpr int kMidMaxRows = kMidCap / (kWarpMaxFlop + 1) + 2;
 constexpr int kMwF = 768;
 constexpr int kMwRangeBits = 22;
 constexpr int kMtF = 64;          // tile rows: at most 64 products, half a warp each
-constexpr int kMtRangeBits = 26;
+constexpr int kMt2F = 128;        // second tile class: at most 128 products
+constexpr int kMtRangeBits = 25;
 constexpr int kMgF = 3072;
 constexpr int kMgRangeBits = 20;
 
@@ -83,7 +84,8 @@ enum RowBin : int {
     kBinMidWarp = 6,  // one warp per row (brm_midwarp.cuh)
     kBinMidGroup = 7, // four warps per row (brm_midwarp.cuh)
     kBinMidTile = 8,  // half a warp per row, products sorted in registers (brm_midwarp.cuh)
-    kNumBins = 9,
+    kBinMidTile2 = 9, // the same with twice the products
+    kNumBins = 10,
 };
 
 // Device counters (one struct in device memory, zeroed per phase).

@@ -380,10 +380,12 @@ def _rows_with_products(rng, targets, K, N, blen_lo=1, blen_hi=6, span=None):
 
 
 def test_mid_row_class_boundaries(ctx, oracle_mod):
-    """Rows of 33, 768, 769, 3072 and 3073 products (warp, group and
-    segmented classes on either side of each boundary)."""
+    """Rows on either side of every class boundary: 33, 64 / 65 and 128 / 129
+    (half-warp tiles), 768 / 769 (warp), 3072 / 3073 (four-warp group, then
+    segmented)."""
     rng = np.random.default_rng(41)
-    A, B = _rows_with_products(rng, [33, 767, 768, 769, 1500, 3071, 3072, 3073, 5000],
+    A, B = _rows_with_products(rng, [33, 64, 65, 128, 129, 767, 768, 769, 1500, 3071, 3072, 3073,
+                                     5000],
                                K=3000, N=20000, blen_lo=1, blen_hi=30)
     R = oracle_mod.precise(A, B)
     assert_same_csr(gpu_precise(ctx, A, B), R, "boundaries split")
