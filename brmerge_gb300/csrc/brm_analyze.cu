@@ -153,11 +153,12 @@ __global__ void __launch_bounds__(kAnaThreads) k_analyze(CsrDev A, CsrDev B, Pla
             bin = kBinCopy;
         else if (f <= kWarpMaxFlop)
             bin = kBinWarp;
-        else if (f <= kMgF && a1 - a0 <= kMidMaxK)  // unless the column range is too wide
+        else if (f <= kMg2F && a1 - a0 <= kMidMaxK)  // unless the column range is too wide
             bin = f <= kMtF    ? kBinMidTile
                   : f <= kMt2F ? kBinMidTile2
                   : f <= kMwF  ? kBinMidWarp
-                               : kBinMidGroup;
+                  : f <= kMgF  ? kBinMidGroup
+                               : kBinMidGroup2;
         else if (f <= P.mid_limit && 2 * nl <= P.mid_limit && a1 - a0 <= kMidMaxK)
             bin = kBinBatch;
         else if (a1 - a0 <= kSegMaxK)
@@ -165,7 +166,7 @@ __global__ void __launch_bounds__(kAnaThreads) k_analyze(CsrDev A, CsrDev B, Pla
         else
             bin = kBinMid;    // row CTA / spill path
         if (bin == kBinHeavy || bin == kBinMidWarp || bin == kBinMidGroup || bin == kBinMidTile ||
-            bin == kBinMidTile2) {
+            bin == kBinMidTile2 || bin == kBinMidGroup2) {
             // column range of the row for the segment planning and the warp
             // mid rows' keys: the first and last column of every nonempty list
             int mn = INT_MAX, mx = -1;
@@ -198,7 +199,8 @@ __global__ void __launch_bounds__(kAnaThreads) k_analyze(CsrDev A, CsrDev B, Pla
             if ((bin == kBinMidWarp && (long long)mx - mn >= (1ll << kMwRangeBits)) ||
                 (bin == kBinMidGroup && (long long)mx - mn >= (1ll << kMgRangeBits)) ||
                 ((bin == kBinMidTile || bin == kBinMidTile2) &&
-                 (long long)mx - mn >= (1ll << kMtRangeBits)))
+                 (long long)mx - mn >= (1ll << kMtRangeBits)) ||
+                (bin == kBinMidGroup2 && (long long)mx - mn >= (1ll << kMg2RangeBits)))
                 bin = (f <= P.mid_limit && 2 * nl <= P.mid_limit) ? kBinBatch : kBinHeavy;
             if (bin == kBinHeavy && a1 - a0 > kSegMaxK)
                 bin = kBinMid;
@@ -214,7 +216,7 @@ __global__ void __launch_bounds__(kAnaThreads) k_analyze(CsrDev A, CsrDev B, Pla
             P.mid_flop[row] = bin == kBinBatch ? max((int)f, 2 * nl) : 0;  // batch weight
             P.mw_flop[row] =
                 (bin == kBinMidWarp || bin == kBinMidGroup || bin == kBinMidTile ||
-                 bin == kBinMidTile2)
+                 bin == kBinMidTile2 || bin == kBinMidGroup2)
                     ? (int)f
                     : 0;
             P.spill[row] = 0;

@@ -627,7 +627,8 @@ __global__ void __launch_bounds__(256) k_mid_compact(PlanDev P, int M, const int
     const int nw4 = P.cnt->bin_count[kBinMidGroup];
     const int nwt = P.cnt->bin_count[kBinMidTile];
     const int nwt2 = P.cnt->bin_count[kBinMidTile2];
-    const int nlist = nw1 + nw4 + nwt + nwt2;
+    const int nw5 = P.cnt->bin_count[kBinMidGroup2];
+    const int nlist = nw1 + nw4 + nwt + nwt2 + nw5;
     const int nsweep = P.cnt->n_batch > 0 ? r1 - P.r_lo : 0;
     for (int it = gw; it < nlist + nsweep; it += nwarps) {
         int row;
@@ -636,7 +637,9 @@ __global__ void __launch_bounds__(256) k_mid_compact(PlanDev P, int M, const int
             row = it < nw1              ? P.rows[(size_t)kBinMidWarp * M + it]
                   : it < nw1 + nw4       ? P.rows[(size_t)kBinMidGroup * M + (it - nw1)]
                   : it < nw1 + nw4 + nwt ? P.rows[(size_t)kBinMidTile * M + (it - nw1 - nw4)]
-                                         : P.rows[(size_t)kBinMidTile2 * M + (it - nw1 - nw4 - nwt)];
+                  : it < nw1 + nw4 + nwt + nwt2
+                      ? P.rows[(size_t)kBinMidTile2 * M + (it - nw1 - nw4 - nwt)]
+                      : P.rows[(size_t)kBinMidGroup2 * M + (it - nw1 - nw4 - nwt - nwt2)];
             if (row < P.r_lo || row >= r1)
                 continue;
             src = P.mid_pre[M] + P.mw_pre[row];

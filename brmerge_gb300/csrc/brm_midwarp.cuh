@@ -34,13 +34,15 @@ namespace brm {
 
 enum MidWarpMode : int { kMwSymbolic = 0, kMwPrecise = 1, kMwUpper = 2, kMwScratch = 3 };
 
-// A group of G warps works on one row at a time: G = 1 for rows of at most
-// kMwF products, G = 4 (named barriers) up to kMgF.  Keys are (column -
-// cmin) << IDX | product index.
-template <int G>
+// Shapes (SID): a group of G warps works on one row at a time, GROUPS groups
+// a CTA.  SID 1: one warp, rows of at most kMwF products; SID 4: four warps
+// (named barriers) up to kMgF; SID 5: four warps up to kMg2F, two groups a
+// CTA.  Keys are (column - cmin) << IDX | product index.
+template <int SID>
 struct MwShape;
 template <>
 struct MwShape<1> {
+    static constexpr int G = 1;
     static constexpr int F = kMwF;
     static constexpr int IDX = 10;
     static constexpr int RANGE = kMwRangeBits;
@@ -49,21 +51,39 @@ struct MwShape<1> {
 };
 template <>
 struct MwShape<4> {
+    static constexpr int G = 4;
     static constexpr int F = kMgF;
     static constexpr int IDX = 12;
     static constexpr int RANGE = kMgRangeBits;
     static constexpr int GROUPS = 3;
     static constexpr int BIN = kBinMidGroup;
 };
-constexpr int kMwThreads = 384;  // both shapes: 12 x 1 and 3 x 4 warps
+template <>
+struct MwShape<5> {
+    static constexpr int G = 4;
+    static constexpr int F = kMg2F;
+    static constexpr int IDX = 13;
+    static constexpr int RANGE = kMg2RangeBits;
+    static constexpr int GROUPS = 2;
+    static constexpr int BIN = kBinMidGroup2;
+};
+constexpr int kMwThreads = 384;  // threads of the tile kernels
+template <int SID>
+constexpr int mw_threads()
+{
+    return MwShape<SID>::GROUPS * MwShape<SID>::G * 32;
+}
 static_assert(MwShape<1>::F <= (1 << MwShape<1>::IDX) && MwShape<1>::RANGE + MwShape<1>::IDX <= 32,
               "warp keys are 32-bit");
 static_assert(MwShape<4>::F <= (1 << MwShape<4>::IDX) && MwShape<4>::RANGE + MwShape<4>::IDX <= 32,
               "group keys are 32-bit");
+static_assert(MwShape<5>::F <= (1 << MwShape<5>::IDX) && MwShape<5>::RANGE + MwShape<5>::IDX <= 32,
+              "group keys are 32-bit");
 
-template <int G>
+template <int SID>
 struct MidWarpLayout {
-    static constexpr int FM = MwShape<G>::F;
+    static constexpr int G = MwShape<SID>::G;
+    static constexpr int FM = MwShape<SID>::F;
     // keys, merged back and forth between k0 and k1; the free one then lists
     // the runs (up to FM + 1 entries)
     static constexpr size_t o_k0 = 0;
@@ -74,7 +94,7 @@ struct MidWarpLayout {
     static constexpr size_t o_lleaf = o_lbs + (kMidMaxK + 1) * 4;
     static constexpr size_t o_gs = o_lleaf + mid_a16(kMidMaxK + 1);    // group scan scratch
     static constexpr size_t per_group = mid_a16(o_gs + 4 * (G + 1));
-    static constexpr size_t bytes = per_group * MwShape<G>::GROUPS;
+    static constexpr size_t bytes = per_group * MwShape<SID>::GROUPS;
 };
 
 template <int G>
@@ -246,12 +266,88 @@ __device__ __forceinline__ void warp_sort_small(unsigned *keys, int F)
     __syncwarp();
 }
 
-template <typename T, int MODE, int G>
-__global__ void __launch_bounds__(kMwThreads, 2) k_mid_warp(CsrDev A, CsrDev B, PlanDev P,
-                                                         const int *crpt, int *ccol, T *cval)
+// Values of the runs h = t, t + NT, ... of sorted keys (run h covers
+// key[head[h], head[h + 1])).  The runs are taken U at a time and the
+// products of runs of at most 4 are loaded before any is reduced, so that
+// several B gathers are in flight per thread; longer runs load as they
+// reduce.
+template <typename T, int NT, int IDX, int U>
+__device__ __forceinline__ void mw_reduce_runs(const unsigned *key, const unsigned *head, int len,
+                                               int t, int k, const unsigned char *plist,
+                                               const unsigned char *lleaf, const int *lbs,
+                                               const unsigned short *loff,
+                                               const T *__restrict__ arow,
+                                               const T *__restrict__ bval, int cmin, int *ccol,
+                                               T *cval)
 {
-    using S = MwShape<G>;
-    using L = MidWarpLayout<G>;
+    constexpr unsigned imask = (1u << IDX) - 1u;
+    for (int hb = t; hb < len; hb += U * NT) {
+        int p[U], m[U];
+        unsigned lf[U];  // leaves of the first 4 products, a byte each
+        T v[U][4];
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            const int h = hb + u * NT;
+            p[u] = h < len ? (int)head[h] : 0;
+            m[u] = h < len ? (int)head[h + 1] - p[u] : 0;
+        }
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            lf[u] = 0;
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                v[u][q] = T(0);
+                if (q < m[u] && m[u] <= 4) {
+                    const int e = (int)(key[p[u] + q] & imask);
+                    const int j = plist[e];
+                    const int l = lleaf[j];
+                    lf[u] |= (unsigned)l << (8 * q);
+                    v[u][q] = vmul(arow[l], bval[lbs[j] + (e - loff[j])]);
+                }
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            const int h = hb + u * NT;
+            if (h >= len)
+                break;
+            const unsigned *run = key + p[u];
+            T r;
+            if (m[u] == 1) {
+                r = v[u][0];
+            } else if (m[u] == 2) {
+                r = vadd(v[u][0], v[u][1]);
+            } else if (m[u] == 3) {
+                r = trie3((int)(lf[u] & 255u), (int)((lf[u] >> 8) & 255u),
+                          (int)((lf[u] >> 16) & 255u), v[u][0], v[u][1], v[u][2]);
+            } else if (m[u] == 4) {
+                r = trie4((int)(lf[u] & 255u), (int)((lf[u] >> 8) & 255u),
+                          (int)((lf[u] >> 16) & 255u), (int)(lf[u] >> 24), v[u][0], v[u][1],
+                          v[u][2], v[u][3]);
+            } else {
+                auto leaf = [&](int i) { return (int)lleaf[plist[run[i] & imask]]; };
+                auto val = [&](int i) {
+                    const int e = (int)(run[i] & imask);
+                    const int j = plist[e];
+                    return vmul(arow[lleaf[j]], bval[lbs[j] + (e - loff[j])]);
+                };
+                // leaves below 32 need at most 5 stack entries below the top
+                r = k <= 32 ? mw_run_value<T, 6>(m[u], leaf, val)
+                            : mw_run_value<T, 9>(m[u], leaf, val);
+            }
+            ccol[h] = cmin + (int)(run[0] >> IDX);
+            cval[h] = r;
+        }
+    }
+}
+
+template <typename T, int MODE, int SID>
+__global__ void __launch_bounds__(mw_threads<SID>(), 2) k_mid_warp(CsrDev A, CsrDev B, PlanDev P,
+                                                               const int *crpt, int *ccol, T *cval)
+{
+    using S = MwShape<SID>;
+    using L = MidWarpLayout<SID>;
+    constexpr int G = S::G;
     constexpr int NT = 32 * G;
     constexpr int IDX = S::IDX;
     extern __shared__ __align__(16) unsigned char smem[];
@@ -317,12 +413,28 @@ __global__ void __launch_bounds__(kMwThreads, 2) k_mid_warp(CsrDev A, CsrDev B, 
                     hi = m - 1;
             }
             int j = lo;
-            for (int e = t; e < F; e += NT) {
-                while (e >= loff[j + 1])
-                    j++;
-                const int c = bcol[lbs[j] + (e - loff[j])];
-                k0[e] = ((unsigned)(c - cmin) << IDX) | (unsigned)e;
-                plist[e] = (unsigned char)j;
+            constexpr int KU = 4;  // column loads in flight per thread
+            for (int eb = t; eb < F; eb += KU * NT) {
+                int c[KU], jj[KU];
+#pragma unroll
+                for (int u = 0; u < KU; u++) {
+                    const int e = eb + u * NT;
+                    c[u] = 0;
+                    if (e < F) {
+                        while (e >= loff[j + 1])
+                            j++;
+                        c[u] = bcol[lbs[j] + (e - loff[j])];
+                    }
+                    jj[u] = j;
+                }
+#pragma unroll
+                for (int u = 0; u < KU; u++) {
+                    const int e = eb + u * NT;
+                    if (e < F) {
+                        k0[e] = ((unsigned)(c[u] - cmin) << IDX) | (unsigned)e;
+                        plist[e] = (unsigned char)jj[u];
+                    }
+                }
             }
         }
         grp_sync<G>(gid);
@@ -378,22 +490,11 @@ __global__ void __launch_bounds__(kMwThreads, 2) k_mid_warp(CsrDev A, CsrDev B, 
         }
         if ((MODE == kMwUpper || MODE == kMwScratch) && t == 0)
             P.nnz[row] = len;
-        const T *arow = aval + a0;
-        constexpr unsigned imask = (1u << IDX) - 1u;
-        for (int h = t; h < len; h += NT) {
-            const int p = (int)dst[h], m = (int)dst[h + 1] - p;
-            const unsigned *run = src + p;
-            auto leaf = [&](int i) { return (int)lleaf[plist[run[i] & imask]]; };
-            auto val = [&](int i) {
-                const int e = (int)(run[i] & imask);
-                const int j = plist[e];
-                return vmul(arow[lleaf[j]], bval[lbs[j] + (e - loff[j])]);
-            };
-            // leaves below 32 need at most 5 stack entries below the top
-            const T v = k <= 32 ? mw_run_value<T, 6>(m, leaf, val) : mw_run_value<T, 9>(m, leaf, val);
-            ccol[base + h] = cmin + (int)(run[0] >> IDX);
-            cval[base + h] = v;
-        }
+        // gathers in flight: two runs a thread within 80 registers, four
+        // with 128
+        constexpr int RU = S::GROUPS * NT > 256 ? 2 : 4;
+        mw_reduce_runs<T, NT, IDX, RU>(src, dst, len, t, k, plist, lleaf, lbs, loff, aval + a0,
+                                       bval, cmin, ccol + base, cval + base);
         grp_sync<G>(gid);
     }
 }
@@ -626,14 +727,15 @@ __global__ void __launch_bounds__(kMwThreads, 2) k_mid_tile(CsrDev A, CsrDev B, 
     }
 }
 
-template <typename T, int MODE, int G>
+template <typename T, int MODE, int SID>
 inline void launch_mid_group(const CsrDev &A, const CsrDev &B, const PlanDev &P, const int *crpt,
                              int *ccol, T *cval, int num_sms, cudaStream_t s)
 {
-    const size_t sm = MidWarpLayout<G>::bytes;
-    cudaFuncSetAttribute(k_mid_warp<T, MODE, G>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    const size_t sm = MidWarpLayout<SID>::bytes;
+    cudaFuncSetAttribute(k_mid_warp<T, MODE, SID>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)sm);
-    k_mid_warp<T, MODE, G><<<num_sms * 2, kMwThreads, sm, s>>>(A, B, P, crpt, ccol, cval);
+    k_mid_warp<T, MODE, SID><<<num_sms * 2, mw_threads<SID>(), sm, s>>>(A, B, P, crpt, ccol,
+                                                                         cval);
     count_launch();
 }
 
@@ -653,8 +755,9 @@ template <typename T, int MODE>
 inline void launch_mid_warp(const CsrDev &A, const CsrDev &B, const PlanDev &P, const int *crpt,
                             int *ccol, T *cval, int num_sms, cudaStream_t s)
 {
-    launch_mid_group<T, MODE, 1>(A, B, P, crpt, ccol, cval, num_sms, s);
+    launch_mid_group<T, MODE, 5>(A, B, P, crpt, ccol, cval, num_sms, s);
     launch_mid_group<T, MODE, 4>(A, B, P, crpt, ccol, cval, num_sms, s);
+    launch_mid_group<T, MODE, 1>(A, B, P, crpt, ccol, cval, num_sms, s);
     launch_mid_tile<T, MODE, 8>(A, B, P, crpt, ccol, cval, num_sms, s);
     launch_mid_tile<T, MODE, 4>(A, B, P, crpt, ccol, cval, num_sms, s);
 }

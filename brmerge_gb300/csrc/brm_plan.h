@@ -45,6 +45,8 @@ constexpr int kMt2F = 128;        // second tile class: at most 128 products
 constexpr int kMtRangeBits = 25;
 constexpr int kMgF = 3072;
 constexpr int kMgRangeBits = 20;
+constexpr int kMg2F = 5888;       // second group class: two groups a CTA fit 2 CTAs an SM
+constexpr int kMg2RangeBits = 19;
 
 // Segmented heavy rows: a row that is not a mid row is cut, at 32-column word
 // (or, inside very dense words, column) boundaries, into column segments of at
@@ -85,7 +87,8 @@ enum RowBin : int {
     kBinMidGroup = 7, // four warps per row (brm_midwarp.cuh)
     kBinMidTile = 8,  // half a warp per row, products sorted in registers (brm_midwarp.cuh)
     kBinMidTile2 = 9, // the same with twice the products
-    kNumBins = 10,
+    kBinMidGroup2 = 10,  // four warps per row, longer rows (brm_midwarp.cuh)
+    kNumBins = 11,
 };
 
 // Device counters (one struct in device memory, zeroed per phase).

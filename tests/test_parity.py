@@ -381,11 +381,11 @@ def _rows_with_products(rng, targets, K, N, blen_lo=1, blen_hi=6, span=None):
 
 def test_mid_row_class_boundaries(ctx, oracle_mod):
     """Rows on either side of every class boundary: 33, 64 / 65 and 128 / 129
-    (half-warp tiles), 768 / 769 (warp), 3072 / 3073 (four-warp group, then
-    segmented)."""
+    (half-warp tiles), 768 / 769 (warp), 3072 / 3073 (four-warp groups) and
+    5888 / 5889 (longer four-warp groups, then segmented)."""
     rng = np.random.default_rng(41)
     A, B = _rows_with_products(rng, [33, 64, 65, 128, 129, 767, 768, 769, 1500, 3071, 3072, 3073,
-                                     5000],
+                                     5000, 5888, 5889],
                                K=3000, N=20000, blen_lo=1, blen_hi=30)
     R = oracle_mod.precise(A, B)
     assert_same_csr(gpu_precise(ctx, A, B), R, "boundaries split")
@@ -394,11 +394,12 @@ def test_mid_row_class_boundaries(ctx, oracle_mod):
 
 
 def test_mid_rows_wide_column_range(ctx, oracle_mod):
-    """Mid-size rows whose columns span more than 2^20 / 2^22 columns take the
-    batched or segmented paths instead of the warp kernels."""
+    """Mid-size rows whose columns span more than 2^19 / 2^20 / 2^22 columns
+    take the batched or segmented paths instead of the warp kernels."""
     rng = np.random.default_rng(42)
     N = 6_000_000
-    A, B = _rows_with_products(rng, [100, 700, 2000, 3000], K=2000, N=N, blen_lo=1, blen_hi=30)
+    A, B = _rows_with_products(rng, [100, 700, 2000, 3000, 5000], K=2000, N=N, blen_lo=1,
+                               blen_hi=30)
     R = oracle_mod.precise(A, B)
     assert_same_csr(gpu_precise(ctx, A, B), R, "wide split")
     assert_same_csr(gpu_precise_one_call(ctx, A, B), R, "wide one call")
