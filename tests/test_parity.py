@@ -393,13 +393,26 @@ def test_mid_row_class_boundaries(ctx, oracle_mod):
     assert_same_csr(gpu_upper(ctx, A, B), R, "boundaries upper")
 
 
+def test_mid_rows_long_groups(ctx, oracle_mod):
+    """Rows around the long four-warp group limit (5888 / 5889 products) and
+    longer rows of at most 255 lists (segmented), built from long B rows."""
+    rng = np.random.default_rng(44)
+    A, B = _rows_with_products(rng, [5888, 5889, 8000, 11776, 11777], K=3000, N=20000,
+                               blen_lo=40, blen_hi=60)
+    assert np.diff(A.rpt).max() <= 255
+    R = oracle_mod.precise(A, B)
+    assert_same_csr(gpu_precise(ctx, A, B), R, "long groups split")
+    assert_same_csr(gpu_precise_one_call(ctx, A, B), R, "long groups one call")
+    assert_same_csr(gpu_upper(ctx, A, B), R, "long groups upper")
+
+
 def test_mid_rows_wide_column_range(ctx, oracle_mod):
-    """Mid-size rows whose columns span more than 2^19 / 2^20 / 2^22 columns
-    take the batched or segmented paths instead of the warp kernels."""
+    """Mid-size rows whose columns span more than 2^19 .. 2^22 columns take
+    the batched or segmented paths instead of the warp kernels."""
     rng = np.random.default_rng(42)
     N = 6_000_000
-    A, B = _rows_with_products(rng, [100, 700, 2000, 3000, 5000], K=2000, N=N, blen_lo=1,
-                               blen_hi=30)
+    A, B = _rows_with_products(rng, [100, 700, 2000, 3000, 5000, 7000], K=2000, N=N, blen_lo=1,
+                               blen_hi=40)
     R = oracle_mod.precise(A, B)
     assert_same_csr(gpu_precise(ctx, A, B), R, "wide split")
     assert_same_csr(gpu_precise_one_call(ctx, A, B), R, "wide one call")
