@@ -394,7 +394,7 @@ struct RowPart {
 
 int numeric_launch(brm_context ctx, brm_dtype dtype, bool upper, const brm_csr *A,
                    const brm_csr *B, const int *crpt, int *ccol, void *cval, bool use_mid = false,
-                   const RowPart &part = RowPart())
+                   const RowPart &part = RowPart(), bool clear_err = true)
 {
     const bool mid = use_mid && ctx->mid_ready && !upper;
     if (ctx->spill_bytes)
@@ -406,7 +406,8 @@ int numeric_launch(brm_context ctx, brm_dtype dtype, bool upper, const brm_csr *
     P.seg_range = part.seg_range;
     if (part.seg_list)
         P.seg_list = (int *)part.seg_list;
-    BRM_CK(cudaMemsetAsync(&P.cnt->work_num, 0, 2 * sizeof(int), s));  // work_num, err
+    // work_num and (unless the errors of earlier parts must survive) err
+    BRM_CK(cudaMemsetAsync(&P.cnt->work_num, 0, (clear_err ? 2 : 1) * sizeof(int), s));
     BRM_CK(cudaMemsetAsync(&P.cnt->work_bnum, 0, 2 * sizeof(int), s));  // work_bnum, work_seg
     BRM_TRY(grow(ctx->splitbuf, ((size_t)ctx->h_cnt->table_cap + 1) * sizeof(int)));
     P.split = (int *)ctx->splitbuf.p;
@@ -525,10 +526,23 @@ int numeric_by_parts(brm_context ctx, brm_dtype dtype, const brm_csr *A, const b
     int *d_list = (int *)((char *)ctx->partbuf.p + b_small);
     BRM_CK(cudaMemcpyAsync(d_pb, pb, sizeof(int) * (size_t)(nparts + 1), cudaMemcpyHostToDevice, s));
     BRM_CK(cudaMemsetAsync(d_cnt, 0, sizeof(int) * 2 * brm::kMaxParts, s));  // cnt, fill
-    if (nseg > 0)
+    // parts run in order of their heavy-row segments, fewest first: the
+    // copy then starts after a light part, and the heavy parts compute while
+    // earlier parts are copied
+    int order[brm::kMaxParts];
+    for (int p = 0; p < nparts; p++)
+        order[p] = p;
+    if (nseg > 0) {
         brm::launch_seg_partition(ctx->plan, d_pb, nparts, d_cnt, d_fill, d_list, d_ranges,
                                   ctx->num_sms, s);
-    for (int p = 0; p < nparts; p++) {
+        int hseg[brm::kMaxParts];
+        BRM_CK(cudaMemcpyAsync(hseg, d_cnt, sizeof(int) * (size_t)nparts, cudaMemcpyDeviceToHost,
+                               s));
+        BRM_CK(cudaStreamSynchronize(s));
+        std::stable_sort(order, order + nparts, [&](int x, int y) { return hseg[x] < hseg[y]; });
+    }
+    for (int q = 0; q < nparts; q++) {
+        const int p = order[q];
         RowPart part;
         part.r_lo = pb[p];
         part.r_hi = pb[p + 1];
@@ -536,11 +550,11 @@ int numeric_by_parts(brm_context ctx, brm_dtype dtype, const brm_csr *A, const b
             part.seg_range = d_ranges + 2 * p;
             part.seg_list = d_list;
         }
-        BRM_TRY(numeric_launch(ctx, dtype, false, A, B, d_rpt, dcol, dval, true, part));
+        BRM_TRY(numeric_launch(ctx, dtype, false, A, B, d_rpt, dcol, dval, true, part, q == 0));
         const long long e0 = h_rpt[pb[p]], e1 = h_rpt[pb[p + 1]];
         if (e1 > e0) {
-            BRM_CK(cudaEventRecord(ctx->part_ev[p], s));
-            BRM_CK(cudaStreamWaitEvent(cs, ctx->part_ev[p], 0));
+            BRM_CK(cudaEventRecord(ctx->part_ev[q], s));
+            BRM_CK(cudaStreamWaitEvent(cs, ctx->part_ev[q], 0));
             BRM_CK(cudaMemcpyAsync(h_col + e0, dcol + e0, 4 * (size_t)(e1 - e0),
                                    cudaMemcpyDeviceToHost, cs));
             BRM_CK(cudaMemcpyAsync((char *)h_val + vb * (size_t)e0, (char *)dval + vb * (size_t)e0,
