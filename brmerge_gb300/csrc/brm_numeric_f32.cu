@@ -40,6 +40,8 @@ static void numeric_f32(const CsrDev &A, const CsrDev &B, const PlanDev &P, cons
     count_launch();
     k_long_reduce<float><<<num_sms * 4, 128, 0, s>>>(P, ccol, cval);
     count_launch();
+    k_long_warp<float><<<num_sms * 4, 128, 0, s>>>(P, ccol, cval);
+    count_launch();
     const size_t smem = NumLayout<float>::bytes;
     cudaFuncSetAttribute(k_rows_numeric<float, UPPER>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)smem);

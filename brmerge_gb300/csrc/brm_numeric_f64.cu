@@ -40,6 +40,8 @@ static void numeric_f64(const CsrDev &A, const CsrDev &B, const PlanDev &P, cons
     count_launch();
     k_long_reduce<double><<<num_sms * 4, 128, 0, s>>>(P, ccol, cval);
     count_launch();
+    k_long_warp<double><<<num_sms * 4, 128, 0, s>>>(P, ccol, cval);
+    count_launch();
     const size_t smem = NumLayout<double>::bytes;
     cudaFuncSetAttribute(k_rows_numeric<double, UPPER>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)smem);

@@ -942,31 +942,82 @@ __global__ void __launch_bounds__(kSegThreads) k_seg_numeric(CsrDev A, CsrDev B,
 //    below the top).
 // ---------------------------------------------------------------------------
 // Sequential trie of the elements [b, e) of a long column (leaves in
-// increasing order, below 2^(D-1)).
-template <typename T, int D>
+// increasing order, below 2^(D-1)); the elements are loaded GB at a time, so
+// a long column does not wait for one load per element.
+template <typename T, int D, int GB = kGatherBatch>
 __device__ __forceinline__ T long_run(const unsigned short *__restrict__ lleaf,
                                       const T *__restrict__ lval, long long b, long long e)
 {
     RegShiftReduce<T, D> sr;
     sr.init(lleaf[b], lval[b]);
-    // elements in groups of kGatherBatch independent loads, so a long
-    // column does not wait for one load per element
-    for (long long j0 = b + 1; j0 < e; j0 += kGatherBatch) {
-        int lf[kGatherBatch];
-        T lv[kGatherBatch];
+    for (long long j0 = b + 1; j0 < e; j0 += GB) {
+        int lf[GB];
+        T lv[GB];
 #pragma unroll
-        for (int q = 0; q < kGatherBatch; q++) {
+        for (int q = 0; q < GB; q++) {
             if (j0 + q < e) {
                 lf[q] = lleaf[j0 + q];
                 lv[q] = lval[j0 + q];
             }
         }
 #pragma unroll
-        for (int q = 0; q < kGatherBatch; q++)
+        for (int q = 0; q < GB; q++)
             if (j0 + q < e)
                 sr.push(lf[q], lv[q]);
     }
     return sr.finish();
+}
+
+constexpr int kLrWarpMin = 32;  // columns with more products are reduced by a whole warp
+                                // (and so are columns with leaves of 4096 or more)
+
+// A long column reduced by a whole warp.  Its leaves (strictly increasing,
+// below 2^bits) are cut into the 32 aligned ranges of 2^s leaves, s = bits - 5:
+// every range is one subtree of the merge tree at level s, so lane j reduces
+// the products of range j on its own (at most s split levels: 12 stack
+// entries suffice for 16-bit leaves), and the subtree values are then joined
+// by the trie over their range indices (warp_trie); every lane returns the
+// value.  cnt and sv are the warp's 32-entry shared scratch.
+template <typename T>
+__device__ __forceinline__ T warp_long_column(const unsigned short *__restrict__ lleaf,
+                                              const T *__restrict__ lval, long long b, int len,
+                                              int *cnt, T *sv)
+{
+    const int lane = threadIdx.x & 31;
+    const int bits = 32 - __clz((int)lleaf[b + len - 1] | 1);
+    const int s = bits > 5 ? bits - 5 : 0;
+    cnt[lane] = 0;
+    __syncwarp();
+    for (int p = lane; p < len; p += 32)
+        atomicAdd(&cnt[lleaf[b + p] >> s], 1);
+    __syncwarp();
+    const int mc = cnt[lane];
+    const int lo = warp_incl_scan(mc) - mc;
+    T v = T(0);
+    if (mc > 0)
+        v = long_run<T, 12, 4>(lleaf, lval, b + lo, b + lo + mc);
+    // the nonempty ranges in order, one per lane
+    const unsigned hm = __ballot_sync(kFull, mc > 0);
+    const int r = __popc(hm & ((1u << lane) - 1u));
+    __syncwarp();
+    if (mc > 0) {
+        sv[r] = v;
+        cnt[r] = lane;
+    }
+    __syncwarp();
+    const int nh = __popc(hm);
+    const int li = lane < nh ? cnt[lane] : 0;
+    const T vi = lane < nh ? sv[lane] : T(0);
+    __syncwarp();
+    return __shfl_sync(kFull, warp_trie<T>(li, vi, nh), 0);  // the trie's value is in lane 0
+}
+
+// Columns of at most kLrWarpMin products with leaves below 4096 are reduced
+// one per thread (k_long_reduce), the others by whole warps (k_long_warp):
+// two kernels, so that neither pays the other's registers.
+__device__ __forceinline__ bool long_by_thread(const LongCol &c, int last)
+{
+    return c.len <= kLrWarpMin && last < 4096;
 }
 
 template <typename T>
@@ -983,17 +1034,47 @@ __global__ void __launch_bounds__(128) k_long_reduce(PlanDev P, int *ccol, T *cv
         c.len = 0;
         if (i < n)
             c = P.long_col[i];
-        // the stack depth follows the largest leaf (the last one); the warp
-        // takes the shallow stack when all of its columns allow it
-        const bool shallow = c.len <= 0 || lleaf[c.off + c.len - 1] < 256;
-        if (__all_sync(kFull, shallow)) {
-            if (c.len > 0) {
-                ccol[c.out] = c.col;
-                cval[c.out] = long_run<T, 9>(lleaf, lval, c.off, c.off + c.len);
-            }
-        } else if (c.len > 0) {
+        const int last = c.len > 0 ? (int)lleaf[c.off + c.len - 1] : 0;
+        const bool mine = c.len > 0 && long_by_thread(c, last);
+        // the stack depth follows the warp's largest last leaf
+        const int top = __reduce_max_sync(kFull, mine ? last : 0);
+        if (mine) {
             ccol[c.out] = c.col;
-            cval[c.out] = long_run<T, 17>(lleaf, lval, c.off, c.off + c.len);
+            cval[c.out] = top < 256 ? long_run<T, 9>(lleaf, lval, c.off, c.off + c.len)
+                                    : long_run<T, 13, 4>(lleaf, lval, c.off, c.off + c.len);
+        }
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(128) k_long_warp(PlanDev P, int *ccol, T *cval)
+{
+    __shared__ int s_cnt[4][32];
+    __shared__ T s_val[4][32];
+    const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const unsigned long long used = P.cnt->long_used;
+    const long long n = min((long long)(used >> 40), P.long_cap_cols);
+    const T *__restrict__ lval = (const T *)P.long_val;
+    const unsigned short *__restrict__ lleaf = P.long_leaf;
+    for (long long i0 = (long long)blockIdx.x * blockDim.x; i0 < n;
+         i0 += (long long)gridDim.x * blockDim.x) {
+        const long long i = i0 + threadIdx.x;
+        LongCol c;
+        c.len = 0;
+        if (i < n)
+            c = P.long_col[i];
+        const int last = c.len > 0 ? (int)lleaf[c.off + c.len - 1] : 0;
+        unsigned lm = __ballot_sync(kFull, c.len > 0 && !long_by_thread(c, last));
+        while (lm) {
+            const int src = __ffs(lm) - 1;
+            lm &= lm - 1u;
+            const long long off = __shfl_sync(kFull, c.off, src);
+            const int len = __shfl_sync(kFull, c.len, src);
+            const T r = warp_long_column<T>(lleaf, lval, off, len, s_cnt[wid], s_val[wid]);
+            if (lane == src) {
+                ccol[c.out] = c.col;
+                cval[c.out] = r;
+            }
         }
     }
 }

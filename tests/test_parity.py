@@ -433,3 +433,30 @@ def test_mid_rows_list_counts(ctx, oracle_mod):
     assert_same_csr(gpu_upper(ctx, A, B), R, "list counts upper")
     C32 = gpu_precise(ctx, A.astype(np.float32), B.astype(np.float32))
     assert_same_csr(C32, oracle_mod.precise(A.astype(np.float32), B.astype(np.float32)), "f32")
+
+
+def test_heavy_segments_list_counts(ctx, oracle_mod):
+    """Heavy-row segments done by four-warp groups: about 400 sub-lists per
+    segment with long runs (stack of 13 levels), 200 lists (9 levels), and
+    100 nonempty lists at leaves above 4900 of a 5000-entry row (17 levels);
+    and segments of about 1000 short sub-lists, left to the segment kernel."""
+    rng = np.random.default_rng(45)
+    N = 400
+    # B rows: 0..4999 empty, 5000..5599 long (30..60 columns), 5600..6999 short
+    Brows = ([[] for _ in range(5000)]
+             + [sorted(rng.choice(N, int(rng.integers(30, 61)), replace=False)) for _ in range(600)]
+             + [sorted(rng.choice(N, int(rng.integers(1, 4)), replace=False)) for _ in range(1400)])
+    K = len(Brows)
+    longs, shorts = np.arange(5000, 5600), np.arange(5600, 7000)
+    Arows = [sorted(rng.choice(longs, 400, replace=False)),
+             sorted(rng.choice(shorts, 1000, replace=False)),
+             sorted(list(rng.choice(5000, 4900, replace=False)) + list(rng.choice(longs, 100, replace=False))),
+             sorted(rng.choice(longs, 200, replace=False)),
+             [5000, 5001, 5600]]
+    A, B = _csr(Arows, K, 11), _csr(Brows, N, 12)
+    R = oracle_mod.precise(A, B)
+    assert_same_csr(gpu_precise(ctx, A, B), R, "segment lists split")
+    assert_same_csr(gpu_precise_one_call(ctx, A, B), R, "segment lists one call")
+    assert_same_csr(gpu_upper(ctx, A, B), R, "segment lists upper")
+    C32 = gpu_precise(ctx, A.astype(np.float32), B.astype(np.float32))
+    assert_same_csr(C32, oracle_mod.precise(A.astype(np.float32), B.astype(np.float32)), "f32")
