@@ -628,6 +628,8 @@ def run_ours(args):
         "metric": "SpGEMM GFLOP/s (BRMerge-Precise, C=A*A)",
         "value": round(value, 3), "unit": "GFLOP/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(statistics.mean(step_ms), 4),
+        "step_ms": {"min": round(min(step_ms), 4), "median": round(statistics.median(step_ms), 4),
+                    "max": round(max(step_ms), 4)},
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic",
         "config": dict(desc, products=int(products), nnz_A=int(A.nnz), nnz_C=int(cnnz),
