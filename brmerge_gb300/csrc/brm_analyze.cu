@@ -59,7 +59,8 @@ __global__ void __launch_bounds__(kAnaThreads) k_analyze(CsrDev A, CsrDev B, Pla
 {
     constexpr int NW = kAnaThreads / 32;
     constexpr int NGR = kAnaThreads / TW;  // groups per block
-    constexpr int RPB = NGR * kAnaRowsPerGroup;
+    constexpr int RPG = LISTED ? 1 : kAnaRowsPerGroup;  // rows per group (one listed long row)
+    constexpr int RPB = NGR * RPG;
     __shared__ int s_cnt[kNumBins];
     __shared__ int s_base[kNumBins];
     __shared__ int s_bin[RPB];
@@ -78,8 +79,8 @@ __global__ void __launch_bounds__(kAnaThreads) k_analyze(CsrDev A, CsrDev B, Pla
     const int row0 = blockIdx.x * RPB;
     unsigned long long gflop = 0;
     int gmaxk = 0;
-    for (int r = 0; r < kAnaRowsPerGroup; r++) {
-        const int slot = grp * kAnaRowsPerGroup + r;
+    for (int r = 0; r < RPG; r++) {
+        const int slot = grp * RPG + r;
         if (row0 + slot >= nrows) {
             if (gl == 0)
                 s_bin[slot] = -1;
@@ -102,16 +103,20 @@ __global__ void __launch_bounds__(kAnaThreads) k_analyze(CsrDev A, CsrDev B, Pla
             bad = true;
             a0 = a1 = 0;
         }
-        // four entries a lane in flight (long rows on narrow groups)
-        for (int jb = a0 + gl; jb < a1; jb += 4 * TW) {
-            int b[4], bs[4], be[4];
+        // UN entries a lane in flight; the listed long rows also take the
+        // first and last column of every nonempty list in the same pass (the
+        // column range), so their long lists are walked once
+        constexpr int UN = LISTED ? 8 : 4;
+        int mn = INT_MAX, mx = -1;
+        for (int jb = a0 + gl; jb < a1; jb += UN * TW) {
+            int b[UN], bs[UN], be[UN];
 #pragma unroll
-            for (int u = 0; u < 4; u++) {
+            for (int u = 0; u < UN; u++) {
                 const int j = jb + u * TW;
                 b[u] = j < a1 ? A.col[j] : -1;
             }
 #pragma unroll
-            for (int u = 0; u < 4; u++) {
+            for (int u = 0; u < UN; u++) {
                 const int j = jb + u * TW;
                 bs[u] = be[u] = 0;
                 if (j < a1) {
@@ -123,8 +128,25 @@ __global__ void __launch_bounds__(kAnaThreads) k_analyze(CsrDev A, CsrDev B, Pla
                     }
                 }
             }
+            if (LISTED) {
+                int c0[UN], c1[UN];
 #pragma unroll
-            for (int u = 0; u < 4; u++) {
+                for (int u = 0; u < UN; u++) {
+                    c0[u] = INT_MAX;
+                    c1[u] = -1;
+                    if (be[u] > bs[u]) {
+                        c0[u] = B.col[bs[u]];
+                        c1[u] = B.col[be[u] - 1];
+                    }
+                }
+#pragma unroll
+                for (int u = 0; u < UN; u++) {
+                    mn = min(mn, c0[u]);
+                    mx = max(mx, c1[u]);
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < UN; u++) {
                 const int j = jb + u * TW;
                 if (j < a1) {
                     const int len = be[u] - bs[u];
@@ -169,8 +191,7 @@ __global__ void __launch_bounds__(kAnaThreads) k_analyze(CsrDev A, CsrDev B, Pla
             bin == kBinMidTile2 || bin == kBinMidGroup2) {
             // column range of the row for the segment planning and the warp
             // mid rows' keys: the first and last column of every nonempty list
-            int mn = INT_MAX, mx = -1;
-            for (int jb = a0 + gl; jb < a1; jb += 4 * TW) {
+            for (int jb = a0 + gl; !LISTED && jb < a1; jb += 4 * TW) {
                 int c0[4], c1[4];
 #pragma unroll
                 for (int u = 0; u < 4; u++) {
@@ -284,7 +305,8 @@ void launch_analyze(const CsrDev &A, const CsrDev &B, const PlanDev &P, cudaStre
         k_analyze<8, false><<<(A.M + RPB - 1) / RPB, kAnaThreads, 0, s>>>(A, B, P);
         count_launch();
         const long long most = std::min<long long>(A.M, (long long)A.nnz / (kAnaLongK + 1));
-        const int g = (int)std::max<long long>(1, (most + RPB32 - 1) / RPB32);
+        constexpr int RPBL = kAnaThreads / 32;  // one listed row per warp
+        const int g = (int)std::max<long long>(1, (most + RPBL - 1) / RPBL);
         k_analyze<32, true><<<g, kAnaThreads, 0, s>>>(A, B, P);
     } else {
         k_analyze<32, false><<<(A.M + RPB32 - 1) / RPB32, kAnaThreads, 0, s>>>(A, B, P);
