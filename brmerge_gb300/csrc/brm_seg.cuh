@@ -617,10 +617,20 @@ __global__ void __launch_bounds__(kSegThreads) k_seg_numeric(CsrDev A, CsrDev B,
             misc[1] = 0;  // long runs
             misc[2] = 0;  // staged column out of range
         }
-        if (tid < nsum)
+        // a segment spanning at most 32 * kSegCap columns ranks its columns
+        // with one flat bitmap in cw (a prefix per word); wider ones with a
+        // summary bit per nonempty word and compressed words
+        const bool flat = span <= 32 * kSegCap;
+        const int nwf = (span + 31) >> 5;
+        if (flat) {
+            for (int i = tid; i < nwf; i += NT)
+                cw[i] = 0;
+        } else if (tid < nsum) {
             summ[tid] = 0;
+        }
         __syncthreads();
-        // stage products in list-major (= leaf) order; mark their words in the summary
+        // stage products in list-major (= leaf) order; mark their words in the
+        // flat bitmap or in the summary
         const int ipt = (nprod + NT - 1) / NT;
         const int p0 = min(tid * ipt, nprod), p1 = min(p0 + ipt, nprod);
         // a thread's products are column-sorted within each list, so runs of
@@ -666,19 +676,19 @@ __global__ void __launch_bounds__(kSegThreads) k_seg_numeric(CsrDev A, CsrDev B,
                         prc[e] = rc;
                         pval[e] = vmul(av[i], bv[i]);
                         pleaf[e] = lleaf[lid[i]];
-                        const unsigned sw = (unsigned)rc >> 10;
+                        const unsigned sw = (unsigned)rc >> (flat ? 5 : 10);
                         if (sw != run_w) {
                             if (run_b)
-                                atomicOr(&summ[run_w], run_b);
+                                atomicOr(flat ? &cw[run_w] : &summ[run_w], run_b);
                             run_w = sw;
                             run_b = 0;
                         }
-                        run_b |= 1u << ((rc >> 5) & 31);
+                        run_b |= 1u << ((rc >> (flat ? 0 : 5)) & 31);
                     }
                 }
             }
             if (run_b)
-                atomicOr(&summ[run_w], run_b);
+                atomicOr(flat ? &cw[run_w] : &summ[run_w], run_b);
         }
         __syncthreads();
         if (misc[2]) {  // a column outside the segment: the plan does not match the input
@@ -686,22 +696,23 @@ __global__ void __launch_bounds__(kSegThreads) k_seg_numeric(CsrDev A, CsrDev B,
                 atomicOr(&P.cnt->err, kErrBadInput);
             continue;
         }
-        // compressed words: one per nonempty 32-column word
-        long long ncw_t;
-        {
+        // compressed words: one per nonempty 32-column word (flat: every word)
+        int ncw = nwf;
+        if (!flat) {
+            long long ncw_t;
             const unsigned sv = tid < nsum ? summ[tid] : 0u;
             const int sx = (int)block_excl_scan<NT, long long>(__popc(sv), ws, &ncw_t);
             if (tid < nsum)
                 srank[tid] = (unsigned short)sx;
+            ncw = (int)ncw_t;
+            for (int i = tid; i < ncw; i += NT)
+                cw[i] = 0;
         }
-        const int ncw = (int)ncw_t;
-        for (int i = tid; i < ncw; i += NT)
-            cw[i] = 0;
         for (int i = tid; i <= nprod; i += NT)  // the sub-list table is dead now
             ucnt[i] = 0;
         __syncthreads();
         // mark the compressed words; keep each product's word index in pu
-        {
+        if (!flat) {
             int run_ci = -1;
             unsigned bits = 0;
             for (int p = p0; p < p1; p++) {
@@ -742,8 +753,9 @@ __global__ void __launch_bounds__(kSegThreads) k_seg_numeric(CsrDev A, CsrDev B,
         // every column (the rank within a column, from the atomic, is in
         // arbitrary order and is put in leaf order when the column is reduced)
         for (int p = p0; p < p1; p++) {
-            const int ci = pu[p];
-            const int u = cwr[ci] + __popc(cw[ci] & ((1u << (prc[p] & 31)) - 1u));
+            const int rc = prc[p];
+            const int ci = flat ? rc >> 5 : pu[p];
+            const int u = cwr[ci] + __popc(cw[ci] & ((1u << (rc & 31)) - 1u));
             pu[p] = (unsigned short)u;
             if (!nodup)
                 ia[p] = (unsigned short)atomicAdd(&ucnt[u], 1);
