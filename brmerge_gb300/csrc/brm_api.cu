@@ -81,6 +81,9 @@ struct brm_context_s {
     DevBuf partbuf;
     cudaStream_t copy_stream = nullptr;
     cudaEvent_t part_ev[brm::kMaxParts] = {};
+    // a second compute stream: the mid rows run on it beside the heavy-row
+    // planning, and the copy, warp and mid rows beside the segments
+    brm::Fork fork;
     cudaEvent_t ev[kNumEvents] = {};
 };
 
@@ -345,13 +348,21 @@ int plan_phase(brm_context ctx, const brm_csr *A, const brm_csr *B, int *crpt, b
         ctx->plan.seg_list = P.seg_list;
     }
     ev_record(ctx, timed, 1);
-    brm::launch_symbolic(a, b, P, ctx->num_sms, upper, fused, s);
     if (fused) {
+        // the mid rows (values into the scratch) on the second stream, beside
+        // the warp-row counts and the heavy-row planning
+        const brm::Fork &fk = ctx->fork;
+        BRM_CK(cudaEventRecord(fk.fork, s));
+        BRM_CK(cudaStreamWaitEvent(fk.aux, fk.fork, 0));
         if (fused_dtype == BRM_F64)
-            brm::launch_mid_scratch_f64(a, b, P, ctx->mid_col, ctx->mid_val, ctx->num_sms, s);
+            brm::launch_mid_scratch_f64(a, b, P, ctx->mid_col, ctx->mid_val, ctx->num_sms, fk.aux);
         else
-            brm::launch_mid_scratch_f32(a, b, P, ctx->mid_col, ctx->mid_val, ctx->num_sms, s);
+            brm::launch_mid_scratch_f32(a, b, P, ctx->mid_col, ctx->mid_val, ctx->num_sms, fk.aux);
+        BRM_CK(cudaEventRecord(fk.join, fk.aux));
     }
+    brm::launch_symbolic(a, b, P, ctx->num_sms, upper, fused, s);
+    if (fused)
+        BRM_CK(cudaStreamWaitEvent(s, ctx->fork.join, 0));
     ev_record(ctx, timed, 2);
     if (upper)
         brm::launch_scan_i64(P.flop, P.scan_flop, A->M, ctx->scan_tmp, s);
@@ -433,10 +444,10 @@ int numeric_launch(brm_context ctx, brm_dtype dtype, bool upper, const brm_csr *
     const void *mval = mid ? ctx->mid_val : nullptr;
     if (dtype == BRM_F64)
         brm::launch_numeric_f64(upper, a, b, P, crpt, ccol, cval, ctx->spill.p, ctx->spill_bytes,
-                                mcol, mval, ctx->num_sms, s);
+                                mcol, mval, ctx->num_sms, s, ctx->fork);
     else
         brm::launch_numeric_f32(upper, a, b, P, crpt, ccol, cval, ctx->spill.p, ctx->spill_bytes,
-                                mcol, mval, ctx->num_sms, s);
+                                mcol, mval, ctx->num_sms, s, ctx->fork);
     BRM_CK(cudaGetLastError());
     return BRM_SUCCESS;
 }
@@ -784,6 +795,12 @@ int brm_create(brm_context *out)
         e = cudaEventCreateWithFlags(&ctx->part_ev[i], cudaEventDisableTiming);
     if (e == cudaSuccess)
         e = cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess)
+        e = cudaStreamCreateWithFlags(&ctx->fork.aux, cudaStreamNonBlocking);
+    if (e == cudaSuccess)
+        e = cudaEventCreateWithFlags(&ctx->fork.fork, cudaEventDisableTiming);
+    if (e == cudaSuccess)
+        e = cudaEventCreateWithFlags(&ctx->fork.join, cudaEventDisableTiming);
     if (e == cudaSuccess) {
         // keep freed stream-ordered allocations cached in this process so
         // repeated calls do not return memory to the driver between calls
@@ -846,6 +863,14 @@ int brm_destroy(brm_context ctx)
         cudaStreamSynchronize(ctx->copy_stream);
         cudaStreamDestroy(ctx->copy_stream);
     }
+    if (ctx->fork.aux) {
+        cudaStreamSynchronize(ctx->fork.aux);
+        cudaStreamDestroy(ctx->fork.aux);
+    }
+    if (ctx->fork.fork)
+        cudaEventDestroy(ctx->fork.fork);
+    if (ctx->fork.join)
+        cudaEventDestroy(ctx->fork.join);
     release(ctx->partbuf);
     delete ctx;
     return BRM_SUCCESS;

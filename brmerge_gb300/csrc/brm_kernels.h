@@ -69,17 +69,28 @@ void launch_validate(const CsrDev &X, int ncols, int *bad_row, cudaStream_t s);
 }  // namespace brm
 
 namespace brm {
+// A second stream for work independent of the main stream's: `fork` is
+// recorded on the main stream and waited for by `aux`, `join` recorded on
+// `aux` and waited for by the main stream.  aux == nullptr: one stream.
+struct Fork {
+    cudaStream_t aux = nullptr;
+    cudaEvent_t fork = nullptr;
+    cudaEvent_t join = nullptr;
+};
+
 // Numeric launchers per value type.  mid_col/mid_val (Precise only): the
 // scratch written by launch_mid_scratch_*, moved to C instead of running the
-// mid-row kernel again.
+// mid-row kernel again.  With a fork, the rows that need no split table
+// (copy, warp and mid rows) run on its aux stream beside the heavy-row
+// segments; the launcher joins the streams before it returns.
 void launch_numeric_f64(bool upper, const CsrDev &A, const CsrDev &B, const PlanDev &P,
                         const int *crpt, int *ccol, void *cval, void *spill_scratch,
                         unsigned long long spill_bytes, const int *mid_col, const void *mid_val,
-                        int num_sms, cudaStream_t s);
+                        int num_sms, cudaStream_t s, const Fork &fk);
 void launch_numeric_f32(bool upper, const CsrDev &A, const CsrDev &B, const PlanDev &P,
                         const int *crpt, int *ccol, void *cval, void *spill_scratch,
                         unsigned long long spill_bytes, const int *mid_col, const void *mid_val,
-                        int num_sms, cudaStream_t s);
+                        int num_sms, cudaStream_t s, const Fork &fk);
 
 // One-call Precise: the mid rows' values and lengths (P.nnz) computed with
 // the plan, into a scratch of P.mid_pre[M] entries (row r at P.mid_pre[r]).

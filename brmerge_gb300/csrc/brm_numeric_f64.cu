@@ -10,8 +10,17 @@ namespace brm {
 template <bool UPPER>
 static void numeric_f64(const CsrDev &A, const CsrDev &B, const PlanDev &P, const int *crpt,
                        int *ccol, double *cval, void *spill_scratch, unsigned long long spill_bytes,
-                       const int *mid_col, const void *mid_val, int num_sms, cudaStream_t s)
+                       const int *mid_col, const void *mid_val, int num_sms, cudaStream_t s0,
+                       const Fork &fk)
 {
+    // copy, warp and mid rows on the aux stream (when there is one), beside
+    // the split table and the segments of the heavy rows on s0
+    cudaStream_t s = s0;
+    if (fk.aux) {
+        cudaEventRecord(fk.fork, s0);
+        cudaStreamWaitEvent(fk.aux, fk.fork, 0);
+        s = fk.aux;
+    }
     k_copy_numeric<double, UPPER><<<num_sms * 8, 256, 0, s>>>(A, B, P, crpt, ccol, cval);
     count_launch();
     k_warp_numeric<double, UPPER><<<num_sms * 8, 256, 0, s>>>(A, B, P, crpt, ccol, cval);
@@ -31,6 +40,9 @@ static void numeric_f64(const CsrDev &A, const CsrDev &B, const PlanDev &P, cons
                                                                             cval);
         count_launch();
     }
+    if (fk.aux)
+        cudaEventRecord(fk.join, fk.aux);
+    s = s0;
     k_split<0><<<num_sms * 8, 256, 0, s>>>(A, B, P);
     count_launch();
     const size_t ssm = SegLayout<double>::bytes;
@@ -52,21 +64,23 @@ static void numeric_f64(const CsrDev &A, const CsrDev &B, const PlanDev &P, cons
             A, B, P, crpt, ccol, cval, (unsigned char *)spill_scratch, spill_bytes);
         count_launch();
     }
+    if (fk.aux)
+        cudaStreamWaitEvent(s0, fk.join, 0);
 }
 
 void launch_numeric_f64(bool upper, const CsrDev &A, const CsrDev &B, const PlanDev &P,
                        const int *crpt, int *ccol, void *cval, void *spill_scratch,
                        unsigned long long spill_bytes, const int *mid_col, const void *mid_val,
-                       int num_sms, cudaStream_t s)
+                       int num_sms, cudaStream_t s, const Fork &fk)
 {
     if (A.M <= 0)
         return;
     if (upper)
         numeric_f64<true>(A, B, P, crpt, ccol, (double *)cval, spill_scratch, spill_bytes, nullptr,
-                          nullptr, num_sms, s);
+                          nullptr, num_sms, s, fk);
     else
         numeric_f64<false>(A, B, P, crpt, ccol, (double *)cval, spill_scratch, spill_bytes, mid_col,
-                           mid_val, num_sms, s);
+                           mid_val, num_sms, s, fk);
 }
 
 void launch_mid_scratch_f64(const CsrDev &A, const CsrDev &B, const PlanDev &P, int *mid_col,
