@@ -349,20 +349,30 @@ int plan_phase(brm_context ctx, const brm_csr *A, const brm_csr *B, int *crpt, b
     }
     ev_record(ctx, timed, 1);
     if (fused) {
-        // the mid rows (values into the scratch) on the second stream, beside
-        // the warp-row counts and the heavy-row planning
+        // the batched and four-warp group mid rows (values into the scratch)
+        // on the second stream, beside the warp-row counts, the heavy-row
+        // planning and then the warp and tile mid rows
         const brm::Fork &fk = ctx->fork;
         BRM_CK(cudaEventRecord(fk.fork, s));
         BRM_CK(cudaStreamWaitEvent(fk.aux, fk.fork, 0));
         if (fused_dtype == BRM_F64)
-            brm::launch_mid_scratch_f64(a, b, P, ctx->mid_col, ctx->mid_val, ctx->num_sms, fk.aux);
+            brm::launch_mid_scratch_f64(a, b, P, ctx->mid_col, ctx->mid_val, ctx->num_sms, fk.aux,
+                                        brm::kMidGroups);
         else
-            brm::launch_mid_scratch_f32(a, b, P, ctx->mid_col, ctx->mid_val, ctx->num_sms, fk.aux);
+            brm::launch_mid_scratch_f32(a, b, P, ctx->mid_col, ctx->mid_val, ctx->num_sms, fk.aux,
+                                        brm::kMidGroups);
         BRM_CK(cudaEventRecord(fk.join, fk.aux));
     }
     brm::launch_symbolic(a, b, P, ctx->num_sms, upper, fused, s);
-    if (fused)
+    if (fused) {
+        if (fused_dtype == BRM_F64)
+            brm::launch_mid_scratch_f64(a, b, P, ctx->mid_col, ctx->mid_val, ctx->num_sms, s,
+                                        brm::kMidWarps);
+        else
+            brm::launch_mid_scratch_f32(a, b, P, ctx->mid_col, ctx->mid_val, ctx->num_sms, s,
+                                        brm::kMidWarps);
         BRM_CK(cudaStreamWaitEvent(s, ctx->fork.join, 0));
+    }
     ev_record(ctx, timed, 2);
     if (upper)
         brm::launch_scan_i64(P.flop, P.scan_flop, A->M, ctx->scan_tmp, s);

@@ -94,8 +94,10 @@ void launch_numeric_f32(bool upper, const CsrDev &A, const CsrDev &B, const Plan
 
 // One-call Precise: the mid rows' values and lengths (P.nnz) computed with
 // the plan, into a scratch of P.mid_pre[M] entries (row r at P.mid_pre[r]).
+// which: 1 = the batched mid rows and the four-warp group rows, 2 = the warp
+// and tile rows, 3 = all (the parts can run on different streams).
 void launch_mid_scratch_f64(const CsrDev &A, const CsrDev &B, const PlanDev &P, int *mid_col,
-                            void *mid_val, int num_sms, cudaStream_t s);
+                            void *mid_val, int num_sms, cudaStream_t s, int which);
 void launch_mid_scratch_f32(const CsrDev &A, const CsrDev &B, const PlanDev &P, int *mid_col,
-                            void *mid_val, int num_sms, cudaStream_t s);
+                            void *mid_val, int num_sms, cudaStream_t s, int which);
 }  // namespace brm

@@ -751,15 +751,22 @@ inline void launch_mid_tile(const CsrDev &A, const CsrDev &B, const PlanDev &P, 
 }
 
 // The warp rows, the four-warp group rows and the tile rows of one mode.
+// which: kMidGroups (the four-warp groups), kMidWarps (warp and tile rows) or
+// both.
 template <typename T, int MODE>
 inline void launch_mid_warp(const CsrDev &A, const CsrDev &B, const PlanDev &P, const int *crpt,
-                            int *ccol, T *cval, int num_sms, cudaStream_t s)
+                            int *ccol, T *cval, int num_sms, cudaStream_t s,
+                            int which = kMidGroups | kMidWarps)
 {
-    launch_mid_group<T, MODE, 5>(A, B, P, crpt, ccol, cval, num_sms, s);
-    launch_mid_group<T, MODE, 4>(A, B, P, crpt, ccol, cval, num_sms, s);
-    launch_mid_group<T, MODE, 1>(A, B, P, crpt, ccol, cval, num_sms, s);
-    launch_mid_tile<T, MODE, 8>(A, B, P, crpt, ccol, cval, num_sms, s);
-    launch_mid_tile<T, MODE, 4>(A, B, P, crpt, ccol, cval, num_sms, s);
+    if (which & kMidGroups) {
+        launch_mid_group<T, MODE, 5>(A, B, P, crpt, ccol, cval, num_sms, s);
+        launch_mid_group<T, MODE, 4>(A, B, P, crpt, ccol, cval, num_sms, s);
+    }
+    if (which & kMidWarps) {
+        launch_mid_group<T, MODE, 1>(A, B, P, crpt, ccol, cval, num_sms, s);
+        launch_mid_tile<T, MODE, 8>(A, B, P, crpt, ccol, cval, num_sms, s);
+        launch_mid_tile<T, MODE, 4>(A, B, P, crpt, ccol, cval, num_sms, s);
+    }
 }
 
 }  // namespace brm

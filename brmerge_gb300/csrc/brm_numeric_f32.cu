@@ -84,17 +84,19 @@ void launch_numeric_f32(bool upper, const CsrDev &A, const CsrDev &B, const Plan
 }
 
 void launch_mid_scratch_f32(const CsrDev &A, const CsrDev &B, const PlanDev &P, int *mid_col,
-                            void *mid_val, int num_sms, cudaStream_t s)
+                            void *mid_val, int num_sms, cudaStream_t s, int which)
 {
     if (A.M <= 0)
         return;
-    const size_t msm = MidNumLayout<float>::bytes;
-    cudaFuncSetAttribute(k_mid_numeric<float, false, true>,
-                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)msm);
-    k_mid_numeric<float, false, true><<<num_sms * 2, kMidThreads, msm, s>>>(
-        A, B, P, nullptr, mid_col, (float *)mid_val);
-    count_launch();
-    launch_mid_warp<float, kMwScratch>(A, B, P, nullptr, mid_col, (float *)mid_val, num_sms, s);
+    if (which & kMidGroups) {
+        const size_t msm = MidNumLayout<float>::bytes;
+        cudaFuncSetAttribute(k_mid_numeric<float, false, true>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)msm);
+        k_mid_numeric<float, false, true><<<num_sms * 2, kMidThreads, msm, s>>>(
+            A, B, P, nullptr, mid_col, (float *)mid_val);
+        count_launch();
+    }
+    launch_mid_warp<float, kMwScratch>(A, B, P, nullptr, mid_col, (float *)mid_val, num_sms, s, which);
 }
 
 }  // namespace brm

@@ -47,6 +47,9 @@ constexpr int kMgF = 3072;
 constexpr int kMgRangeBits = 20;
 constexpr int kMg2F = 5888;       // second group class: two groups a CTA fit 2 CTAs an SM
 constexpr int kMg2RangeBits = 19;
+// Subsets of the mid-row kernels (they can run on different streams).
+constexpr int kMidGroups = 1;     // the batched mid rows and the four-warp group rows
+constexpr int kMidWarps = 2;      // the warp and tile rows
 
 // Segmented heavy rows: a row that is not a mid row is cut, at 32-column word
 // (or, inside very dense words, column) boundaries, into column segments of at
