@@ -1,4 +1,5 @@
-// brm_kernels.h -- host-side launchers of the BRMerge kernels (one GPU, one stream).
+// brm_kernels.h -- host-side launchers of the BRMerge kernels (one GPU; a main stream and an
+// optional second stream).
 #pragma once
 
 #include <mutex>
