@@ -16,7 +16,10 @@
  *
  * Every function returns a brm_status (0 on success) instead of the
  * reference's assert/throw.  A context binds to the device that is current
- * when it is created and serialises its work on one CUDA stream; separate
+ * when it is created and orders its work on one CUDA stream (brm_set_stream);
+ * inside a call it also uses a second stream of its own, forked from and
+ * joined back into that stream with events, so every call stays in order on
+ * the caller's stream and can be captured in a CUDA graph.  Separate
  * contexts may run concurrently on separate streams.
  */
 #ifndef BRMERGE_H
