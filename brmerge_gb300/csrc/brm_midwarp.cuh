@@ -15,10 +15,12 @@
 //      lists, ceil(log2 lists) levels (merge path: every lane a contiguous
 //      share of the output); the keys are unique and equal columns end in
 //      leaf order;
-//   4. the runs of one column are listed and lane i reduces runs i, i + 32,
-//      ... with the merge-tree rule (adjacent leaves join at their split
-//      level: closed forms up to four leaves, a register shift-reduce beyond,
-//      spgemm.h:639-707), values recomputed from A and B at this point.
+//   4. the runs of one column are listed and reduced with the merge-tree rule
+//      (adjacent leaves join at their split level, a register shift-reduce,
+//      spgemm.h:639-707), values recomputed from A and B at this point; the
+//      products are split evenly over the lanes (a lane takes the runs that
+//      start in its share), so long runs do not leave the other lanes idle.
+//      Tile rows keep one lane per run (closed forms up to four leaves).
 //
 // The same kernel counts the row (symbolic), writes it at crpt (Precise), at
 // the row's product offset (Upper) or into the one-call scratch.
@@ -266,79 +268,77 @@ __device__ __forceinline__ void warp_sort_small(unsigned *keys, int F)
     __syncwarp();
 }
 
-// Values of the runs h = t, t + NT, ... of sorted keys (run h covers
-// key[head[h], head[h + 1])).  The runs are taken U at a time and the
-// products of runs of at most 4 are loaded before any is reduced, so that
-// several B gathers are in flight per thread; longer runs load as they
-// reduce.
-template <typename T, int NT, int IDX, int U>
-__device__ __forceinline__ void mw_reduce_runs(const unsigned *key, const unsigned *head, int len,
-                                               int t, int k, const unsigned char *plist,
-                                               const unsigned char *lleaf, const int *lbs,
-                                               const unsigned short *loff,
-                                               const T *__restrict__ arow,
-                                               const T *__restrict__ bval, int cmin, int *ccol,
-                                               T *cval)
+// Values of all runs with the products split evenly over the NT threads:
+// thread t takes the runs that start among products [t F / NT, (t + 1) F / NT)
+// and walks their products in order (run h covers key[head[h], head[h + 1]),
+// head[len] = F), gathering GB products ahead of the merge-tree reduction.
+// Every thread then handles about F / NT products however long the runs are
+// (a lane per run leaves most lanes idle while one reduces a long run).
+template <typename T, int NT, int IDX, int D, int GB>
+__device__ __forceinline__ void mw_reduce_balanced(const unsigned *key, const unsigned *head,
+                                                   int len, int F, int t,
+                                                   const unsigned char *plist,
+                                                   const unsigned char *lleaf, const int *lbs,
+                                                   const unsigned short *loff,
+                                                   const T *__restrict__ arow,
+                                                   const T *__restrict__ bval, int cmin, int *ccol,
+                                                   T *cval)
 {
     constexpr unsigned imask = (1u << IDX) - 1u;
-    for (int hb = t; hb < len; hb += U * NT) {
-        int p[U], m[U];
-        unsigned lf[U];  // leaves of the first 4 products, a byte each
-        T v[U][4];
+    // first run that starts at or after product q (len if none)
+    auto first_run = [&](int q) {
+        int lo = 0, hi = len;
+        while (lo < hi) {
+            const int m = (lo + hi) >> 1;
+            if ((int)head[m] < q)
+                lo = m + 1;
+            else
+                hi = m;
+        }
+        return lo;
+    };
+    const int h0 = first_run((int)((long long)t * F / NT));
+    const int h1 = first_run((int)((long long)(t + 1) * F / NT));
+    if (h0 >= h1)
+        return;
+    const int pend = (int)head[h1];
+    int h = h0;
+    int next = (int)head[h0 + 1];
+    RegShiftReduce<T, D> sr;
+    for (int p0 = (int)head[h0]; p0 < pend; p0 += GB) {
+        int lf[GB];
+        T v[GB];
 #pragma unroll
-        for (int u = 0; u < U; u++) {
-            const int h = hb + u * NT;
-            p[u] = h < len ? (int)head[h] : 0;
-            m[u] = h < len ? (int)head[h + 1] - p[u] : 0;
+        for (int q = 0; q < GB; q++) {
+            lf[q] = 0;
+            v[q] = T(0);
+            if (p0 + q < pend) {
+                const int e = (int)(key[p0 + q] & imask);
+                const int j = plist[e];
+                lf[q] = lleaf[j];
+                v[q] = vmul(arow[lf[q]], bval[lbs[j] + (e - loff[j])]);
+            }
         }
 #pragma unroll
-        for (int u = 0; u < U; u++) {
-            lf[u] = 0;
-#pragma unroll
-            for (int q = 0; q < 4; q++) {
-                v[u][q] = T(0);
-                if (q < m[u] && m[u] <= 4) {
-                    const int e = (int)(key[p[u] + q] & imask);
-                    const int j = plist[e];
-                    const int l = lleaf[j];
-                    lf[u] |= (unsigned)l << (8 * q);
-                    v[u][q] = vmul(arow[l], bval[lbs[j] + (e - loff[j])]);
+        for (int q = 0; q < GB; q++) {
+            const int p = p0 + q;
+            if (p < pend) {
+                if (p == (int)head[h0]) {
+                    sr.init(lf[q], v[q]);
+                } else if (p == next) {  // run h is complete
+                    ccol[h] = cmin + (int)(key[head[h]] >> IDX);
+                    cval[h] = sr.finish();
+                    h++;
+                    next = (int)head[h + 1];
+                    sr.init(lf[q], v[q]);
+                } else {
+                    sr.push(lf[q], v[q]);
                 }
             }
         }
-#pragma unroll
-        for (int u = 0; u < U; u++) {
-            const int h = hb + u * NT;
-            if (h >= len)
-                break;
-            const unsigned *run = key + p[u];
-            T r;
-            if (m[u] == 1) {
-                r = v[u][0];
-            } else if (m[u] == 2) {
-                r = vadd(v[u][0], v[u][1]);
-            } else if (m[u] == 3) {
-                r = trie3((int)(lf[u] & 255u), (int)((lf[u] >> 8) & 255u),
-                          (int)((lf[u] >> 16) & 255u), v[u][0], v[u][1], v[u][2]);
-            } else if (m[u] == 4) {
-                r = trie4((int)(lf[u] & 255u), (int)((lf[u] >> 8) & 255u),
-                          (int)((lf[u] >> 16) & 255u), (int)(lf[u] >> 24), v[u][0], v[u][1],
-                          v[u][2], v[u][3]);
-            } else {
-                auto leaf = [&](int i) { return (int)lleaf[plist[run[i] & imask]]; };
-                auto val = [&](int i) {
-                    const int e = (int)(run[i] & imask);
-                    const int j = plist[e];
-                    return vmul(arow[lleaf[j]], bval[lbs[j] + (e - loff[j])]);
-                };
-                // leaves below 32 need at most 5 stack entries below the top
-                r = k <= 32 ? mw_run_value<T, 6>(m[u], leaf, val)
-                            : mw_run_value<T, 9>(m[u], leaf, val);
-            }
-            ccol[h] = cmin + (int)(run[0] >> IDX);
-            cval[h] = r;
-        }
     }
+    ccol[h] = cmin + (int)(key[head[h]] >> IDX);
+    cval[h] = sr.finish();
 }
 
 template <typename T, int MODE, int SID>
@@ -459,8 +459,8 @@ __global__ void __launch_bounds__(mw_threads<SID>(), 2) k_mid_warp(CsrDev A, Csr
             }
         }
         // 4. runs of one column: each thread finds the heads (first products
-        //    of runs) in its share, they are listed in order, and thread i
-        //    reduces runs i, i + NT, ... (coalesced stores)
+        //    of runs) in its share, they are listed in order, and every
+        //    thread reduces the runs that start in its share of the products
         int nh = 0;
         for (int p = p0; p < p1; p++)
             nh += p == 0 || (src[p] >> IDX) != (src[p - 1] >> IDX);
@@ -492,9 +492,12 @@ __global__ void __launch_bounds__(mw_threads<SID>(), 2) k_mid_warp(CsrDev A, Csr
             P.nnz[row] = len;
         // gathers in flight: two runs a thread within 80 registers, four
         // with 128
-        constexpr int RU = S::GROUPS * NT > 256 ? 2 : 4;
-        mw_reduce_runs<T, NT, IDX, RU>(src, dst, len, t, k, plist, lleaf, lbs, loff, aval + a0,
-                                       bval, cmin, ccol + base, cval + base);
+        if (k <= 32)
+            mw_reduce_balanced<T, NT, IDX, 6, 4>(src, dst, len, F, t, plist, lleaf, lbs, loff,
+                                                 aval + a0, bval, cmin, ccol + base, cval + base);
+        else
+            mw_reduce_balanced<T, NT, IDX, 9, 4>(src, dst, len, F, t, plist, lleaf, lbs, loff,
+                                                 aval + a0, bval, cmin, ccol + base, cval + base);
         grp_sync<G>(gid);
     }
 }
