@@ -260,8 +260,10 @@ def upload_pairs(pairs, dev):
 
 
 def device_steps(call, dev, stream, flush, steps: int, warmup: int = 2):
-    """Mean CUDA-event time (ms) of `call()` on `stream`, L2 flushed before
-    every timed call; returns (ms, last result)."""
+    """Median CUDA-event time (ms) of `call()` on `stream`, L2 flushed before
+    every timed call; returns (ms, last result).  The side sections report the
+    median, so that one stalled call (seen now and then on the shared boxes)
+    does not move them; the headline step keeps the mean of its K steps."""
     import torch
     out = None
     for _ in range(warmup):
@@ -279,7 +281,7 @@ def device_steps(call, dev, stream, flush, steps: int, warmup: int = 2):
         ts.append(e0.elapsed_time(e1))
         if i + 1 < steps:
             del out
-    return statistics.mean(ts), out
+    return statistics.median(ts), out
 
 
 def method_entry(ms: float, products: int, alg_bytes: int, peak: float) -> dict:
@@ -618,7 +620,7 @@ def run_ours(args):
     batched = served = stencil = reader = None
     if not args.no_batch:
         reader = reader_section(ctx, A, max(1, min(args.steps, 3)))
-        stencil = stencil_section(ctx, dev, stream, flush, max(1, min(args.steps, 3)), peak)
+        stencil = stencil_section(ctx, dev, stream, flush, max(1, min(args.steps, 5)), peak)
         batched = batched_section(ctx, dev, stream, steps=max(1, min(args.steps, 3)))
         served = [served_section(dev, rate, args.serve_requests) for rate in (2000.0, 400.0, 150.0)]
     if rank != 0:
