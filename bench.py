@@ -94,6 +94,7 @@ class ClockSampler:
         self.idx = gpu_index
         self.proc = None
         self.lines = []
+        self.pre = []
 
     def __enter__(self):
         try:
@@ -103,6 +104,13 @@ class ClockSampler:
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
+            # wait for the first sample: nvidia-smi's start-up (NVML
+            # initialisation) then lies before the timed region, not in it
+            t_end = time.time() + 5.0
+            while not self.lines and self.proc.poll() is None and time.time() < t_end:
+                time.sleep(0.01)
+            self.pre = list(self.lines)  # the sample taken just before the region
+            self.lines.clear()
         except Exception:
             self.proc = None
         return self
@@ -122,7 +130,9 @@ class ClockSampler:
     def summary(self):
         sm, smax, reasons = [], 0.0, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
+        # samples inside the timed region; a region shorter than the sampling
+        # period falls back to the one taken just before it
+        for ln in (self.lines or self.pre):
             parts = [p.strip() for p in ln.split(",")]
             if len(parts) < 8:
                 continue

@@ -616,6 +616,8 @@ __global__ void __launch_bounds__(kSegThreads) k_seg_numeric(CsrDev A, CsrDev B,
             loff[nlists] = nprod;
             misc[1] = 0;  // long runs
             misc[2] = 0;  // staged column out of range
+            misc[3] = 0;  // listed columns of three or four products
+            misc[4] = 0;  // listed columns of five to eight products
         }
         // a segment spanning at most 32 * kSegCap columns ranks its columns
         // with one flat bitmap in cw (a prefix per word); wider ones with a
@@ -788,7 +790,11 @@ __global__ void __launch_bounds__(kSegThreads) k_seg_numeric(CsrDev A, CsrDev B,
                 S[ucnt[pu[p]] + ia[p]] = (unsigned short)p;
         }
         __syncthreads();
-        // one thread per output column (consecutive columns -> coalesced stores)
+        // one thread per output column of one or two products (consecutive
+        // columns -> coalesced stores); columns of three or four and of five to
+        // eight products are listed (at the front and the back of pu, dead
+        // after the scatter) and reduced by a second, dense pass, so that the
+        // lanes of a warp run the same code; longer columns go to longu
         for (int u = tid; u < U; u += NT) {
             int i0 = u, len = 1;
             if (!nodup) {
@@ -804,6 +810,28 @@ __global__ void __launch_bounds__(kSegThreads) k_seg_numeric(CsrDev A, CsrDev B,
                 v = pleaf[e0] < pleaf[e1] ? vadd(pval[e0], pval[e1])   // left + right
                                           : vadd(pval[e1], pval[e0]);
             } else if (len <= 4) {
+                pu[atomicAdd(&misc[3], 1)] = (unsigned short)u;
+                continue;
+            } else if (len <= 8) {
+                pu[kSegCap - 1 - atomicAdd(&misc[4], 1)] = (unsigned short)u;
+                continue;
+            } else {
+                const int li = atomicAdd(&misc[1], 1);
+                if (li < kLongMax)
+                    longu[li] = (unsigned short)u;
+                continue;
+            }
+            ccol[obase + u] = d.c_lo + prc[e0];
+            cval[obase + u] = v;
+        }
+        __syncthreads();
+        const int n34 = misc[3], nmid = n34 + misc[4];
+        for (int i = tid; i < nmid; i += NT) {
+            const int u = i < n34 ? pu[i] : pu[kSegCap - 1 - (i - n34)];
+            const int i0 = ucnt[u], len = ucnt[u + 1] - i0;
+            const int e0 = S[i0];
+            T v;
+            if (len <= 4) {
                 // sort the (leaf, value) pairs in registers, then the closed form
                 const int e1 = S[i0 + 1], e2 = S[i0 + 2];
                 int l0 = pleaf[e0], l1 = pleaf[e1], l2 = pleaf[e2];
@@ -824,7 +852,7 @@ __global__ void __launch_bounds__(kSegThreads) k_seg_numeric(CsrDev A, CsrDev B,
                     leaf_cas(l1, v1, l2, v2);
                     v = trie4(l0, l1, l2, l3, v0, v1, v2, v3);
                 }
-            } else if (len <= 8) {
+            } else {
                 // sorting network and a register stack
                 int l8[8];
                 T v8[8];
@@ -847,11 +875,6 @@ __global__ void __launch_bounds__(kSegThreads) k_seg_numeric(CsrDev A, CsrDev B,
                     if (j < len)
                         sr.push(l8[j], v8[j]);
                 v = sr.finish();
-            } else {
-                const int li = atomicAdd(&misc[1], 1);
-                if (li < kLongMax)
-                    longu[li] = (unsigned short)u;
-                continue;
             }
             ccol[obase + u] = d.c_lo + prc[e0];
             cval[obase + u] = v;
