@@ -49,6 +49,20 @@ def level_pairs(leaves, vals):
     return nodes[0][1]
 
 
+def aligned_ranges(leaves, vals):
+    """Mirror of the long-column warp reducer (k_long_warp): the leaves are cut
+    into the 32 aligned ranges of 2^s leaves (s = bits of the largest leaf - 5),
+    each range is one subtree of the trie and is reduced on its own, and the
+    range values are joined by the trie over the range indices."""
+    s = max((leaves[-1] | 1).bit_length() - 5, 0)
+    ranges = {}
+    for l, v in zip(leaves, vals):
+        ranges.setdefault(l >> s, []).append((l, v))
+    idx = sorted(ranges)
+    sub = [shift_reduce([x[0] for x in ranges[j]], [x[1] for x in ranges[j]]) for j in idx]
+    return shift_reduce(idx, sub)
+
+
 def trie_product(A, B, reducer):
     rows, cols, vals = [], [], []
     for i in range(A.M):
@@ -68,7 +82,7 @@ def trie_product(A, B, reducer):
                np.array(vals, np.float64))
 
 
-@pytest.mark.parametrize("reducer", [shift_reduce, level_pairs])
+@pytest.mark.parametrize("reducer", [shift_reduce, level_pairs, aligned_ranges])
 @pytest.mark.parametrize("seed", range(3))
 def test_trie_forms_match_oracle(oracle_mod, reducer, seed):
     from brmerge_gb300 import gen_uniform
@@ -89,3 +103,15 @@ def test_trie_order_differs_from_sequential_sum():
             seq = np.float64(seq + x)
         diffs += shift_reduce(list(range(7)), list(v)) != seq
     assert diffs > 0
+
+
+@pytest.mark.parametrize("reducer", [shift_reduce, aligned_ranges])
+@pytest.mark.parametrize("seed", range(2))
+def test_trie_forms_wide_rows(oracle_mod, reducer, seed):
+    """Rows of 200 lists: columns with many products at leaves up to 199, so
+    the aligned ranges of the warp reducer span 8 leaves each."""
+    from brmerge_gb300 import gen_uniform
+    from conftest import assert_same_csr
+    A = gen_uniform(6, 600, 200, seed=seed)
+    B = gen_uniform(600, 40, 10, seed=seed + 100)
+    assert_same_csr(trie_product(A, B, reducer), oracle_mod.precise(A, B), reducer.__name__)
