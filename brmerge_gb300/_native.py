@@ -108,6 +108,7 @@ def lib() -> C.CDLL:
         _decl(L.brm_set_stream, C.c_int, [vp, vp])
         _decl(L.brm_set_validate, C.c_int, [vp, C.c_int])
         _decl(L.brm_last_device_error, C.c_int, [vp])
+        _decl(L.brm_device_code_version, C.c_int, [c_int_p])
         _decl(L.brm_symbolic, C.c_int, [vp, csrp, csrp, vp, c_int_p])
         _decl(L.brm_numeric, C.c_int, [vp, C.c_int, csrp, csrp, vp, vp, vp])
         _decl(L.brm_precise_device, C.c_int,

@@ -523,3 +523,18 @@ void launch_validate(const CsrDev &X, int ncols, int *bad_row, cudaStream_t s)
 }
 
 }  // namespace brm
+
+// SM version of the device code this library runs on the current device.
+extern "C" int brm_device_code_version(int *sm)
+{
+    if (!sm)
+        return BRM_ERR_INVALID_VALUE;
+    cudaFuncAttributes fa;
+    const cudaError_t e = cudaFuncGetAttributes(&fa, brm::k_scan_reduce);
+    if (e != cudaSuccess) {
+        (void)cudaGetLastError();
+        return e == cudaErrorNoDevice ? BRM_ERR_NO_DEVICE : BRM_ERR_CUDA;
+    }
+    *sm = fa.binaryVersion;
+    return BRM_SUCCESS;
+}

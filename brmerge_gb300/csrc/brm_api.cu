@@ -30,7 +30,27 @@ struct DevBuf {
     size_t cap = 0;
 };
 
-constexpr int kNumEvents = 12;
+// CUDA events of a timed call, in stream order: kEvIn before the host-to-device
+// copies of a host drop-in; kEvStart .. kEvScan around the planning phases;
+// kEvNum0/kEvNum1 around the numeric phase; kEvScan2 after Upper's nnz scan;
+// kEvCopy0/kEvCopy1 around Upper's compaction; kEvOut after the last copy
+// of C back to the host.
+enum TimingEvent : int {
+    kEvStart = 0,   // start of the plan
+    kEvAna = 1,     // after the row analysis (products per row, bins)
+    kEvSym = 2,     // after the symbolic phase
+    kEvScan = 3,    // after the crpt (Precise) or scan_flop (Upper) scan
+    kEvNum0 = 4,
+    kEvNum1 = 5,
+    kEvScan2 = 6,
+    kEvCopy0 = 7,
+    kEvCopy1 = 8,
+    kEvPre = 9,     // after the prefix sums of the mid-row products
+    kEvSized = 10,  // after the host read of the bin counts and buffer sizing
+    kEvIn = 11,
+    kEvOut = 12,
+    kNumEvents = 13
+};
 constexpr long long kLongElems = 16ll << 20;  // products in the long-column scratch
 // candidates of brm_autotune (heavy-row cut target x mid-row weight limit)
 constexpr int kTuneSegCut[] = {1536, 1024, 768, 512};
@@ -296,8 +316,34 @@ double ev_sec(brm_context ctx, int a, int b)
     return ms * 1e-3;
 }
 
+// Planning phase fields of the timing structs, from the events of a timed
+// plan_phase.  Precise: compute_flop = row analysis and binning,
+// prefix_sum_flop = prefix sums of the mid-row products and batch starts,
+// load_balance = host read of the bin counts and sizing of the segment and
+// scratch buffers, symbolic = exact row nnz (heavy-row planning included),
+// prefix_sum_nnz = crpt scan.
+void plan_times(brm_context ctx, brm_precise_timing *t)
+{
+    t->compute_flop = ev_sec(ctx, kEvStart, kEvAna);
+    t->prefix_sum_flop = ev_sec(ctx, kEvAna, kEvPre);
+    t->load_balance = ev_sec(ctx, kEvPre, kEvSized);
+    t->symbolic = ev_sec(ctx, kEvSized, kEvSym);
+    t->prefix_sum_nnz = ev_sec(ctx, kEvSym, kEvScan);
+}
+
+// Upper (spgemm.h:220-457 has no symbolic pass): compute_flop = row
+// analysis, prefix_sum_flop = the mid-row prefix sums and the scan_flop scan,
+// load_balance = buffer sizing plus the heavy-row planning that cuts long
+// rows into balanced segments.
+void plan_times_upper(brm_context ctx, brm_upper_timing *t)
+{
+    t->compute_flop = ev_sec(ctx, kEvStart, kEvAna);
+    t->prefix_sum_flop = ev_sec(ctx, kEvAna, kEvPre) + ev_sec(ctx, kEvSym, kEvScan);
+    t->load_balance = ev_sec(ctx, kEvPre, kEvSym);
+}
+
 // Analysis + symbolic (+ crpt scan for Precise).  Leaves ctx->h_cnt filled.
-// Event indices: 0 start, 1 after analysis, 2 after symbolic, 3 after scan.
+// Timed: events kEvStart, kEvAna, kEvPre, kEvSized, kEvSym, kEvScan.
 // fused_dtype >= 0 (one-call Precise only): the mid rows are computed here,
 // values included, into ctx->midbuf, and the numeric phase only moves them.
 int plan_phase(brm_context ctx, const brm_csr *A, const brm_csr *B, int *crpt, bool upper,
@@ -316,10 +362,12 @@ int plan_phase(brm_context ctx, const brm_csr *A, const brm_csr *B, int *crpt, b
     ctx->plan.seg_range = nullptr;
     brm::PlanDev P = ctx->plan;
     cudaStream_t s = ctx->stream;
-    ev_record(ctx, timed, 0);
+    ev_record(ctx, timed, kEvStart);
     BRM_CK(cudaMemsetAsync(P.cnt, 0, sizeof(brm::Counters), s));
     brm::launch_analyze(a, b, P, s);
+    ev_record(ctx, timed, kEvAna);
     brm::launch_batches(P, A->M, ctx->scan_tmp, s);
+    ev_record(ctx, timed, kEvPre);
     // the segment descriptors of heavy rows are sized by the analysis
     BRM_CK(cudaGetLastError());
     BRM_CK(cudaMemcpyAsync(ctx->h_cnt, P.cnt, sizeof(brm::Counters), cudaMemcpyDeviceToHost, s));
@@ -347,7 +395,7 @@ int plan_phase(brm_context ctx, const brm_csr *A, const brm_csr *B, int *crpt, b
         ctx->plan.seg = P.seg;
         ctx->plan.seg_list = P.seg_list;
     }
-    ev_record(ctx, timed, 1);
+    ev_record(ctx, timed, kEvSized);
     if (fused) {
         // the batched and four-warp group mid rows (values into the scratch)
         // on the second stream, beside the warp-row counts, the heavy-row
@@ -373,12 +421,12 @@ int plan_phase(brm_context ctx, const brm_csr *A, const brm_csr *B, int *crpt, b
                                         brm::kMidWarps);
         BRM_CK(cudaStreamWaitEvent(s, ctx->fork.join, 0));
     }
-    ev_record(ctx, timed, 2);
+    ev_record(ctx, timed, kEvSym);
     if (upper)
         brm::launch_scan_i64(P.flop, P.scan_flop, A->M, ctx->scan_tmp, s);
     else
         brm::launch_scan_i32(P.nnz, crpt, A->M, P.cnt, ctx->scan_tmp, s);
-    ev_record(ctx, timed, 3);
+    ev_record(ctx, timed, kEvScan);
     BRM_CK(cudaGetLastError());
     BRM_CK(cudaMemcpyAsync(ctx->h_cnt, P.cnt, sizeof(brm::Counters), cudaMemcpyDeviceToHost, s));
     BRM_CK(cudaStreamSynchronize(s));
@@ -510,7 +558,7 @@ double now_sec()
 // blocks.  crpt (device io_crpt) is copied first; it also gives the cuts.
 int numeric_by_parts(brm_context ctx, brm_dtype dtype, const brm_csr *A, const brm_csr *B, int M,
                      int cnnz, size_t vb, int *h_rpt, int *h_col, void *h_val, int *dcol,
-                     void *dval)
+                     void *dval, bool timed)
 {
     cudaStream_t s = ctx->stream, cs = ctx->copy_stream;
     const int *d_rpt = (const int *)ctx->io_crpt.p;
@@ -521,6 +569,7 @@ int numeric_by_parts(brm_context ctx, brm_dtype dtype, const brm_csr *A, const b
     const int nparts = (int)std::min<long long>(kHostParts, std::max<long long>(1, bytes >> 25));
     if (nparts <= 1) {
         BRM_TRY(numeric_launch(ctx, dtype, false, A, B, d_rpt, dcol, dval, true));
+        ev_record(ctx, timed, kEvNum1);
         if (cnnz > 0) {
             BRM_CK(cudaMemcpyAsync(h_col, dcol, 4 * (size_t)cnnz, cudaMemcpyDeviceToHost, s));
             BRM_CK(cudaMemcpyAsync((char *)h_val, dval, vb * (size_t)cnnz, cudaMemcpyDeviceToHost, s));
@@ -582,7 +631,11 @@ int numeric_by_parts(brm_context ctx, brm_dtype dtype, const brm_csr *A, const b
                                    vb * (size_t)(e1 - e0), cudaMemcpyDeviceToHost, cs));
         }
     }
-    BRM_CK(cudaStreamSynchronize(cs));
+    ev_record(ctx, timed, kEvNum1);
+    // the context stream waits for the copies (the caller synchronises it)
+    cudaEvent_t done = ctx->part_ev[brm::kMaxParts - 1];
+    BRM_CK(cudaEventRecord(done, cs));
+    BRM_CK(cudaStreamWaitEvent(s, done, 0));
     return BRM_SUCCESS;
 }
 
@@ -621,9 +674,16 @@ int host_call(bool upper, const int *arpt, const int *acol, const T *aval, const
     if (nnzA < 0 || nnzB < 0 || (nnzA > 0 && (!acol || !aval)) || (nnzB > 0 && (!bcol || !bval)))
         return BRM_ERR_INVALID_VALUE;
     const bool same = (arpt == brpt && acol == bcol && aval == bval && M == K);
+    const bool timed = pt || ut;
     BRM_TRY(grow(ctx->io_arpt, 4 * ((size_t)M + 1)));
     BRM_TRY(grow(ctx->io_acol, 4 * (size_t)nnzA));
     BRM_TRY(grow(ctx->io_aval, sizeof(T) * (size_t)nnzA));
+    if (!same) {
+        BRM_TRY(grow(ctx->io_brpt, 4 * ((size_t)K + 1)));
+        BRM_TRY(grow(ctx->io_bcol, 4 * (size_t)nnzB));
+        BRM_TRY(grow(ctx->io_bval, sizeof(T) * (size_t)nnzB));
+    }
+    ev_record(ctx, timed, kEvIn);
     BRM_CK(cudaMemcpyAsync(ctx->io_arpt.p, arpt, 4 * ((size_t)M + 1), cudaMemcpyHostToDevice, s));
     BRM_CK(cudaMemcpyAsync(ctx->io_acol.p, acol, 4 * (size_t)nnzA, cudaMemcpyHostToDevice, s));
     BRM_CK(cudaMemcpyAsync(ctx->io_aval.p, aval, sizeof(T) * (size_t)nnzA, cudaMemcpyHostToDevice, s));
@@ -631,9 +691,6 @@ int host_call(bool upper, const int *arpt, const int *acol, const T *aval, const
     brm_csr B = A;
     B.N = N;
     if (!same) {
-        BRM_TRY(grow(ctx->io_brpt, 4 * ((size_t)K + 1)));
-        BRM_TRY(grow(ctx->io_bcol, 4 * (size_t)nnzB));
-        BRM_TRY(grow(ctx->io_bval, sizeof(T) * (size_t)nnzB));
         BRM_CK(cudaMemcpyAsync(ctx->io_brpt.p, brpt, 4 * ((size_t)K + 1), cudaMemcpyHostToDevice, s));
         BRM_CK(cudaMemcpyAsync(ctx->io_bcol.p, bcol, 4 * (size_t)nnzB, cudaMemcpyHostToDevice, s));
         BRM_CK(cudaMemcpyAsync(ctx->io_bval.p, bval, sizeof(T) * (size_t)nnzB, cudaMemcpyHostToDevice, s));
@@ -669,19 +726,23 @@ int host_call(bool upper, const int *arpt, const int *acol, const T *aval, const
         t_sym0 = now_sec();
         BRM_TRY(check_pair(&A, &B));
         ctx->planned = false;
-        BRM_TRY(plan_phase(ctx, &A, &B, (int *)ctx->io_crpt.p, false, false, dtype));
+        BRM_TRY(plan_phase(ctx, &A, &B, (int *)ctx->io_crpt.p, false, timed, dtype));
         cnnz = (int)ctx->h_cnt->cnnz;
         t_sym1 = now_sec();
         BRM_TRY(alloc_results());
         t_num0 = now_sec();
+        ev_record(ctx, timed, kEvNum0);
         BRM_TRY(numeric_by_parts(ctx, dtype, &A, &B, M, cnnz, sizeof(T), R.rpt, R.col, R.val, dcol,
-                                 dval));
+                                 dval, timed));
         copied = true;
     } else {
         t_sym0 = now_sec();
-        BRM_TRY(plan_phase(ctx, &A, &B, nullptr, true, false));
+        BRM_TRY(plan_phase(ctx, &A, &B, nullptr, true, timed));
+        ev_record(ctx, timed, kEvNum0);
         BRM_TRY(upper_numeric_into_bar(ctx, dtype, &A, &B));
+        ev_record(ctx, timed, kEvNum1);
         brm::launch_scan_i32(ctx->plan.nnz, (int *)ctx->io_crpt.p, M, ctx->plan.cnt, ctx->scan_tmp, s);
+        ev_record(ctx, timed, kEvScan2);
         BRM_CK(cudaGetLastError());
         BRM_CK(cudaMemcpyAsync(ctx->h_cnt, ctx->plan.cnt, sizeof(brm::Counters), cudaMemcpyDeviceToHost, s));
         BRM_CK(cudaStreamSynchronize(s));
@@ -691,8 +752,10 @@ int host_call(bool upper, const int *arpt, const int *acol, const T *aval, const
         t_sym1 = now_sec();
         BRM_TRY(alloc_results());
         t_num0 = now_sec();
+        ev_record(ctx, timed, kEvCopy0);
         brm::launch_compact(dtype == BRM_F64 ? 0 : 1, ctx->plan, (const int *)ctx->bar_col.p,
                             ctx->bar_val.p, (const int *)ctx->io_crpt.p, dcol, dval, s);
+        ev_record(ctx, timed, kEvCopy1);
         BRM_CK(cudaGetLastError());
     }
     if (!copied) {
@@ -702,6 +765,8 @@ int host_call(bool upper, const int *arpt, const int *acol, const T *aval, const
             BRM_CK(cudaMemcpyAsync(R.val, dval, sizeof(T) * (size_t)cnnz, cudaMemcpyDeviceToHost, s));
         }
     }
+    if (timed)  // every copy of C back to the host has been issued on s or joined into it
+        BRM_CK(cudaEventRecord(ctx->ev[kEvOut], s));
     BRM_TRY(read_err(ctx));  // synchronises the stream
     t_num1 = now_sec();
     int *crpt = R.rpt, *ccol = R.col;
@@ -712,22 +777,31 @@ int host_call(bool upper, const int *arpt, const int *acol, const T *aval, const
     *ccol_ = ccol;
     *cval_ = cval;
     *cnnz_ = cnnz;
+    (void)t_pre;
+    (void)t_sym0;
+    // phases from the call's CUDA events; pre_allocate = the host-to-device
+    // copies of A and B (plus the workspace set-up before the plan starts),
+    // allocate_C = host wall time between the symbolic and numeric phases
+    // (result blocks), cleanup = the copy of C back to the host that is not
+    // overlapped with the numeric phase
     if (pt) {
         std::memset(pt, 0, sizeof(*pt));
-        pt->pre_allocate = t_pre - t_start;
-        pt->symbolic = t_sym1 - t_sym0;
+        pt->pre_allocate = ev_sec(ctx, kEvIn, kEvStart);
+        plan_times(ctx, pt);
         pt->allocate_C = t_num0 - t_sym1;
-        pt->compute = t_num1 - t_num0;
-        pt->cleanup = t_end - t_num1;
+        pt->compute = ev_sec(ctx, kEvNum0, kEvNum1);
+        pt->cleanup = ev_sec(ctx, kEvNum1, kEvOut);
         pt->total = t_end - t_start;
     }
     if (ut) {
         std::memset(ut, 0, sizeof(*ut));
-        ut->pre_allocate = t_pre - t_start;
-        ut->compute = t_sym1 - t_sym0;
+        ut->pre_allocate = ev_sec(ctx, kEvIn, kEvStart);
+        plan_times_upper(ctx, ut);
+        ut->compute = ev_sec(ctx, kEvNum0, kEvNum1);
+        ut->prefix_sum_nnz = ev_sec(ctx, kEvNum1, kEvScan2);
         ut->allocate_C = t_num0 - t_sym1;
-        ut->copy = t_num1 - t_num0;
-        ut->cleanup = t_end - t_num1;
+        ut->copy = ev_sec(ctx, kEvCopy0, kEvCopy1);
+        ut->cleanup = ev_sec(ctx, kEvCopy1, kEvOut);
         ut->total = t_end - t_start;
     }
     return BRM_SUCCESS;
@@ -1049,9 +1123,9 @@ int brm_precise_device(brm_context ctx, brm_dtype dtype, const brm_csr *A, const
         return cuda_status(e);
     }
     double t3 = now_sec();
-    ev_record(ctx, timed, 4);
+    ev_record(ctx, timed, kEvNum0);
     st = numeric_launch(ctx, dtype, false, A, B, crpt, ccol, cval, true);
-    ev_record(ctx, timed, 5);
+    ev_record(ctx, timed, kEvNum1);
     if (st == BRM_SUCCESS)
         st = read_err(ctx);
     if (st != BRM_SUCCESS) {
@@ -1068,11 +1142,9 @@ int brm_precise_device(brm_context ctx, brm_dtype dtype, const brm_csr *A, const
     if (timed) {
         std::memset(timing, 0, sizeof(*timing));
         timing->pre_allocate = t1 - t0;
-        timing->compute_flop = ev_sec(ctx, 0, 1);
-        timing->symbolic = ev_sec(ctx, 1, 2);
-        timing->prefix_sum_nnz = ev_sec(ctx, 2, 3);
+        plan_times(ctx, timing);
         timing->allocate_C = t3 - t2;
-        timing->compute = ev_sec(ctx, 4, 5);
+        timing->compute = ev_sec(ctx, kEvNum0, kEvNum1);
         timing->total = t4 - t0;
     }
     return BRM_SUCCESS;
@@ -1095,12 +1167,12 @@ int brm_upper_device(brm_context ctx, brm_dtype dtype, const brm_csr *A, const b
     double t2 = now_sec();
     int *crpt = nullptr;
     BRM_CK(cudaMallocAsync((void **)&crpt, 4 * ((size_t)A->M + 1), ctx->stream));
-    ev_record(ctx, timed, 4);
+    ev_record(ctx, timed, kEvNum0);
     int st = numeric_launch(ctx, dtype, true, A, B, nullptr, (int *)ctx->bar_col.p, ctx->bar_val.p);
-    ev_record(ctx, timed, 5);
+    ev_record(ctx, timed, kEvNum1);
     if (st == BRM_SUCCESS) {
         brm::launch_scan_i32(ctx->plan.nnz, crpt, A->M, ctx->plan.cnt, ctx->scan_tmp, ctx->stream);
-        ev_record(ctx, timed, 6);
+        ev_record(ctx, timed, kEvScan2);
         cudaError_t e = cudaMemcpyAsync(ctx->h_cnt, ctx->plan.cnt, sizeof(brm::Counters),
                                         cudaMemcpyDeviceToHost, ctx->stream);
         if (e == cudaSuccess)
@@ -1130,10 +1202,10 @@ int brm_upper_device(brm_context ctx, brm_dtype dtype, const brm_csr *A, const b
         return cuda_status(e);
     }
     double t4 = now_sec();
-    ev_record(ctx, timed, 7);
+    ev_record(ctx, timed, kEvCopy0);
     brm::launch_compact(dtype == BRM_F64 ? 0 : 1, ctx->plan, (const int *)ctx->bar_col.p,
                         ctx->bar_val.p, crpt, ccol, cval, ctx->stream);
-    ev_record(ctx, timed, 8);
+    ev_record(ctx, timed, kEvCopy1);
     st = read_err(ctx);
     if (st != BRM_SUCCESS) {
         cudaFreeAsync(crpt, ctx->stream);
@@ -1148,14 +1220,12 @@ int brm_upper_device(brm_context ctx, brm_dtype dtype, const brm_csr *A, const b
     *cnnz_ = cnnz;
     if (timed) {
         std::memset(timing, 0, sizeof(*timing));
-        timing->compute_flop = ev_sec(ctx, 0, 1);
-        timing->load_balance = ev_sec(ctx, 1, 2);
-        timing->prefix_sum_flop = ev_sec(ctx, 2, 3);
+        plan_times_upper(ctx, timing);
         timing->allocate_hook = t2 - t1;
-        timing->compute = ev_sec(ctx, 4, 5);
-        timing->prefix_sum_nnz = ev_sec(ctx, 5, 6);
+        timing->compute = ev_sec(ctx, kEvNum0, kEvNum1);
+        timing->prefix_sum_nnz = ev_sec(ctx, kEvNum1, kEvScan2);
         timing->allocate_C = t4 - t3;
-        timing->copy = ev_sec(ctx, 7, 8);
+        timing->copy = ev_sec(ctx, kEvCopy0, kEvCopy1);
         timing->total = t5 - t0;
     }
     return BRM_SUCCESS;

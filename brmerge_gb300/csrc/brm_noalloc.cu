@@ -15,6 +15,12 @@
 // it, so calls whose work overlaps on the GPU (different streams, different
 // host threads) race on it; serialise them.  Each call clears what must start
 // at zero (the error word) and overwrites the rest.
+//
+// The device address of the array is looked up once per device and kept for
+// the life of the process.  A cudaDeviceReset (or anything else that tears
+// down and recreates the device's primary context) reloads this library's
+// device code at a possibly different address, so the kept address is stale
+// afterwards: do not use this entry point after resetting a device.
 #include <climits>
 #include <mutex>
 
@@ -30,11 +36,14 @@ constexpr long long kNoAllocMaxRows = (long long)kNoAllocMaxBlocks * kNoAllocRow
 constexpr int kMaxDevices = 64;
 
 // [0, kNoAllocMaxBlocks): per-block partial sums; [kNoAllocMaxBlocks]: total;
-// [kNoAllocMaxBlocks + 1]: error word (bad column index seen).
+// [kNoAllocMaxBlocks + 1]: error word (kNaBadInput | kNaRowOverflow).
 static __device__ __align__(256) unsigned long long g_noalloc_scratch[kNoAllocMaxBlocks + 2];
 
 // Host-side stand-ins are not device addresses: the device address of the
 // array is looked up once per device with that device current.
+constexpr unsigned long long kNaBadInput = 1;     // A.rpt, A.col or B.rpt not valid CSR
+constexpr unsigned long long kNaRowOverflow = 2;  // a row's count above INT_MAX
+
 std::mutex g_noalloc_mu;
 unsigned long long *g_noalloc_dev[kMaxDevices] = {};
 
@@ -48,7 +57,7 @@ __global__ void __launch_bounds__(kNoAllocThreads)
     const int M = A.M, K = B.M;
     const int rows_per_warp = kNoAllocRowsPerBlock / (kNoAllocThreads / 32);
     unsigned long long wsum = 0;
-    bool bad = false;
+    bool bad = false, big = false;
     for (int r = 0; r < rows_per_warp; r++) {
         const int row = blockIdx.x * kNoAllocRowsPerBlock + w * rows_per_warp + r;
         if (row >= M)
@@ -61,20 +70,31 @@ __global__ void __launch_bounds__(kNoAllocThreads)
         long long f = 0;
         for (int j = a0 + lane; j < a1; j += 32) {
             const int b = A.col[j];
-            if ((unsigned)b < (unsigned)K)
-                f += B.rpt[b + 1] - B.rpt[b];
-            else
+            if ((unsigned)b < (unsigned)K) {
+                const int b0 = B.rpt[b], b1 = B.rpt[b + 1];
+                if (b0 < 0 || b1 < b0)
+                    bad = true;  // a negative length would wrap the unsigned total
+                else
+                    f += b1 - b0;
+            } else {
                 bad = true;
+            }
         }
         f = brm::warp_sum(f);
         if (lane == 0) {
-            if (row_flop)
-                row_flop[row] = f > INT_MAX ? INT_MAX : (int)f;
+            // with valid CSR a row's count is at most nnz(B) <= INT_MAX; more
+            // means repeated columns in the A row, reported, never clamped
+            if (f > INT_MAX)
+                big = true;
+            else if (row_flop)
+                row_flop[row] = (int)f;
             wsum += (unsigned long long)f;
         }
     }
-    if (__any_sync(brm::kFull, bad) && lane == 0)
-        atomicOr(&scratch[kNoAllocMaxBlocks + 1], 1ull);
+    const unsigned long long ew = (__any_sync(brm::kFull, bad) ? kNaBadInput : 0ull) |
+                                  (__any_sync(brm::kFull, big) ? kNaRowOverflow : 0ull);
+    if (ew && lane == 0)
+        atomicOr(&scratch[kNoAllocMaxBlocks + 1], ew);
     if (lane == 0)
         s_part[w] = wsum;
     __syncthreads();
@@ -162,8 +182,10 @@ extern "C" int brm_compute_flop_noalloc(const brm_csr *A, const brm_csr *B, int 
         (void)cudaGetLastError();
         return BRM_ERR_CUDA;
     }
-    if (res[1])
+    if (res[1] & kNaBadInput)
         return BRM_ERR_INVALID_CSR;
+    if (res[1] & kNaRowOverflow)
+        return BRM_ERR_OVERFLOW;
     *products = (long long)res[0];
     return BRM_SUCCESS;
 }

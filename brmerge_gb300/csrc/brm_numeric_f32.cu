@@ -1,102 +1,21 @@
 // brm_numeric_f32.cu -- numeric phase launchers for float values.
-#include "brm_kernels.h"
-#include "brm_mid.cuh"
-#include "brm_midwarp.cuh"
-#include "brm_seg.cuh"
-#include "brm_rows.cuh"
+#include "brm_numeric.cuh"
 
 namespace brm {
-
-template <bool UPPER>
-static void numeric_f32(const CsrDev &A, const CsrDev &B, const PlanDev &P, const int *crpt,
-                       int *ccol, float *cval, void *spill_scratch, unsigned long long spill_bytes,
-                       const int *mid_col, const void *mid_val, int num_sms, cudaStream_t s0,
-                       const Fork &fk)
-{
-    // copy, warp and mid rows on the aux stream (when there is one), beside
-    // the split table and the segments of the heavy rows on s0
-    cudaStream_t s = s0;
-    if (fk.aux) {
-        cudaEventRecord(fk.fork, s0);
-        cudaStreamWaitEvent(fk.aux, fk.fork, 0);
-        s = fk.aux;
-    }
-    k_copy_numeric<float, UPPER><<<num_sms * 8, 256, 0, s>>>(A, B, P, crpt, ccol, cval);
-    count_launch();
-    k_warp_numeric<float, UPPER><<<num_sms * 8, 256, 0, s>>>(A, B, P, crpt, ccol, cval);
-    count_launch();
-    if (mid_col) {
-        // mid rows were computed with the plan (one-call Precise): move them
-        k_mid_compact<float><<<num_sms * 8, 256, 0, s>>>(P, A.M, mid_col, (const float *)mid_val,
-                                                          crpt, ccol, cval);
-        count_launch();
-    } else {
-        launch_mid_warp<float, UPPER ? kMwUpper : kMwPrecise>(A, B, P, crpt, ccol, cval, num_sms,
-                                                          s);
-        const size_t msm = MidNumLayout<float>::bytes;
-        cudaFuncSetAttribute(k_mid_numeric<float, UPPER>,
-                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)msm);
-        k_mid_numeric<float, UPPER><<<num_sms * 2, kMidThreads, msm, s>>>(A, B, P, crpt, ccol,
-                                                                            cval);
-        count_launch();
-    }
-    if (fk.aux)
-        cudaEventRecord(fk.join, fk.aux);
-    s = s0;
-    k_split<0><<<num_sms * 8, 256, 0, s>>>(A, B, P);
-    count_launch();
-    const size_t ssm = SegLayout<float>::bytes;
-    cudaFuncSetAttribute(k_seg_numeric<float, UPPER>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)ssm);
-    k_seg_numeric<float, UPPER><<<num_sms * 2, kSegThreads, ssm, s>>>(A, B, P, crpt, ccol, cval);
-    count_launch();
-    k_long_reduce<float><<<num_sms * 4, 128, 0, s>>>(P, ccol, cval);
-    count_launch();
-    k_long_warp<float><<<num_sms * 4, 128, 0, s>>>(P, ccol, cval);
-    count_launch();
-    const size_t smem = NumLayout<float>::bytes;
-    cudaFuncSetAttribute(k_rows_numeric<float, UPPER>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)smem);
-    k_rows_numeric<float, UPPER><<<num_sms, kRowThreads, smem, s>>>(A, B, P, crpt, ccol, cval);
-    count_launch();
-    if (spill_bytes) {
-        k_spill_numeric<float, UPPER><<<num_sms * 4, 32, 0, s>>>(
-            A, B, P, crpt, ccol, cval, (unsigned char *)spill_scratch, spill_bytes);
-        count_launch();
-    }
-    if (fk.aux)
-        cudaStreamWaitEvent(s0, fk.join, 0);
-}
 
 void launch_numeric_f32(bool upper, const CsrDev &A, const CsrDev &B, const PlanDev &P,
                        const int *crpt, int *ccol, void *cval, void *spill_scratch,
                        unsigned long long spill_bytes, const int *mid_col, const void *mid_val,
                        int num_sms, cudaStream_t s, const Fork &fk)
 {
-    if (A.M <= 0)
-        return;
-    if (upper)
-        numeric_f32<true>(A, B, P, crpt, ccol, (float *)cval, spill_scratch, spill_bytes, nullptr,
-                          nullptr, num_sms, s, fk);
-    else
-        numeric_f32<false>(A, B, P, crpt, ccol, (float *)cval, spill_scratch, spill_bytes, mid_col,
-                           mid_val, num_sms, s, fk);
+    launch_numeric_t<float>(upper, A, B, P, crpt, ccol, cval, spill_scratch, spill_bytes, mid_col,
+                          mid_val, num_sms, s, fk);
 }
 
 void launch_mid_scratch_f32(const CsrDev &A, const CsrDev &B, const PlanDev &P, int *mid_col,
                             void *mid_val, int num_sms, cudaStream_t s, int which)
 {
-    if (A.M <= 0)
-        return;
-    if (which & kMidGroups) {
-        const size_t msm = MidNumLayout<float>::bytes;
-        cudaFuncSetAttribute(k_mid_numeric<float, false, true>,
-                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)msm);
-        k_mid_numeric<float, false, true><<<num_sms * 2, kMidThreads, msm, s>>>(
-            A, B, P, nullptr, mid_col, (float *)mid_val);
-        count_launch();
-    }
-    launch_mid_warp<float, kMwScratch>(A, B, P, nullptr, mid_col, (float *)mid_val, num_sms, s, which);
+    launch_mid_scratch_t<float>(A, B, P, mid_col, mid_val, num_sms, s, which);
 }
 
 }  // namespace brm

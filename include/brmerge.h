@@ -54,8 +54,15 @@ typedef enum brm_dtype { BRM_F64 = 0, BRM_F32 = 1 } brm_dtype;
 
 /* Phase times in seconds; the fields mirror Precise_Timing
  * (BRMerge-SpGEMM/inc/Timings.h:26-46).  GPU phases are timed with CUDA
- * events: compute_flop = row analysis and binning, load_balance = 0 (binning
- * replaces it), symbolic, prefix_sum_nnz = crpt scan, compute = numeric. */
+ * events on the call's stream: compute_flop = row analysis and binning,
+ * prefix_sum_flop = prefix sums of the mid-row products, load_balance = host
+ * read of the bin counts and sizing of the segment buffers, symbolic = exact
+ * row nnz (heavy rows cut into balanced segments), prefix_sum_nnz = crpt
+ * scan, compute = numeric phase.  Device forms: pre_allocate and allocate_C
+ * are host wall times of the output allocations.  Host drop-ins:
+ * pre_allocate = host-to-device copies of A and B, allocate_C = result
+ * blocks, cleanup = the part of the copy of C back to the host that is not
+ * overlapped with the numeric phase.  The phases never sum above total. */
 typedef struct brm_precise_timing {
     double pre_allocate;
     double compute_flop;
@@ -69,7 +76,12 @@ typedef struct brm_precise_timing {
     double total;
 } brm_precise_timing;
 
-/* Mirrors Upper_Timing (BRMerge-SpGEMM/inc/Timings.h:4-24). */
+/* Mirrors Upper_Timing (BRMerge-SpGEMM/inc/Timings.h:4-24): compute_flop =
+ * row analysis, prefix_sum_flop = the row-product scans, load_balance =
+ * buffer sizing and heavy-row segment planning, compute = merge into the
+ * upper-bound buffer, prefix_sum_nnz = crpt scan, copy = compaction into C;
+ * host drop-ins add pre_allocate = copies of A and B and cleanup = copy of
+ * C back to the host.  thread is 0 (one GPU, no thread team). */
 typedef struct brm_upper_timing {
     double thread;
     double pre_allocate;
@@ -131,6 +143,10 @@ int brm_get_tuning(brm_context ctx, brm_tuning *t);
  * counterpart in the reference. */
 int brm_autotune(brm_context ctx, brm_dtype dtype, int n, const brm_csr *A, const brm_csr *B,
                  brm_tuning *best);
+/* SM version of this library's device code as loaded on the current device
+ * (cudaFuncAttributes.binaryVersion: 103 for the sm_103a build).
+ * Diagnostics; no counterpart in the reference. */
+int brm_device_code_version(int *sm);
 /* Device-side error bits of the last call on this context (diagnostics). */
 int brm_last_device_error(brm_context ctx);
 const char *brm_status_string(int status);
@@ -373,8 +389,15 @@ int brm_upper_bound(brm_context ctx, brm_dtype dtype, const brm_csr *A, const br
  * 512 KB array in device memory shared by all calls: A->M may be at most
  * 4,194,304 rows (BRM_ERR_CAPACITY beyond), and calls that overlap on the GPU
  * race on the scratch.  The first call on each device looks up the scratch's
- * device address, so make it before any stream capture.  The call
- * synchronises `stream` (cudaStream_t as void*; NULL = legacy default). */
+ * device address, so make it before any stream capture; the address is kept
+ * for the life of the process, so do not call this after a cudaDeviceReset
+ * of that device.  The call synchronises `stream` (cudaStream_t as void*;
+ * NULL = legacy default).  Status: BRM_ERR_INVALID_CSR when A.rpt, a column
+ * of A or B.rpt is not valid CSR (a column out of range, a decreasing row
+ * pointer); BRM_ERR_OVERFLOW when a row's count exceeds INT_MAX, which valid
+ * CSR cannot produce (a row's count is at most nnz(B)) and which therefore
+ * means an A row with repeated columns; row_flop is then left unwritten for
+ * that row and *products is 0. */
 int brm_compute_flop_noalloc(const brm_csr *A, const brm_csr *B, int *row_flop,
                              long long *products, void *stream);
 

@@ -15,7 +15,6 @@ package brmerge_gb300 never imports it.
 from __future__ import annotations
 
 import ctypes as C
-import os
 import subprocess
 from pathlib import Path
 
@@ -35,11 +34,11 @@ def build(with_ref: bool = True) -> None:
     if r.returncode != 0:
         raise RuntimeError("oracle build failed:\n" + r.stdout + r.stderr)
     if with_ref and not _REF.exists():
-        refdir = Path(os.environ.get("BRM_REFERENCE_DIR", "/root/reference"))
-        if (refdir / "BRMerge-SpGEMM" / "inc" / "spgemm.h").exists():
-            r = subprocess.run(["bash", str(HERE / "build_ref.sh")], capture_output=True, text=True)
-            if r.returncode != 0:
-                raise RuntimeError("reference build failed:\n" + r.stdout + r.stderr)
+        # build_ref.sh finds the reference tree (BRM_REFERENCE_DIR) and exits
+        # 3 when its sources are absent, as on hosts that only run the tests
+        r = subprocess.run(["bash", str(HERE / "build_ref.sh")], capture_output=True, text=True)
+        if r.returncode not in (0, 3):
+            raise RuntimeError("reference build failed:\n" + r.stdout + r.stderr)
 
 
 def _sig(f, args):

@@ -126,6 +126,47 @@ def test_host_drop_in_matches_device(ctx):
     assert_same_csr(C1, gpu_precise(ctx, A, A), "host vs device")
 
 
+PRECISE_PHASES = ("pre_allocate", "compute_flop", "prefix_sum_flop", "load_balance", "symbolic",
+                  "prefix_sum_nnz", "allocate_C", "compute", "cleanup")
+UPPER_PHASES = ("pre_allocate", "compute_flop", "prefix_sum_flop", "load_balance",
+                "allocate_hook", "compute", "prefix_sum_nnz", "allocate_C", "copy", "cleanup")
+
+
+def _check_phases(t, names, must_be_positive):
+    vals = {n: getattr(t, n) for n in names}
+    assert all(v >= 0 for v in vals.values()), vals
+    for n in must_be_positive:
+        assert vals[n] > 0, (n, vals)
+    # the phases are disjoint intervals of one call (1 us of slack for the
+    # rounding of event and wall-clock times)
+    assert sum(vals.values()) <= t.total + 1e-6, (sum(vals.values()), t.total, vals)
+
+
+def test_timing_fields(ctx):
+    """Every form fills the reference's phase fields (Timings.h:4-46) from
+    CUDA events, and the phases sum to at most the call's total time
+    (spgemm.h:476-503 times compute_flop, prefix_sum_flop, load_balance and
+    the rest as consecutive phases)."""
+    A = brm.gen_rmat(14, int(2.35 * (1 << 14)), seed=17)
+    gpu_phases = ("compute_flop", "prefix_sum_flop", "symbolic", "prefix_sum_nnz", "compute")
+    for _ in range(2):  # the second call runs with grown workspaces
+        t = brm.PreciseTiming()
+        brm.brmerge_precise(A, A, timing=t)
+        _check_phases(t, PRECISE_PHASES, gpu_phases + ("pre_allocate", "load_balance"))
+        u = brm.UpperTiming()
+        brm.brmerge_upper(A, A, timing=u)
+        _check_phases(u, UPPER_PHASES, ("pre_allocate", "compute_flop", "prefix_sum_flop",
+                                        "load_balance", "compute", "prefix_sum_nnz", "copy"))
+        dA = brm.DeviceCSR.from_host(A)
+        t = brm.PreciseTiming()
+        ctx.precise_device(dA, dA, timing=t)
+        _check_phases(t, PRECISE_PHASES, gpu_phases + ("load_balance",))
+        u = brm.UpperTiming()
+        ctx.upper(dA, dA, timing=u)
+        _check_phases(u, UPPER_PHASES, ("compute_flop", "prefix_sum_flop", "load_balance",
+                                        "compute", "prefix_sum_nnz", "copy"))
+
+
 def test_host_results_are_independent_blocks(oracle_mod):
     """Results held at the same time never share a cached host block, and a
     released block is reused only after its result is gone."""

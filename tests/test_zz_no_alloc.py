@@ -18,6 +18,8 @@ from brmerge_gb300 import _native
 
 pytestmark = pytest.mark.gpu
 
+BRM_ERR_INVALID_CSR = 2
+BRM_ERR_OVERFLOW = 5
 BRM_ERR_CAPACITY = 10
 MAX_ROWS = 65536 * 64
 
@@ -74,3 +76,54 @@ def test_noalloc_rejects_too_many_rows():
     B = brm.DeviceCSR(4, 4, torch.zeros(5, dtype=torch.int32, device="cuda"), col[:0], val[:0])
     st, _ = _noalloc(lib, A, B, None)
     assert st == BRM_ERR_CAPACITY
+
+
+def _dev_csr(M, N, rpt, col, dtype=np.float64):
+    """A device CSR from raw arrays (no validation: the cases below are
+    deliberately not valid CSR).  The value array is never read by the count."""
+    import torch
+    rpt_t = torch.tensor(np.asarray(rpt, dtype=np.int32), device="cuda")
+    col_t = torch.tensor(np.asarray(col if len(col) else [0], dtype=np.int32), device="cuda")
+    val_t = torch.zeros(max(1, len(col)), dtype=torch.float64, device="cuda")
+    return brm.DeviceCSR(M, N, rpt_t, col_t[:len(col)], val_t[:len(col)])
+
+
+def test_noalloc_reports_invalid_input_and_clears_the_error_word():
+    """A column of A out of range, then B.rpt decreasing: each call returns
+    BRM_ERR_INVALID_CSR (the kernel checks every column before it reads
+    B.rpt, so nothing is read out of bounds).  A valid call right after each
+    failure succeeds, so the shared error word is cleared per call."""
+    lib = _native.lib()
+    good_A = _dev_csr(2, 3, [0, 2, 3], [0, 2, 1])
+    good_B = _dev_csr(3, 4, [0, 1, 3, 4], [0, 1, 3, 2])
+    # out-of-range column (3 >= K = 3) in row 1
+    bad_A = _dev_csr(2, 3, [0, 2, 3], [0, 2, 3])
+    st, total = _noalloc(lib, bad_A, good_B, None)
+    assert st == BRM_ERR_INVALID_CSR and total == 0
+    st, total = _noalloc(lib, good_A, good_B, None)
+    assert st == 0 and total == (1 + 1) + 2
+    # B.rpt decreasing at row 1: a negative row length
+    bad_B = _dev_csr(3, 4, [0, 3, 2, 4], [0, 1, 3, 2])
+    st, total = _noalloc(lib, good_A, bad_B, None)
+    assert st == BRM_ERR_INVALID_CSR and total == 0
+    st, total = _noalloc(lib, good_A, good_B, None)
+    assert st == 0 and total == 4
+
+
+def test_noalloc_reports_row_count_overflow():
+    """With valid CSR a row's count is at most nnz(B) <= INT_MAX.  An A row
+    that repeats a column can exceed it: the call returns BRM_ERR_OVERFLOW
+    instead of clamping the row's count.  Only B.rpt is read (never B.col),
+    so B's row pointers can describe long rows without holding them."""
+    import torch
+    lib = _native.lib()
+    A = _dev_csr(1, 1, [0, 3], [0, 0, 0])
+    B = _dev_csr(1, 1, [0, 1 << 30], [0])
+    row_flop = torch.full((1,), -7, dtype=torch.int32, device="cuda")
+    st, total = _noalloc(lib, A, B, row_flop.data_ptr())
+    assert st == BRM_ERR_OVERFLOW and total == 0
+    assert int(row_flop.item()) == -7  # left unwritten, not clamped
+    good_A = _dev_csr(2, 3, [0, 2, 3], [0, 2, 1])
+    good_B = _dev_csr(3, 4, [0, 1, 3, 4], [0, 1, 3, 2])
+    st, total = _noalloc(lib, good_A, good_B, None)
+    assert st == 0 and total == 4
