@@ -2,10 +2,12 @@
 """Benchmark: BRMerge SpGEMM GFLOP/s and HBM-roofline fraction on one GB300.
 
 Workload (default): C = A*A, A = R-MAT(a,b,c,d = .57,.19,.19,.05) with n = 2^18
-and 2.35*n samples (duplicates removed: ~607k nnz, ~9.0e7 intermediate
+and 2.35*n samples (duplicates removed: ~607k nnz, ~9e7 intermediate
 products), float64, BRMerge-Precise, plain per-call GPU path.  A "step" is
 one SpGEMM call.  GFLOP/s = 2 * intermediate products / time, the
-reference's definition (BRMerge-SpGEMM/src/brmerge_precise.cpp:65-69).
+reference's definition (BRMerge-SpGEMM/src/brmerge_precise.cpp:65-69).  The
+matrices are generated here with numpy, so both arms multiply the same
+inputs and the reference arm loads nothing of this library.
 
 * value   -- device-resident inputs: one brm_precise_device call (C ABI)
              timed with CUDA events on the call's stream, L2 flushed between
@@ -17,6 +19,17 @@ reference's definition (BRMerge-SpGEMM/src/brmerge_precise.cpp:65-69).
              copy bandwidth in MEASURED_PEAKS.json.
 * cpu_baseline -- the oracle restatement of BRMerge-Precise (OpenMP, all
              host cores) on the same input.
+* side sections (--sections): ER n=16384 (the reference's CPU case) and the
+             27-point stencil, each with its CPU baseline; the MatrixMarket
+             reader; the 4096-pair uneven batch in float64 and float32 with
+             its graph replay; the served request stream.
+* checks  -- every timed result is compared with the oracle or with a
+             result that is: the headline step bit for bit against the
+             oracle, e2e / Upper against it, the hash comparator within the
+             reference's 1e-9 compare, the stencil on three row blocks against
+             the oracle, every pair of the batches against its plain call and
+             sixteen against the oracle, every served result against its
+             isolated call.  "verified" is true when all of them hold.
 
 --impl reference times the reference algorithm on the host cores instead
 (oracle/_ref when it was built here, else the oracle restatement).
@@ -32,6 +45,7 @@ import sys
 import threading
 import time
 from pathlib import Path
+from types import SimpleNamespace
 
 import numpy as np
 
@@ -46,33 +60,151 @@ def csr_bytes(M: int, nnz: int, vbytes: int) -> int:
     return 4 * (M + 1) + nnz * (4 + vbytes)
 
 
+# ---------------------------------------------------------------------------
+# Workloads, generated here with numpy (seeded PCG64) so that both arms --
+# this library and the reference algorithm on the host cores -- multiply the
+# same matrices and the reference arm loads nothing of the library.
+# ---------------------------------------------------------------------------
+def host_csr(M, N, rpt, col, val):
+    return SimpleNamespace(M=int(M), N=int(N), rpt=np.ascontiguousarray(rpt, np.int32),
+                           col=np.ascontiguousarray(col, np.int32),
+                           val=np.ascontiguousarray(val), nnz=int(len(col)))
+
+
+def gen_rmat_np(scale: int, edges: int, a: float, b: float, c: float, seed: int):
+    """R-MAT(a, b, c, d = 1-a-b-c) on 2^scale x 2^scale: `edges` samples, one
+    quadrant draw per bit, duplicates removed, values U[-1, 1)."""
+    rng = np.random.default_rng(seed)
+    n = 1 << scale
+    r = np.zeros(edges, np.int64)
+    cc = np.zeros(edges, np.int64)
+    ab, abc = a + b, a + b + c
+    for bit in range(scale - 1, -1, -1):
+        u = rng.random(edges)
+        r |= (u >= ab).astype(np.int64) << bit
+        cc |= (((u >= a) & (u < ab)) | (u >= abc)).astype(np.int64) << bit
+    keys = np.unique((r << 32) | cc)
+    rows = keys >> 32
+    rpt = np.zeros(n + 1, np.int64)
+    np.cumsum(np.bincount(rows, minlength=n), out=rpt[1:])
+    return host_csr(n, n, rpt, keys & 0xFFFFFFFF, rng.uniform(-1.0, 1.0, len(keys)))
+
+
+def gen_er_np(n: int, per_row: int, seed: int):
+    """Erdos-Renyi: exactly per_row distinct uniform columns per row (sorted),
+    values U[-1, 1)."""
+    rng = np.random.default_rng(seed)
+    cols = np.empty((n, per_row), np.int64)
+    for i in range(n):
+        cols[i] = np.sort(rng.choice(n, per_row, replace=False))
+    rpt = np.arange(n + 1, dtype=np.int64) * per_row
+    return host_csr(n, n, rpt, cols.ravel(), rng.uniform(-1.0, 1.0, n * per_row))
+
+
+def gen_stencil27_np(m: int, seed: int, jitter: float = 1e-3):
+    """27-point stencil on an m^3 grid: 26 on the diagonal, -1 off it, each
+    entry plus U[-jitter, jitter); columns sorted within each row."""
+    rng = np.random.default_rng(seed)
+    n = m ** 3
+    idx = np.arange(n, dtype=np.int64)
+    x, y, z = idx % m, (idx // m) % m, idx // (m * m)
+    cols = np.empty((n, 27), np.int32)
+    ok = np.empty((n, 27), bool)
+    j = 0
+    for dz in (-1, 0, 1):
+        for dy in (-1, 0, 1):
+            for dx in (-1, 0, 1):
+                ok[:, j] = ((x + dx >= 0) & (x + dx < m) & (y + dy >= 0) & (y + dy < m)
+                            & (z + dz >= 0) & (z + dz < m))
+                cols[:, j] = idx + (dz * m + dy) * m + dx
+                j += 1
+    rpt = np.zeros(n + 1, np.int64)
+    np.cumsum(ok.sum(axis=1), out=rpt[1:])
+    col = cols[ok]
+    rows = np.repeat(idx, np.diff(rpt))
+    val = np.where(col == rows, 26.0, -1.0) + rng.uniform(-jitter, jitter, len(col))
+    return host_csr(n, n, rpt, col, val)
+
+
 def make_workload(name: str, stencil_n: int = 128):
-    import brmerge_gb300 as brm
     if name == "rmat":
         n = 1 << RMAT_SCALE
-        A = brm.gen_rmat(RMAT_SCALE, int(RMAT_EDGE_FACTOR * n), seed=0)
+        A = gen_rmat_np(RMAT_SCALE, int(RMAT_EDGE_FACTOR * n), 0.57, 0.19, 0.19, seed=0)
         desc = {"workload": "rmat_n2^18_ef2.35_AxA", "n": n, "a": 0.57, "b": 0.19, "c": 0.19,
-                "seed": 0}
+                "seed": 0, "generator": "numpy PCG64"}
     elif name == "er":
-        A = brm.gen_er(16384, 8, seed=0)
-        desc = {"workload": "er_n16384_8perrow_AxA", "n": 16384, "seed": 0}
+        A = gen_er_np(16384, 8, seed=0)
+        desc = {"workload": "er_n16384_8perrow_AxA", "n": 16384, "seed": 0,
+                "generator": "numpy PCG64"}
     elif name == "stencil":
-        A = brm.gen_stencil27(stencil_n)
-        desc = {"workload": f"stencil27_{stencil_n}^3_AxA", "n": stencil_n ** 3}
+        A = gen_stencil27_np(stencil_n, seed=0)
+        desc = {"workload": f"stencil27_{stencil_n}^3_AxA", "n": stencil_n ** 3, "seed": 0,
+                "generator": "numpy PCG64"}
     else:
         raise SystemExit(f"unknown workload {name}")
     return A, desc
 
 
-def measured_traffic():
-    """DRAM bytes of one Precise call on the R-MAT workload, from the committed
-    ncu launch-list summary (a capture of this bench's own command)."""
-    p = ROOT / "profiles" / "rmat18_precise_launches.md"
+def products_of(A, B) -> int:
+    """Intermediate products of A*B (2x this is the reference's flop count)."""
+    return int(np.diff(B.rpt.astype(np.int64))[A.col].sum()) if A.nnz else 0
+
+
+def row_block(A, r0: int, r1: int):
+    """Rows [r0, r1) of A as a CSR of their own (the same per-row work)."""
+    a0, a1 = int(A.rpt[r0]), int(A.rpt[r1])
+    return host_csr(r1 - r0, A.N, A.rpt[r0:r1 + 1].astype(np.int64) - a0, A.col[a0:a1],
+                    A.val[a0:a1])
+
+
+# ---------------------------------------------------------------------------
+# Result checks: structure bit-exact, values bit-exact unless a tolerance is
+# given (the hash comparator sums in hardware order).
+# ---------------------------------------------------------------------------
+def same_csr(X, R, tol: float | None = None) -> bool:
+    if not (np.array_equal(np.asarray(X.rpt), np.asarray(R.rpt))
+            and np.array_equal(np.asarray(X.col), np.asarray(R.col))):
+        return False
+    xv, rv = np.asarray(X.val), np.asarray(R.val)
+    if tol is None:
+        return xv.dtype == rv.dtype and np.array_equal(xv.view(np.uint8), rv.view(np.uint8))
+    d = np.abs(xv.astype(np.float64) - rv.astype(np.float64))
+    return bool(np.all((d <= tol) | (d <= tol * np.abs(rv.astype(np.float64)))))
+
+
+def rows_of(C, r0: int, r1: int):
+    """Rows [r0, r1) of a host CSR result, row pointers from 0."""
+    e0, e1 = int(C.rpt[r0]), int(C.rpt[r1])
+    return SimpleNamespace(rpt=np.asarray(C.rpt[r0:r1 + 1], np.int64) - e0,
+                           col=C.col[e0:e1], val=C.val[e0:e1])
+
+
+def dev_equal(x, y) -> bool:
+    """Bit equality of two device tensors (values compared as raw bits)."""
+    import torch
+    if x.shape != y.shape or x.dtype != y.dtype:
+        return False
+    if x.dtype == torch.float64:
+        x, y = x.view(torch.int64), y.view(torch.int64)
+    elif x.dtype == torch.float32:
+        x, y = x.view(torch.int32), y.view(torch.int32)
+    return bool(torch.equal(x, y))
+
+
+def dev_same_csr(X, Y) -> bool:
+    return dev_equal(X.rpt, Y.rpt) and dev_equal(X.col, Y.col) and dev_equal(X.val, Y.val)
+
+
+def traffic_record():
+    """DRAM bytes of one Precise call on the R-MAT workload as recorded by an
+    ncu capture of this bench (profiles/rmat18_precise_traffic.json); it is
+    a recorded profile value, not a measurement of this run."""
+    p = ROOT / "profiles" / "rmat18_precise_traffic.json"
     if p.exists():
-        for line in p.read_text().splitlines():
-            if line.startswith("traffic_bytes_per_step:"):
-                return int(line.split(":")[1])
-    return None
+        d = json.loads(p.read_text())
+        return int(d["dram_bytes_per_call"]), {k: d[k] for k in ("captured", "commit", "command")
+                                               if k in d}
+    return None, None
 
 
 def peaks():
@@ -173,24 +305,29 @@ def barrier(ws):
         dist.barrier()
 
 
-def cpu_baseline(A, budget_s: float = 20.0):
-    """The oracle restatement on all host cores: 1 warm-up + timed calls,
-    bounded by budget_s (BRMerge-SpGEMM/src/brmerge_precise.cpp:68-82)."""
+def oracle_precise_timed(A, B, budget_s: float):
+    """The oracle restatement of BRMerge-Precise on all host cores, timed the
+    way the reference's driver times it (BRMerge-SpGEMM/src/
+    brmerge_precise.cpp:68-82): one warm-up call, then the mean of up to ten
+    calls within budget_s.  Returns (seconds per call, calls timed, threads,
+    the warm-up call's result)."""
     import oracle
     oracle.build(with_ref=False)
     nt = oracle.max_threads()
-    flop = oracle.compute_flop(A, A)
     t0 = time.perf_counter()
-    oracle.precise(A, A, nt)
+    R = oracle.precise(A, B, nt)
     one = time.perf_counter() - t0
     reps = max(1, min(10, int(budget_s / max(one, 1e-3))))
     t0 = time.perf_counter()
     for _ in range(reps):
-        oracle.precise(A, A, nt)
-    dt = (time.perf_counter() - t0) / reps
-    return {"value": round(2 * flop / dt / 1e9, 4), "unit": "GFLOP/s", "cores": nt,
+        oracle.precise(A, B, nt)
+    return (time.perf_counter() - t0) / reps, reps, nt, R
+
+
+def cpu_baseline_entry(products: int, sec: float, reps: int, nt: int, sample: str) -> dict:
+    return {"value": round(2 * products / sec / 1e9, 4), "unit": "GFLOP/s", "cores": nt,
             "kind": "port",
-            "sample": f"full workload, 1 warm-up + mean of {reps} calls, {dt * 1e3:.1f} ms/call"}
+            "sample": f"{sample}, 1 warm-up + mean of {reps} calls, {sec * 1e3:.1f} ms/call"}
 
 
 def run_reference(args):
@@ -203,7 +340,7 @@ def run_reference(args):
     A, desc = make_workload(args.workload, args.stencil_n)
     use_ref = oracle.ref_available()
     nt = oracle.max_threads()
-    flop = oracle.compute_flop(A, A)
+    flop = products_of(A, A)
 
     def call():
         if use_ref:
@@ -238,18 +375,25 @@ def run_reference(args):
 BATCH_PAIRS = 4096
 
 
+_BATCH_CACHE = {}
+
+
 def make_batch(npairs: int, seed: int, dtype=np.float64):
     """Uneven batch: C_i = A_i * B_i, n_i ~ U[256, 8192], rows lognormal(ln 6,
-    0.8) capped at 256, uniform random columns, values U[-1, 1]."""
+    0.8) capped at 256, uniform random columns, values U[-1, 1].  The float32
+    variant is the float64 batch with its values rounded to float32."""
     import brmerge_gb300 as brm
-    rng = np.random.default_rng(seed)
-    ns = rng.integers(256, 8193, npairs)
-    pairs = []
-    for i, n in enumerate(ns):
-        A = brm.gen_lognormal(int(n), int(n), seed=seed * 100003 + 2 * i)
-        B = brm.gen_lognormal(int(n), int(n), seed=seed * 100003 + 2 * i + 1)
-        pairs.append((A.astype(dtype), B.astype(dtype)))
-    return pairs
+    key = (npairs, seed)
+    if key not in _BATCH_CACHE:
+        rng = np.random.default_rng(seed)
+        ns = rng.integers(256, 8193, npairs)
+        pairs = []
+        for i, n in enumerate(ns):
+            A = brm.gen_lognormal(int(n), int(n), seed=seed * 100003 + 2 * i)
+            B = brm.gen_lognormal(int(n), int(n), seed=seed * 100003 + 2 * i + 1)
+            pairs.append((A, B))
+        _BATCH_CACHE[key] = pairs
+    return [(A.astype(dtype), B.astype(dtype)) for A, B in _BATCH_CACHE[key]]
 
 
 def upload_pairs(pairs, dev):
@@ -300,26 +444,71 @@ def method_entry(ms: float, products: int, alg_bytes: int, peak: float) -> dict:
             "achieved_gbs": round(ach, 1), "frac": round(ach / peak, 4)}
 
 
-def stencil_section(ctx, dev, stream, flush, steps: int, peak: float):
-    """27-point stencil on 128^3 (C = A*A, a 125-point stencil): Precise and
-    Upper through the one-call device forms."""
+def stencil_section(ctx, dev, stream, flush, steps: int, peak: float, cpu_budget: float,
+                    m: int = 128):
+    """27-point stencil on m^3 (C = A*A, a 125-point stencil): Precise and
+    Upper through the one-call device forms, the hash comparator beside them.
+    Checked on three row blocks (first, middle, last 1/32 of the rows) against
+    the oracle, which is also the CPU baseline on those blocks."""
     import brmerge_gb300 as brm
-    S = brm.gen_stencil27(128)
-    products = brm.compute_flop_host(S, S)
+    S, _ = make_workload("stencil", m)
+    products = products_of(S, S)
     dS = brm.DeviceCSR.from_host(S, dev)
-    res = {"workload": "stencil27_128^3_AxA", "n": S.M, "nnz_A": int(S.nnz),
+    res = {"workload": f"stencil27_{m}^3_AxA", "n": S.M, "nnz_A": int(S.nnz),
            "products": int(products)}
     ms, C = device_steps(lambda: ctx.precise_device(dS, dS), dev, stream, flush, steps)
     res["nnz_C"] = int(C.nnz)
     alg = 2 * csr_bytes(S.M, S.nnz, 8) + csr_bytes(S.M, C.nnz, 8)
+    Cp = C.to_host()
     del C
     res["precise"] = method_entry(ms, products, alg, peak)
     ms, C = device_steps(lambda: ctx.upper(dS, dS), dev, stream, flush, steps)
-    del C
     res["upper"] = method_entry(ms, products, alg, peak)
-    ms, C = device_steps(lambda: ctx.hash_device(dS, dS), dev, stream, flush, steps)
+    res["upper"]["verified_vs_precise"] = same_csr(C.to_host(), Cp)
     del C
+    ms, C = device_steps(lambda: ctx.hash_device(dS, dS), dev, stream, flush, steps)
     res["hash_comparator"] = method_entry(ms, products, alg, peak)
+    res["hash_comparator"]["verified_vs_precise_1e-9"] = same_csr(C.to_host(), Cp, tol=1e-9)
+    del C, dS
+    # oracle on sampled row blocks: the check of the Precise result and the
+    # CPU baseline on the same blocks
+    blk = max(1, S.M // 32)
+    starts = [0, (S.M // 2) // blk * blk, S.M - blk]
+    ok, sec_tot, prod_tot, reps_min, nt = True, 0.0, 0, 10, 1
+    for r0 in starts:
+        Sb = row_block(S, r0, r0 + blk)
+        sec, reps, nt, R = oracle_precise_timed(Sb, S, cpu_budget / len(starts))
+        ok &= same_csr(rows_of(Cp, r0, r0 + blk), R)
+        sec_tot += sec
+        prod_tot += products_of(Sb, S)
+        reps_min = min(reps_min, reps)
+    res["precise"]["verified_vs_oracle"] = bool(ok)
+    res["verified"] = bool(ok and res["upper"]["verified_vs_precise"]
+                           and res["hash_comparator"]["verified_vs_precise_1e-9"])
+    res["cpu_baseline"] = cpu_baseline_entry(
+        prod_tot, sec_tot, reps_min, nt,
+        f"rows [0,{blk}), [{starts[1]},{starts[1] + blk}), [{starts[2]},{S.M}) of C (3/32 of "
+        f"the rows, {prod_tot} products)")
+    return res
+
+
+def er_section(ctx, dev, stream, flush, steps: int, peak: float, cpu_budget: float):
+    """Config 1, the reference's CPU case: Erdos-Renyi n=16384, exactly 8
+    columns per row, C = A*A; one-call Precise on the GPU, the oracle on the
+    host cores as its baseline and its check."""
+    import brmerge_gb300 as brm
+    A, desc = make_workload("er")
+    products = products_of(A, A)
+    dA = brm.DeviceCSR.from_host(A, dev)
+    ms, C = device_steps(lambda: ctx.precise_device(dA, dA), dev, stream, flush, steps)
+    Ch = C.to_host()
+    del C
+    alg = 2 * csr_bytes(A.M, A.nnz, 8) + csr_bytes(A.M, len(Ch.col), 8)
+    sec, reps, nt, R = oracle_precise_timed(A, A, cpu_budget)
+    res = dict(desc, products=int(products), nnz_C=int(len(Ch.col)))
+    res["precise"] = method_entry(ms, products, alg, peak)
+    res["verified"] = same_csr(Ch, R)
+    res["cpu_baseline"] = cpu_baseline_entry(products, sec, reps, nt, "full workload")
     return res
 
 
@@ -366,15 +555,32 @@ def reader_section(ctx, A, steps: int):
     }
 
 
-def batched_section(ctx, dev, stream, steps: int):
+def batch_views(out, pairs):
+    """Per-pair views (rpt from 0, col, val) of a brm_batch_precise result."""
+    crpt, ccol, cval, row_off, nnz_off, rpt_local = out
+    views = []
+    for i in range(len(pairs)):
+        r0, r1 = int(row_off[i]), int(row_off[i + 1])
+        n0, n1 = int(nnz_off[i]), int(nnz_off[i + 1])
+        views.append(SimpleNamespace(rpt=rpt_local[r0 + i:r1 + i + 1], col=ccol[n0:n1],
+                                     val=cval[n0:n1]))
+    return views
+
+
+def batched_section(ctx, dev, stream, steps: int, dtype=np.float64, tune: bool = True,
+                    n_oracle: int = 16):
     """The uneven batch through brm_batch_precise (one pipeline for every
-    pair) against a loop of plain per-pair brm_precise_device calls."""
+    pair) against a loop of plain per-pair brm_precise_device calls.  Every
+    C_i of the batch (and of its graph replay) is checked bit for bit against
+    the plain call on the same pair, and n_oracle pairs against the oracle."""
     import torch
     import brmerge_gb300 as brm
+    import oracle
     L = brm._native.lib()
-    pairs = make_batch(BATCH_PAIRS, seed=7)
-    products = sum(brm.compute_flop_host(A, B) for A, B in pairs)
+    pairs = make_batch(BATCH_PAIRS, seed=7, dtype=dtype)
+    products = sum(products_of(A, B) for A, B in pairs)
     dpairs, keep = upload_pairs(pairs, dev)
+    host_sample = pairs[:n_oracle]
     del pairs
     out = ctx.batch_precise_raw(dpairs)  # warm-up (pools, workspaces)
     nnz = int(out[1].numel())
@@ -384,21 +590,26 @@ def batched_section(ctx, dev, stream, steps: int):
     def timed():
         ts = []
         l0 = L.brm_kernel_launches()
+        out = None
         for _ in range(steps):
+            del out
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record(stream)
             out = ctx.batch_precise_raw(dpairs)
             e1.record(stream)
             torch.cuda.synchronize(dev)
             ts.append(e0.elapsed_time(e1))
-            del out
-        return statistics.mean(ts), (L.brm_kernel_launches() - l0) / steps
+        return statistics.mean(ts), (L.brm_kernel_launches() - l0) / steps, out
 
-    default_ms, _ = timed()
-    t0 = time.perf_counter()
-    tuning = ctx.autotune(dpairs)  # bin thresholds chosen on this batch
-    tune_s = time.perf_counter() - t0
-    b_ms, launches = timed()
+    res = {}
+    default_ms, _, out = timed()
+    del out
+    if tune:
+        t0 = time.perf_counter()
+        res["tuning"] = ctx.autotune(dpairs)  # bin thresholds chosen on this batch
+        res["autotune_s"] = round(time.perf_counter() - t0, 2)
+    b_ms, launches, out = timed()
+    bviews = batch_views(out, dpairs)
     # fixed structure, new values: one CUDA-graph launch per recomputation
     g = ctx.batch_graph(dpairs)
     gts = []
@@ -409,39 +620,55 @@ def batched_section(ctx, dev, stream, steps: int):
         e1.record(stream)
         torch.cuda.synchronize(dev)
         gts.append(e0.elapsed_time(e1))
-    g.close()
     graph_ms = statistics.mean(gts[1:])
+    graph_ok = all(dev_same_csr(x, y) for x, y in zip(g.results, bviews))
+    g.close()
     ctx.set_tuning()  # the plain loop below runs with the defaults
-    # plain per-call loop over the same pairs (one pass, results released)
+    # plain per-call loop over the same pairs (one pass; results kept for the check)
     for a, b in dpairs[:16]:
         ctx.precise_device(a, b)
     torch.cuda.synchronize(dev)
+    plain = []
     t0 = time.perf_counter()
     for a, b in dpairs:
-        C = ctx.precise_device(a, b)
-        del C
+        plain.append(ctx.precise_device(a, b))
     torch.cuda.synchronize(dev)
     plain_s = time.perf_counter() - t0
-    return {
-        "tuning": tuning, "default_tuning_ms": round(default_ms, 3),
-        "autotune_s": round(tune_s, 2),
+    batch_ok = all(dev_same_csr(x, y) for x, y in zip(bviews, plain))
+    oracle.build(with_ref=False)
+    nt = oracle.max_threads()
+    oracle_ok = all(same_csr(SimpleNamespace(rpt=v.rpt.cpu().numpy(), col=v.col.cpu().numpy(),
+                                             val=v.val.cpu().numpy()), oracle.precise(A, B, nt))
+                    for v, (A, B) in zip(bviews, host_sample))
+    del plain, bviews, out
+    vt = "f64" if dtype == np.float64 else "f32"
+    res.update({
+        "default_tuning_ms": round(default_ms, 3),
         "graph_replay_ms": round(graph_ms, 3),
         "graph_replay_gflops": round(2 * products / (graph_ms / 1e3) / 1e9, 3),
-        "workload": f"{BATCH_PAIRS} pairs, n_i~U[256,8192], rows lognormal(ln6,0.8) cap 256, f64",
+        "workload": f"{BATCH_PAIRS} pairs, n_i~U[256,8192], rows lognormal(ln6,0.8) cap 256, "
+                    f"{vt}",
         "pairs": BATCH_PAIRS, "products": int(products), "nnz_C": nnz,
         "ms": round(b_ms, 3), "gflops": round(2 * products / (b_ms / 1e3) / 1e9, 3),
         "plain_loop_ms": round(plain_s * 1e3, 2),
         "plain_gflops": round(2 * products / plain_s / 1e9, 3),
         "speedup_vs_plain": round(plain_s * 1e3 / b_ms, 2),
         "launches_per_batch": launches, "steps": steps,
-    }
+        "verified": bool(batch_ok and graph_ok and oracle_ok),
+        "checks": {"every_pair_vs_plain_call": bool(batch_ok),
+                   "graph_replay_vs_batch": bool(graph_ok),
+                   f"first_{n_oracle}_pairs_vs_oracle": bool(oracle_ok)},
+    })
+    return res
 
 
 def served_section(dev, rate: float, nreq: int, seed: int = 11):
     """Poisson request stream into brm_server (continuous batching under a
     60 GiB cap): 70% uneven-batch sizes, 25% R-MAT n=2^16 degree 8, 5% R-MAT
     n=2^20 degree 16; float64 and float32 mixed.  Latency = submit -> result
-    ready; the isolated latency of each class is one call on an idle GPU."""
+    ready; the isolated latency of each class is one call on an idle GPU.
+    Every served result is checked bit for bit against the same pair's
+    isolated brm_precise_device result."""
     import queue as q
     import torch
     import brmerge_gb300 as brm
@@ -462,6 +689,18 @@ def served_section(dev, rate: float, nreq: int, seed: int = 11):
     flops = {}
     ctx = brm.Context()
     iso = {}
+    alone = {}  # (class, f32, index) -> the isolated result
+    for name, pools in classes.items():
+        _, bound = ctx.upper_bound(*pools[0][0])
+        if bound > (60 << 30):
+            continue
+        for f32, pool in enumerate(pools):
+            for j, (a, b) in enumerate(pool):
+                try:
+                    alone[(name, f32, j)] = ctx.precise_device(a, b)
+                except brm.BrmError:
+                    pass
+    torch.cuda.synchronize(dev)
     for name, (p64, _) in classes.items():
         a, b = p64[0]
         flops[name] = 2 * ctx.compute_flop(a, b)
@@ -501,9 +740,10 @@ def served_section(dev, rate: float, nreq: int, seed: int = 11):
                 time.sleep(arrivals[i] - now)
             name = names[kinds[i]]
             pool = classes[name][1 if f32[i] else 0]
-            a, b = pool[int(rng.integers(len(pool)))]
+            j = int(rng.integers(len(pool)))
+            a, b = pool[j]
             try:
-                tickets.put((i, name, srv.submit(a, b)))
+                tickets.put((i, name, (name, int(f32[i]), j), srv.submit(a, b)))
             except brm.BrmError:
                 rejected[name] += 1
         tickets.put(None)
@@ -511,14 +751,18 @@ def served_section(dev, rate: float, nreq: int, seed: int = 11):
     lat = {n: [] for n in names}
     batch_sizes = []
     done_flop = 0
+    mismatches = 0
     th = threading.Thread(target=submitter)
     th.start()
     while True:
         item = tickets.get()
         if item is None:
             break
-        i, name, t = item
+        i, name, key, t = item
         C, st = srv.wait(t, timeout=600.0)
+        ref = alone.get(key)
+        if ref is None or not dev_same_csr(C, ref):
+            mismatches += 1
         lat[name].append(st["latency_s"] * 1e3)
         batch_sizes.append(st["batch_size"])
         done_flop += flops[name]
@@ -537,6 +781,8 @@ def served_section(dev, rate: float, nreq: int, seed: int = 11):
         "p50_ms": pct(allv, 50), "p99_ms": pct(allv, 99),
         "mean_batch": round(float(np.mean(batch_sizes)), 2) if batch_sizes else None,
         "classes": per_class, "mem_cap_gib": 60, "workers": 2,
+        "verified": mismatches == 0,
+        "checks": {"served_results_vs_isolated_call_mismatches": mismatches},
     }
 
 
@@ -550,8 +796,13 @@ def run_ours(args):
         dist.init_process_group("nccl")
     dev = torch.device("cuda", local if ws > 1 else 0)
     torch.cuda.set_device(dev)
+    sections = set(args.sections.split(",")) if args.sections else set(ALL_SECTIONS)
+    if args.no_batch:
+        sections -= {"reader", "stencil", "er", "batch", "batch32", "served"}
+    if args.no_cpu:
+        sections.discard("cpu")
     A, desc = make_workload(args.workload, args.stencil_n)
-    products = brm.compute_flop_host(A, A)
+    products = products_of(A, A)
     stream = torch.cuda.current_stream(dev)
     ctx = brm.Context(stream=stream)
     dA = brm.DeviceCSR.from_host(A, dev)
@@ -587,9 +838,11 @@ def run_ours(args):
     step_ms = [e[0].elapsed_time(e[2]) for e in ev]
     total_s = max_over_ranks(sum(step_ms) / 1e3, ws)
     value = 2 * products * args.steps * ws / total_s / 1e9
-    sym_ms = statistics.mean((e[1].compute_flop + e[1].symbolic + e[1].prefix_sum_nnz) * 1e3
-                             for e in ev)
-    num_ms = statistics.mean(e[1].compute * 1e3 for e in ev)
+    phase_ms = {k: round(statistics.mean(getattr(e[1], k) for e in ev) * 1e3, 4)
+                for k in ("compute_flop", "prefix_sum_flop", "load_balance", "symbolic",
+                          "prefix_sum_nnz", "compute")}
+    Cref = C.to_host()  # the last timed step's result, checked below
+    del C
 
     # roofline of the whole call (every kernel of the step, one stream):
     # compulsory bytes = read A and B once, write C once
@@ -605,11 +858,14 @@ def run_ours(args):
         brm.brmerge_precise(hA, hA)
     e2e_t = []
     d2h = 0
-    for _ in range(args.steps):
+    e2e_ok = True
+    for i in range(args.steps):
         t0 = time.perf_counter()
         Ch = brm.brmerge_precise(hA, hA)
         e2e_t.append(time.perf_counter() - t0)
         d2h = csr_bytes(A.M, len(Ch.col), vb)
+        if i + 1 == args.steps:
+            e2e_ok = same_csr(Ch, Cref)
         # the reference's driver releases C between calls, outside its timing
         # (BRMerge-SpGEMM/src/brmerge_precise.cpp:73-79)
         del Ch
@@ -618,24 +874,48 @@ def run_ours(args):
     h2d = csr_bytes(A.M, A.nnz, vb)  # A and B are the same host arrays: copied once
 
     # BRMerge-Upper on the same workload (one call: C_bar, nnz scan, compaction)
-    del C
     up_ms, Cu = device_steps(lambda: ctx.upper(dA, dA), dev, stream, flush, args.steps)
-    del Cu
     upper = method_entry(up_ms, products, alg_bytes, peak)
+    upper["verified_vs_precise"] = same_csr(Cu.to_host(), Cref)
+    del Cu
     # the hash SpGEMM comparator: same structure, values in hardware order
-    h_ms, Ch = device_steps(lambda: ctx.hash_device(dA, dA), dev, stream, flush, args.steps)
-    del Ch
+    h_ms, Chs = device_steps(lambda: ctx.hash_device(dA, dA), dev, stream, flush, args.steps)
     hashc = method_entry(h_ms, products, alg_bytes, peak)
+    hashc["verified_vs_precise_1e-9"] = same_csr(Chs.to_host(), Cref, tol=1e-9)
+    del Chs
 
-    batched = served = stencil = reader = None
-    if not args.no_batch:
-        reader = reader_section(ctx, A, max(1, min(args.steps, 3)))
-        stencil = stencil_section(ctx, dev, stream, flush, max(1, min(args.steps, 5)), peak)
-        batched = batched_section(ctx, dev, stream, steps=max(1, min(args.steps, 3)))
-        served = [served_section(dev, rate, args.serve_requests) for rate in (2000.0, 400.0, 150.0)]
+    side = {}
+    if "reader" in sections:
+        side["mtx_reader"] = reader_section(ctx, A, max(1, min(args.steps, 3)))
+    if "er" in sections:
+        side["er"] = er_section(ctx, dev, stream, flush, max(1, min(args.steps, 5)), peak,
+                                args.cpu_budget)
+    if "stencil" in sections:
+        side["stencil"] = stencil_section(ctx, dev, stream, flush, max(1, min(args.steps, 5)),
+                                          peak, args.cpu_budget, args.stencil_n)
+    if "batch" in sections:
+        side["batched"] = batched_section(ctx, dev, stream, steps=max(1, min(args.steps, 3)))
+    if "batch32" in sections:
+        side["batched_f32"] = batched_section(ctx, dev, stream, steps=max(1, min(args.steps, 3)),
+                                              dtype=np.float32, tune=False)
+    if "served" in sections:
+        side["served"] = [served_section(dev, rate, args.serve_requests)
+                          for rate in (2000.0, 400.0, 150.0)]
     if rank != 0:
         return
-    cpu = cpu_baseline(A, budget_s=args.cpu_budget) if not args.no_cpu else None
+    # the oracle on the host cores: the check of the headline result and,
+    # timed, the CPU baseline
+    cpu = None
+    import oracle
+    if "cpu" in sections:
+        sec, reps, nt, R = oracle_precise_timed(A, A, args.cpu_budget)
+        cpu = cpu_baseline_entry(products, sec, reps, nt, "full workload")
+    else:
+        oracle.build(with_ref=False)
+        R = oracle.precise(A, A, oracle.max_threads())
+    precise_ok = same_csr(Cref, R)
+    del R
+    traffic, traffic_src = traffic_record() if args.workload == "rmat" else (None, None)
     line = {
         "metric": "SpGEMM GFLOP/s (BRMerge-Precise, C=A*A)",
         "value": round(value, 3), "unit": "GFLOP/s", "n_gpus": ws, "steps": args.steps,
@@ -648,12 +928,11 @@ def run_ours(args):
                        method="precise", call="brm_precise_device (one call)",
                        l2="flushed (512 MB write) between steps",
                        parallelism="replicas" if ws > 1 else "single_gpu",
-                       symbolic_ms=round(sym_ms, 4), numeric_ms=round(num_ms, 4)),
+                       phase_ms=phase_ms),
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak,
                      "unit": "GB/s", "frac": round(achieved / peak, 4),
-                     "traffic": measured_traffic() if args.workload == "rmat" else None,
-                     "traffic_source": "profiles/rmat18_precise_launches.md (ncu DRAM bytes "
-                                       "of every kernel of one call)",
+                     "traffic": traffic,
+                     "traffic_recorded": traffic_src,
                      "kernel": "whole Precise call (all kernels of a step)",
                      "peak_kind": peak_kind, "algorithmic_bytes": int(alg_bytes)},
         "e2e": {"value": round(e2e_val, 3), "unit": "GFLOP/s", "h2d_bytes_per_step": int(h2d),
@@ -665,18 +944,24 @@ def run_ours(args):
     line["hash_comparator"] = dict(hashc, call="brm_hash_device (values not in merge order)")
     if cpu is not None:
         line["cpu_baseline"] = cpu
-    if stencil is not None:
-        line["stencil"] = stencil
-    if reader is not None:
-        line["mtx_reader"] = reader
-    if batched is not None:
-        line["batched"] = batched
-    if served is not None:
-        line["served"] = served
+    line.update(side)
+    checks = {"precise_vs_oracle": precise_ok, "e2e_vs_precise": e2e_ok,
+              "upper_vs_precise": upper["verified_vs_precise"],
+              "hash_vs_precise_1e-9": hashc["verified_vs_precise_1e-9"]}
+    for k, v in side.items():
+        if isinstance(v, dict) and "verified" in v:
+            checks[k] = v["verified"]
+        elif isinstance(v, list):
+            checks[k] = all(x.get("verified", False) for x in v)
+    line["checks"] = checks
+    line["verified"] = all(checks.values())
     print(json.dumps(line), flush=True)
     if ws > 1:
         import torch.distributed as dist
         dist.destroy_process_group()
+
+
+ALL_SECTIONS = ("cpu", "reader", "er", "stencil", "batch", "batch32", "served")
 
 
 def main():
@@ -693,6 +978,10 @@ def main():
     ap.add_argument("--no-batch", action="store_true",
                     help="skip the uneven-batch and served-stream sections")
     ap.add_argument("--serve-requests", type=int, default=600)
+    ap.add_argument("--sections", default="",
+                    help="comma list of side sections to run (default all: "
+                         + ",".join(ALL_SECTIONS) + "); the headline step, e2e, Upper and "
+                         "hash legs always run")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
