@@ -60,24 +60,29 @@ def _run(cmd: list[str]) -> str:
     return r.stdout + r.stderr
 
 
-def build_cuda(verbose: bool = False, debug: bool = False) -> Path:
+def build_cuda(verbose: bool = False, extra: list[str] | None = None) -> Path:
+    """Compiles libbrmerge.so; `extra` (or the BRM_NVCC_FLAGS environment
+    variable) adds nvcc flags, and a change of flags rebuilds every object."""
     nvcc = _nvcc()
     BUILD.mkdir(exist_ok=True)
     out = PKG / "libbrmerge.so"
     headers = list(CSRC.glob("*.cuh")) + list(CSRC.glob("*.h")) + [INCLUDE / "brmerge.h"]
+    extra = list(extra or []) + os.environ.get("BRM_NVCC_FLAGS", "").split()
     flags = ARCH + [
         "-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall",
         "-I", str(INCLUDE), "-I", str(CSRC),
-    ]
+    ] + extra
     if verbose:
         flags += ["-Xptxas", "-v"]
+    stamp = BUILD / "flags.txt"
+    same_flags = stamp.exists() and stamp.read_text() == " ".join(flags)
     objs = []
     jobs = []
     for src in CUDA_SOURCES:
         s = CSRC / src
         o = BUILD / (Path(src).stem + ".o")
         objs.append(o)
-        if _newer(o, [s] + headers):
+        if not same_flags or _newer(o, [s] + headers):
             jobs.append([nvcc] + flags + ["-c", str(s), "-o", str(o)])
     with cf.ThreadPoolExecutor(max_workers=max(1, min(len(jobs), os.cpu_count() or 4))) as ex:
         for log in ex.map(_run, jobs):
@@ -87,6 +92,7 @@ def build_cuda(verbose: bool = False, debug: bool = False) -> Path:
         tmp = out.with_suffix(".so.tmp")
         _run([nvcc] + ARCH + ["-shared", "-cudart", "static", "-o", str(tmp)] + [str(o) for o in objs])
         os.replace(tmp, out)
+    stamp.write_text(" ".join(flags))
     return out
 
 

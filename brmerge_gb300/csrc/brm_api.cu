@@ -53,7 +53,8 @@ enum TimingEvent : int {
 };
 constexpr long long kLongElems = 16ll << 20;  // products in the long-column scratch
 // candidates of brm_autotune (heavy-row cut target x mid-row weight limit)
-constexpr int kTuneSegCut[] = {1536, 1024, 768, 512};
+constexpr int kTuneSegCut[] = {brm::kSegCut, brm::kSegCut * 2 / 3, brm::kSegCut / 2,
+                                brm::kSegCut / 3};
 constexpr int kTuneMidFlop[] = {2048, 1024, 512};
 
 }  // namespace

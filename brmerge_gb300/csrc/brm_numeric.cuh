@@ -52,7 +52,16 @@ void numeric_phase(const CsrDev &A, const CsrDev &B, const PlanDev &P, const int
     const size_t ssm = SegLayout<T>::bytes;
     cudaFuncSetAttribute(k_seg_numeric<T, UPPER>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)ssm);
-    k_seg_numeric<T, UPPER><<<num_sms * 2, kSegThreads, ssm, s>>>(A, B, P, crpt, ccol, cval);
+    // as many segment CTAs as fit on every SM (shared memory and registers)
+    static int seg_per_sm = 0;
+    if (seg_per_sm <= 0) {
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&seg_per_sm, k_seg_numeric<T, UPPER>,
+                                                          kSegThreads, ssm) != cudaSuccess ||
+            seg_per_sm <= 0)
+            seg_per_sm = 1;
+    }
+    k_seg_numeric<T, UPPER><<<num_sms * seg_per_sm, kSegThreads, ssm, s>>>(A, B, P, crpt, ccol,
+                                                                            cval);
     count_launch();
     k_long_reduce<T><<<num_sms * 4, 128, 0, s>>>(P, ccol, cval);
     count_launch();

@@ -57,8 +57,14 @@ constexpr int kMidWarps = 2;      // the warp and tile rows
 // planning pass records, for every segment boundary and every list of the
 // row, where the list crosses the boundary (the split table), so each segment
 // is an independent unit of work.
-constexpr int kSegThreads = 256;
-constexpr int kSegCap = 3072;
+#ifndef BRM_SEG_THREADS
+#define BRM_SEG_THREADS 256
+#endif
+#ifndef BRM_SEG_CAP
+#define BRM_SEG_CAP 3072
+#endif
+constexpr int kSegThreads = BRM_SEG_THREADS;
+constexpr int kSegCap = BRM_SEG_CAP;
 constexpr int kSegCut = kSegCap / 2;      // target products between cuts
 constexpr int kSegMaxK = 65535;           // leaf index stored in 16 bits
 constexpr int kHugeFlop = 16 * kSegCap;   // heavy rows planned first (longest first)

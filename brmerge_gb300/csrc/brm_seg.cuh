@@ -502,9 +502,12 @@ struct SegLayout {
     static constexpr size_t o_pu = o_pleaf + mid_a16(kSegCap * 2);
     static constexpr size_t o_ia = o_pu + mid_a16(kSegCap * 2);
     static constexpr size_t o_ib = o_ia + mid_a16(kSegCap * 2);
-    static constexpr size_t o_summ = o_ib + mid_a16(kSegCap * 2);
+    // the summary words of a wide segment and their ranks are dead before
+    // the scatter first writes ib, so they share its space
+    static constexpr size_t o_summ = o_ib;
     static constexpr size_t o_srank = o_summ + mid_a16(kSumWords * 4);
-    static constexpr size_t o_cw = o_srank + mid_a16(kSumWords * 2);
+    static_assert(kSumWords * 4 + kSumWords * 2 <= kSegCap * 2, "summary words fit in ib");
+    static constexpr size_t o_cw = o_ib + mid_a16(kSegCap * 2);
     static constexpr size_t o_cwr = o_cw + mid_a16(kSegCap * 4);
     static constexpr size_t o_long = o_cwr + mid_a16((kSegCap + 1) * 2);
     static constexpr size_t o_ws = o_long + mid_a16(kLongMax * 2);
@@ -515,7 +518,7 @@ struct SegLayout {
 };
 
 template <typename T, bool UPPER>
-__global__ void __launch_bounds__(kSegThreads) k_seg_numeric(CsrDev A, CsrDev B, PlanDev P,
+__global__ void __launch_bounds__(kSegThreads, 512 / kSegThreads) k_seg_numeric(CsrDev A, CsrDev B, PlanDev P,
                                                              const int *crpt, int *ccol, T *cval)
 {
     constexpr int NT = kSegThreads;

@@ -13,7 +13,19 @@ from conftest import assert_same_csr
 
 pytestmark = pytest.mark.gpu
 
-SETTINGS = [(1536, 2048), (1024, 1024), (768, 512), (512, 2048), (256, 128)]
+
+def _defaults():
+    """The context defaults: the largest cut target and mid-row weight."""
+    c = brm.Context()
+    t = c.tuning()
+    c.close()
+    return t["seg_cut"], t["mid_flop"]
+
+
+def _settings():
+    cut, mid = _defaults()
+    return [(cut, mid), (cut * 2 // 3, mid // 2), (cut // 2, mid // 4), (cut // 3, mid),
+            (256, 128)]
 
 
 @pytest.fixture(scope="module")
@@ -33,28 +45,32 @@ def test_every_setting_gives_the_same_result(ctx, oracle_mod, name, A, B):
     B = A if B is None else B
     R = oracle_mod.precise(A, B)
     dA, dB = brm.DeviceCSR.from_host(A), brm.DeviceCSR.from_host(B)
-    for cut, mid in SETTINGS:
+    for cut, mid in _settings():
         ctx.set_tuning(seg_cut=cut, mid_flop=mid)
         assert ctx.tuning() == {"seg_cut": cut, "mid_flop": mid}
         assert_same_csr(ctx.precise_device(dA, dB).to_host(), R, f"{name} precise {cut}/{mid}")
         assert_same_csr(ctx.precise(dA, dB).to_host(), R, f"{name} split {cut}/{mid}")
         assert_same_csr(ctx.upper(dA, dB).to_host(), R, f"{name} upper {cut}/{mid}")
     ctx.set_tuning()
-    assert ctx.tuning() == {"seg_cut": 1536, "mid_flop": 2048}
+    cut, mid = _defaults()
+    assert ctx.tuning() == {"seg_cut": cut, "mid_flop": mid}
 
 
 def test_out_of_range_rejected(ctx):
-    for cut, mid in [(100, 2048), (1537, 2048), (1536, 4096), (1536, 64)]:
+    cut, mid = _defaults()
+    for c, m in [(100, mid), (cut + 1, mid), (cut, 2 * mid), (cut, 64)]:
         with pytest.raises(brm.BrmError):
-            ctx.set_tuning(seg_cut=cut, mid_flop=mid)
-    assert ctx.tuning() == {"seg_cut": 1536, "mid_flop": 2048}
+            ctx.set_tuning(seg_cut=c, mid_flop=m)
+    assert ctx.tuning() == {"seg_cut": cut, "mid_flop": mid}
 
 
 def test_autotune_single_and_batch(ctx, oracle_mod):
     A = brm.gen_rmat(14, 8 << 14, seed=46)
     dA = brm.DeviceCSR.from_host(A)
     t = ctx.autotune([(dA, dA)])
-    assert t["seg_cut"] in (1536, 1024, 768, 512) and t["mid_flop"] in (2048, 1024, 512)
+    cut, mid = _defaults()
+    assert t["seg_cut"] in (cut, cut * 2 // 3, cut // 2, cut // 3)
+    assert t["mid_flop"] in (mid, mid // 2, mid // 4)
     assert ctx.tuning() == t
     assert_same_csr(ctx.precise_device(dA, dA).to_host(), oracle_mod.precise(A, A), "tuned")
     pairs = [(brm.gen_lognormal(m, m, seed=50 + m), brm.gen_lognormal(m, m, seed=60 + m))
