@@ -630,8 +630,9 @@ __global__ void __launch_bounds__(kSegThreads, 512 / kSegThreads) k_seg_numeric(
         if (flat) {
             for (int i = tid; i < nwf; i += NT)
                 cw[i] = 0;
-        } else if (tid < nsum) {
-            summ[tid] = 0;
+        } else {
+            for (int i = tid; i < nsum; i += NT)
+                summ[i] = 0;
         }
         __syncthreads();
         // stage products in list-major (= leaf) order; mark their words in the
@@ -704,11 +705,18 @@ __global__ void __launch_bounds__(kSegThreads, 512 / kSegThreads) k_seg_numeric(
         // compressed words: one per nonempty 32-column word (flat: every word)
         int ncw = nwf;
         if (!flat) {
+            // SPT consecutive summary words a thread (nsum <= kSumWords)
+            constexpr int SPT = (kSumWords + NT - 1) / NT;
+            const int s0 = min(tid * SPT, nsum), s1 = min(s0 + SPT, nsum);
+            int sc = 0;
+            for (int i = s0; i < s1; i++)
+                sc += __popc(summ[i]);
             long long ncw_t;
-            const unsigned sv = tid < nsum ? summ[tid] : 0u;
-            const int sx = (int)block_excl_scan<NT, long long>(__popc(sv), ws, &ncw_t);
-            if (tid < nsum)
-                srank[tid] = (unsigned short)sx;
+            int sx = (int)block_excl_scan<NT, long long>(sc, ws, &ncw_t);
+            for (int i = s0; i < s1; i++) {
+                srank[i] = (unsigned short)sx;
+                sx += __popc(summ[i]);
+            }
             ncw = (int)ncw_t;
             for (int i = tid; i < ncw; i += NT)
                 cw[i] = 0;
