@@ -390,9 +390,12 @@ int plan_phase(brm_context ctx, const brm_csr *A, const brm_csr *B, int *crpt, b
     }
     {
         const size_t cap = (size_t)ctx->h_cnt->seg_cap + 1;
-        BRM_TRY(grow(ctx->segbuf, cap * (sizeof(brm::SegDesc) + sizeof(int))));
-        P.seg = (brm::SegDesc *)ctx->segbuf.p;
+        const size_t b_run = a256(cap * sizeof(brm::SegRun));
+        BRM_TRY(grow(ctx->segbuf, b_run + cap * (sizeof(brm::SegDesc) + sizeof(int))));
+        P.run = (brm::SegRun *)ctx->segbuf.p;
+        P.seg = (brm::SegDesc *)((unsigned char *)ctx->segbuf.p + b_run);
         P.seg_list = (int *)(P.seg + cap);
+        ctx->plan.run = P.run;
         ctx->plan.seg = P.seg;
         ctx->plan.seg_list = P.seg_list;
     }

@@ -94,6 +94,20 @@ __device__ __forceinline__ T block_excl_scan(T v, T *ws, T *total)
     return r;
 }
 
+// Asynchronous 16-byte global -> shared copy (cp.async, cached in L2 only);
+// both addresses 16-byte aligned.  cp_async_wait_all waits for every copy
+// this thread has issued.
+__device__ __forceinline__ void cp_async16(void *smem_dst, const void *gmem_src)
+{
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem_dst);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem_src) : "memory");
+}
+
+__device__ __forceinline__ void cp_async_wait_all()
+{
+    asm volatile("cp.async.wait_all;\n" ::: "memory");
+}
+
 template <int NT, typename T>
 __device__ __forceinline__ T block_sum(T v, T *ws)
 {

@@ -158,6 +158,23 @@ struct SegDesc {
     long long tab;  // split-table offset of the row (boundary-major, k entries each)
 };
 
+// A segment as the segment kernel reads it: one 48-byte record per entry of
+// the segment list (in list order), written by k_split, so that a segment
+// needs a single dependent load after the work counter (and the next one is
+// copied into shared memory while the current segment runs).
+struct __align__(16) SegRun {
+    long long sp;  // split-table offset of the segment's first boundary row (tab + bidx * k)
+    int row;
+    int c_lo;
+    int c_hi;
+    int u_off;     // distinct columns of the row before c_lo
+    int nprod;
+    int a0;        // A row start and length
+    int k;
+    int next_u;    // distinct columns of the row before the next segment (or its nnz)
+};
+static_assert(sizeof(SegRun) == 48, "three 16-byte copies");
+
 // A column of a heavy-row segment with many products, handed from the
 // segment kernel to the column reducer: its products' leaves and values in
 // leaf order at [off, off + len) of the long-column scratch, and the output
@@ -193,6 +210,7 @@ struct PlanDev {
     int2 *crange;          // [M] smallest and largest column of each heavy row (x > y: none)
     SegDesc *seg;          // [Counters::seg_cap] segment descriptors (numbered per row)
     int *seg_list;         // [Counters::seg_cap] descriptor slot of every written segment
+    SegRun *run;           // [Counters::seg_cap] records of the segment list (numeric phase)
     int *split;            // [Counters::table_cap] split table (numeric phase)
     LongCol *long_col;     // [long_cap_cols] long-column descriptors (numeric phase)
     unsigned short *long_leaf;  // [long_cap_elems] leaves of the long columns' products

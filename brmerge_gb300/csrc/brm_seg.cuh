@@ -472,6 +472,19 @@ __global__ void __launch_bounds__(256) k_split(CsrDev A, CsrDev B, PlanDev P)
         const int a0 = A.rpt[row];
         const int k = A.rpt[row + 1] - a0;
         int *t0 = P.split + tab + (long long)b * k;
+        if (threadIdx.x == 0) {
+            SegRun r;
+            r.sp = tab + (long long)b * k;
+            r.row = row;
+            r.c_lo = c_lo;
+            r.c_hi = P.seg[slot].c_hi;
+            r.u_off = P.seg[slot].u_off;
+            r.nprod = P.seg[slot].nprod;
+            r.a0 = a0;
+            r.k = k;
+            r.next_u = (b + 1 < nseg) ? P.seg[slot + 1].u_off : P.nnz[row];
+            P.run[it] = r;
+        }
         for (int l = threadIdx.x; l < k; l += blockDim.x) {
             const int s = P.abs[a0 + l];
             const int e = s + P.alen[a0 + l];
@@ -489,6 +502,14 @@ constexpr int kLongMin = 9;  // columns with this many products are reduced by w
 constexpr int kLongMax = kSegCap / kLongMin + 1;
 constexpr int kSegPWords = kSegCap / 32;  // words of a bitmap over a segment's products
 static_assert(kSegCap % 32 == 0 && kSegPWords <= 96, "p-bitmap prefix: three words per lane");
+
+// Copies a segment record (48 bytes) into shared memory with cp.async.
+__device__ __forceinline__ void copy_seg_run(SegRun *dst, const SegRun *src)
+{
+#pragma unroll
+    for (int q = 0; q < 3; q++)
+        cp_async16((unsigned char *)dst + 16 * q, (const unsigned char *)src + 16 * q);
+}
 
 template <typename T>
 struct SegLayout {
@@ -512,7 +533,8 @@ struct SegLayout {
     static constexpr size_t o_long = o_cwr + mid_a16((kSegCap + 1) * 2);
     static constexpr size_t o_ws = o_long + mid_a16(kLongMax * 2);
     static constexpr size_t o_misc = o_ws + mid_a16((NW + 1) * 8);
-    static constexpr size_t bytes = o_misc + 64;
+    static constexpr size_t o_run = o_misc + 64;  // the next segment's record
+    static constexpr size_t bytes = o_run + sizeof(SegRun);
     // per-warp p-bitmaps and their word prefixes live in cw once u is known
     static_assert(NW * kSegPWords * 6 <= kSegCap * 4, "cw region holds the warp bitmaps");
 };
@@ -542,32 +564,44 @@ __global__ void __launch_bounds__(kSegThreads, 512 / kSegThreads) k_seg_numeric(
     long long *ws = (long long *)(smem + L::o_ws);
     int *wsi = (int *)(smem + L::o_ws);
     int *misc = (int *)(smem + L::o_misc);
+    SegRun *srun = (SegRun *)(smem + L::o_run);
     const int tid = threadIdx.x;
     const int i0 = P.seg_range ? P.seg_range[0] : 0;
     const int nsegs = P.seg_range ? P.seg_range[1] : P.cnt->n_seg;
     const int *__restrict__ bcol = B.col;
     const T *__restrict__ bval = (const T *)B.val;
     const T *__restrict__ aval = (const T *)A.val;
+    // thread 0 takes the next work item one segment ahead and copies its
+    // record into srun (cp.async) while the current segment runs, so a
+    // segment starts without a chain of dependent global loads
+    int pf = 0;
+    bool pf_copied = false;
+    if (tid == 0)
+        pf = i0 + atomicAdd(&P.cnt->work_seg, 1);
     for (;;) {
-        if (tid == 0)
-            misc[0] = i0 + atomicAdd(&P.cnt->work_seg, 1);
+        if (tid == 0) {
+            if (!pf_copied && pf < nsegs)
+                copy_seg_run(srun, P.run + pf);
+            cp_async_wait_all();
+            misc[0] = pf;
+        }
         __syncthreads();
         const int item = misc[0];
-        __syncthreads();
         if (item >= nsegs)
             break;
-        const int slot = P.seg_list[item];
-        const SegDesc d = P.seg[slot];
+        const SegRun d = *srun;
+        if (tid == 0) {
+            pf = i0 + atomicAdd(&P.cnt->work_seg, 1);  // consumed after the staging
+            pf_copied = false;
+        }
         const int row = d.row;
-        const int a0 = A.rpt[row];
-        const int k = A.rpt[row + 1] - a0;
+        const int a0 = d.a0;
+        const int k = d.k;
         const int span = d.c_hi - d.c_lo;
         // distinct columns of the row up to the next segment (checked at the end)
-        int next_u = 0;
-        if (tid == 0)
-            next_u = (d.bidx + 1 < P.seg_n[row]) ? P.seg[slot + 1].u_off : P.nnz[row];
+        const int next_u = d.next_u;
         const int nsum = (span + 1023) >> 10;
-        const int *sp0 = P.split + d.tab + (long long)d.bidx * k;
+        const int *sp0 = P.split + d.sp;
         const int *sp1 = sp0 + k;
         // nonempty sub-lists of the segment, in leaf order (a thread takes
         // four consecutive lists per pass: hub rows have thousands of lists
@@ -697,6 +731,11 @@ __global__ void __launch_bounds__(kSegThreads, 512 / kSegThreads) k_seg_numeric(
                 atomicOr(flat ? &cw[run_w] : &summ[run_w], run_b);
         }
         __syncthreads();
+        // every thread has read this segment's record: copy the next one
+        if (tid == 0 && pf < nsegs) {
+            copy_seg_run(srun, P.run + pf);
+            pf_copied = true;
+        }
         if (misc[2]) {  // a column outside the segment: the plan does not match the input
             if (tid == 0)
                 atomicOr(&P.cnt->err, kErrBadInput);
@@ -720,10 +759,10 @@ __global__ void __launch_bounds__(kSegThreads, 512 / kSegThreads) k_seg_numeric(
             ncw = (int)ncw_t;
             for (int i = tid; i < ncw; i += NT)
                 cw[i] = 0;
+            for (int i = tid; i <= nprod; i += NT)  // the sub-list table is dead now
+                ucnt[i] = 0;
+            __syncthreads();
         }
-        for (int i = tid; i <= nprod; i += NT)  // the sub-list table is dead now
-            ucnt[i] = 0;
-        __syncthreads();
         // mark the compressed words; keep each product's word index in pu
         if (!flat) {
             int run_ci = -1;
@@ -743,8 +782,14 @@ __global__ void __launch_bounds__(kSegThreads, 512 / kSegThreads) k_seg_numeric(
             }
             if (bits)
                 atomicOr(&cw[run_ci], bits);
+            __syncthreads();
+        } else {
+            // a flat segment clears the column counts here (the sub-list
+            // table they overwrite is dead since the staging barrier); the
+            // barrier of the rank scan below orders them before the counting
+            for (int i = tid; i <= nprod; i += NT)
+                ucnt[i] = 0;
         }
-        __syncthreads();
         // ranks of the compressed words -> distinct columns before each word
         long long U_t;
         {
@@ -903,15 +948,29 @@ __global__ void __launch_bounds__(kSegThreads, 512 / kSegThreads) k_seg_numeric(
             unsigned short *wpre = (unsigned short *)(cw + L::NW * kSegPWords) + wid * kSegPWords;
             const int nwp = (nprod + 31) >> 5;
             T *lval = (T *)P.long_val;
-            for (int li = wid; li < nlong; li += L::NW) {
-                const int u = longu[li];
-                const int i0 = ucnt[u], i1 = ucnt[u + 1], len = i1 - i0;
-                unsigned long long rsv = 0;
-                if (lane == 0)
-                    rsv = atomicAdd(&P.cnt->long_used, (1ull << 40) | (unsigned long long)len);
-                rsv = __shfl_sync(kFull, rsv, 0);
-                const long long lci = (long long)(rsv >> 40);
-                const long long leo = (long long)(rsv & ((1ull << 40) - 1ull));
+            for (int lb = wid; lb < nlong; lb += 32 * L::NW) {
+              // the warp's next (up to) 32 columns lb + j * NW: one
+              // reservation of long-column scratch covers all of them
+              const int lj = lb + lane * L::NW;
+              int myu = 0, mylen = 0;
+              if (lj < nlong) {
+                  myu = longu[lj];
+                  mylen = ucnt[myu + 1] - ucnt[myu];
+              }
+              const int ncol = __popc(__ballot_sync(kFull, lj < nlong));
+              const int lincl = warp_incl_scan(mylen);
+              unsigned long long rsv = 0;
+              if (lane == 31)
+                  rsv = atomicAdd(&P.cnt->long_used,
+                                  ((unsigned long long)ncol << 40) | (unsigned long long)lincl);
+              rsv = __shfl_sync(kFull, rsv, 31);
+              for (int jc = 0; jc < ncol; jc++) {
+                const int u = __shfl_sync(kFull, myu, jc);
+                const int len = __shfl_sync(kFull, mylen, jc);
+                const int i0 = ucnt[u], i1 = i0 + len;
+                const long long lci = (long long)(rsv >> 40) + jc;
+                const long long leo = (long long)(rsv & ((1ull << 40) - 1ull)) +
+                                      __shfl_sync(kFull, lincl - mylen, jc);
                 const bool handoff = lci < P.long_cap_cols && leo + len <= P.long_cap_elems;
                 for (int w = lane; w < nwp; w += 32)
                     bmp[w] = 0;
@@ -972,6 +1031,7 @@ __global__ void __launch_bounds__(kSegThreads, 512 / kSegThreads) k_seg_numeric(
                     cval[obase + u] = sr.finish();
                 }
                 __syncwarp();
+              }
             }
         }
         // the segment must produce exactly its share of the row's columns
