@@ -639,6 +639,26 @@ def batched_section(ctx, dev, stream, steps: int, dtype=np.float64, tune: bool =
     graph_ms = statistics.mean(gts[1:])
     graph_ok = all(dev_same_csr(x, y) for x, y in zip(g.results, bviews))
     g.close()
+    # a new batch every launch: the pipeline captured once (capacities from
+    # this batch + 25 %), run alternately on the pairs and on the pairs in
+    # reverse order (another stacked structure), one graph launch per batch
+    pipe = ctx.batch_pipe(dpairs, headroom=1.25)
+    orders = [list(range(len(dpairs))), list(range(len(dpairs)))[::-1]]
+    pts, pwall = [], []
+    l0 = L.brm_kernel_launches()
+    for i in range(steps + 1):
+        batch = [dpairs[j] for j in orders[i % 2]]
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t0 = time.perf_counter()
+        e0.record(stream)
+        pipe_out = pipe.run_raw(batch, stream)
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        pwall.append(time.perf_counter() - t0)
+        pts.append(e0.elapsed_time(e1))
+    pipe_launches = (L.brm_kernel_launches() - l0) / (steps + 1)
+    pipe_ms = statistics.mean(pts[1:])
+    pipe_order = orders[steps % 2]
     ctx.set_tuning()  # the plain loop below runs with the defaults
     # plain per-call loop over the same pairs (one pass; results kept for the check)
     for a, b in dpairs[:16]:
@@ -651,6 +671,11 @@ def batched_section(ctx, dev, stream, steps: int, dtype=np.float64, tune: bool =
     torch.cuda.synchronize(dev)
     plain_s = time.perf_counter() - t0
     batch_ok = all(dev_same_csr(x, y) for x, y in zip(bviews, plain))
+    pviews = batch_views((None,) + pipe_out[:1] + pipe_out[1:2] + pipe_out[2:5],
+                         [dpairs[j] for j in pipe_order])
+    pipe_ok = all(dev_same_csr(v, plain[j]) for v, j in zip(pviews, pipe_order))
+    del pviews, pipe_out
+    pipe.close()
     oracle.build(with_ref=False)
     nt = oracle.max_threads()
     oracle_ok = all(same_csr(SimpleNamespace(rpt=v.rpt.cpu().numpy(), col=v.col.cpu().numpy(),
@@ -670,9 +695,19 @@ def batched_section(ctx, dev, stream, steps: int, dtype=np.float64, tune: bool =
         "plain_gflops": round(2 * products / plain_s / 1e9, 3),
         "speedup_vs_plain": round(plain_s * 1e3 / b_ms, 2),
         "launches_per_batch": launches, "steps": steps,
-        "verified": bool(batch_ok and graph_ok and oracle_ok),
+        "pipeline": {"call": "brm_batch_pipe_run (one graph launch per new batch)",
+                     "ms": round(pipe_ms, 3),
+                     "gflops": round(2 * products / (pipe_ms / 1e3) / 1e9, 3),
+                     "host_wall_ms": round(statistics.mean(pwall[1:]) * 1e3, 3),
+                     "speedup_vs_plain": round(plain_s * 1e3 / pipe_ms, 2),
+                     "graph_launches_per_batch": 1,
+                     "kernels_per_batch": pipe_launches,
+                     "batches": "pairs in order and reversed, alternately (a new structure "
+                                "every launch)"},
+        "verified": bool(batch_ok and graph_ok and oracle_ok and pipe_ok),
         "checks": {"every_pair_vs_plain_call": bool(batch_ok),
                    "graph_replay_vs_batch": bool(graph_ok),
+                   "pipeline_every_pair_vs_plain_call": bool(pipe_ok),
                    f"first_{n_oracle}_pairs_vs_oracle": bool(oracle_ok)},
     })
     return res

@@ -49,6 +49,14 @@ class BatchC(C.Structure):
                 ("rpt_local", C.c_void_p)]
 
 
+class BatchCapsC(C.Structure):
+    """Mirror of brm_batch_caps."""
+    _fields_ = [("pairs", C.c_int), ("rows", C.c_longlong), ("nnz_a", C.c_longlong),
+                ("b_rows", C.c_longlong), ("nnz_b", C.c_longlong), ("cols", C.c_int),
+                ("products", C.c_longlong), ("seg_slots", C.c_longlong), ("table", C.c_longlong),
+                ("spill_bytes", C.c_longlong)]
+
+
 class ServerConfigC(C.Structure):
     """Mirror of brm_server_config."""
     _fields_ = [("mem_cap_bytes", C.c_longlong), ("max_batch", C.c_int), ("workers", C.c_int)]
@@ -130,6 +138,13 @@ def lib() -> C.CDLL:
               [vp, C.c_int, C.c_int, csrp, csrp, ctxp, C.POINTER(BatchC)])
         _decl(L.brm_batch_graph_launch, C.c_int, [vp, vp])
         _decl(L.brm_batch_graph_destroy, C.c_int, [vp])
+        capsp = C.POINTER(BatchCapsC)
+        _decl(L.brm_batch_caps_for, C.c_int,
+              [vp, C.c_int, C.c_int, csrp, csrp, C.c_double, capsp])
+        _decl(L.brm_batch_pipe_create, C.c_int, [vp, C.c_int, capsp, ctxp])
+        _decl(L.brm_batch_pipe_caps, C.c_int, [vp, capsp])
+        _decl(L.brm_batch_pipe_run, C.c_int, [vp, C.c_int, csrp, csrp, vp, C.POINTER(BatchC)])
+        _decl(L.brm_batch_pipe_destroy, C.c_int, [vp])
         _decl(L.brm_set_tuning, C.c_int, [vp, C.POINTER(TuningC)])
         _decl(L.brm_get_tuning, C.c_int, [vp, C.POINTER(TuningC)])
         _decl(L.brm_autotune, C.c_int, [vp, C.c_int, C.c_int, csrp, csrp, C.POINTER(TuningC)])

@@ -524,6 +524,31 @@ void launch_validate(const CsrDev &X, int ncols, int *bad_row, cudaStream_t s)
 
 }  // namespace brm
 
+namespace brm {
+
+__global__ void k_pipe_admit(PlanDev P, int M, PipeCaps caps, int stage)
+{
+    Counters *c = P.cnt;
+    bool bad;
+    if (stage == 0)
+        bad = (long long)c->total_flop > caps.products || (long long)c->seg_cap > caps.seg_slots ||
+              P.mid_pre[M] + P.mw_pre[M] > caps.products;
+    else
+        bad = (long long)c->table_cap > caps.table || (long long)c->spill_bytes > caps.spill_bytes;
+    if (bad) {
+        c->abort = 1;
+        atomicOr(&c->err, kErrCapacity);
+    }
+}
+
+void launch_pipe_admit(const PlanDev &P, int M, const PipeCaps &caps, int stage, cudaStream_t s)
+{
+    k_pipe_admit<<<1, 1, 0, s>>>(P, M, caps, stage);
+    count_launch();
+}
+
+}  // namespace brm
+
 // SM version of the device code this library runs on the current device.
 extern "C" int brm_device_code_version(int *sm)
 {

@@ -23,6 +23,10 @@ std::atomic<long long> g_launches{0};
 
 void brm::count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 
+void brm::count_launches(long long n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+
+long long brm::launches_so_far() { return g_launches.load(std::memory_order_relaxed); }
+
 namespace {
 
 struct DevBuf {
@@ -279,6 +283,8 @@ int device_err_status(int err)
         return BRM_ERR_OVERFLOW;
     if (err & brm::kErrBadInput)
         return BRM_ERR_INVALID_CSR;
+    if (err & brm::kErrCapacity)
+        return BRM_ERR_CAPACITY;
     return BRM_ERR_INTERNAL;
 }
 
@@ -465,13 +471,40 @@ struct RowPart {
     const int *seg_list = nullptr;
 };
 
+// Bytes of the long-column scratch for `elems` products.
+size_t long_bytes(long long elems, brm_dtype dtype)
+{
+    const long long cols = elems / 8 + 1024;
+    return a256(sizeof(brm::LongCol) * (size_t)cols) + a256(2 * (size_t)elems + 2) +
+           vsize(dtype) * (size_t)elems + 8;
+}
+
+// Sizes of the numeric phase's buffers: from the planning's counters, or
+// the capacities of a captured pipeline (whose buffers are grown ahead).
+struct NumSizes {
+    unsigned long long table_cap = 0;    // split-table entries
+    unsigned long long total_flop = 0;   // products (long-column scratch)
+    unsigned long long spill_bytes = 0;  // spill scratch
+};
+
+NumSizes planned_sizes(brm_context ctx)
+{
+    NumSizes z;
+    z.table_cap = ctx->h_cnt->table_cap;
+    z.total_flop = ctx->h_cnt->total_flop;
+    z.spill_bytes = ctx->spill_bytes;
+    return z;
+}
+
 int numeric_launch(brm_context ctx, brm_dtype dtype, bool upper, const brm_csr *A,
                    const brm_csr *B, const int *crpt, int *ccol, void *cval, bool use_mid = false,
-                   const RowPart &part = RowPart(), bool clear_err = true)
+                   const RowPart &part = RowPart(), bool clear_err = true,
+                   const NumSizes *sizes = nullptr)
 {
     const bool mid = use_mid && ctx->mid_ready && !upper;
-    if (ctx->spill_bytes)
-        BRM_TRY(grow(ctx->spill, ctx->spill_bytes));
+    const NumSizes sz = sizes ? *sizes : planned_sizes(ctx);
+    if (sz.spill_bytes)
+        BRM_TRY(grow(ctx->spill, sz.spill_bytes));
     cudaStream_t s = ctx->stream;
     brm::PlanDev P = ctx->plan;
     P.r_lo = part.r_lo;
@@ -482,17 +515,17 @@ int numeric_launch(brm_context ctx, brm_dtype dtype, bool upper, const brm_csr *
     // work_num and (unless the errors of earlier parts must survive) err
     BRM_CK(cudaMemsetAsync(&P.cnt->work_num, 0, (clear_err ? 2 : 1) * sizeof(int), s));
     BRM_CK(cudaMemsetAsync(&P.cnt->work_bnum, 0, 2 * sizeof(int), s));  // work_bnum, work_seg
-    BRM_TRY(grow(ctx->splitbuf, ((size_t)ctx->h_cnt->table_cap + 1) * sizeof(int)));
+    BRM_TRY(grow(ctx->splitbuf, ((size_t)sz.table_cap + 1) * sizeof(int)));
     P.split = (int *)ctx->splitbuf.p;
     ctx->plan.split = P.split;
     {
         // long-column scratch: at most kLongElems products (columns beyond it
         // are reduced inside the segment kernel)
-        const long long elems = std::min<long long>((long long)ctx->h_cnt->total_flop, kLongElems);
+        const long long elems = std::min<long long>((long long)sz.total_flop, kLongElems);
         const long long cols = elems / 8 + 1024;
         const size_t b_col = a256(sizeof(brm::LongCol) * (size_t)cols);
         const size_t b_leaf = a256(2 * (size_t)elems + 2);
-        BRM_TRY(grow(ctx->longbuf, b_col + b_leaf + vsize(dtype) * (size_t)elems + 8));
+        BRM_TRY(grow(ctx->longbuf, long_bytes(elems, dtype)));
         unsigned char *q = (unsigned char *)ctx->longbuf.p;
         P.long_col = (brm::LongCol *)q;
         P.long_leaf = (unsigned short *)(q + b_col);
@@ -505,10 +538,10 @@ int numeric_launch(brm_context ctx, brm_dtype dtype, bool upper, const brm_csr *
     const int *mcol = mid ? ctx->mid_col : nullptr;
     const void *mval = mid ? ctx->mid_val : nullptr;
     if (dtype == BRM_F64)
-        brm::launch_numeric_f64(upper, a, b, P, crpt, ccol, cval, ctx->spill.p, ctx->spill_bytes,
+        brm::launch_numeric_f64(upper, a, b, P, crpt, ccol, cval, ctx->spill.p, sz.spill_bytes,
                                 mcol, mval, ctx->num_sms, s, ctx->fork);
     else
-        brm::launch_numeric_f32(upper, a, b, P, crpt, ccol, cval, ctx->spill.p, ctx->spill_bytes,
+        brm::launch_numeric_f32(upper, a, b, P, crpt, ccol, cval, ctx->spill.p, sz.spill_bytes,
                                 mcol, mval, ctx->num_sms, s, ctx->fork);
     BRM_CK(cudaGetLastError());
     return BRM_SUCCESS;
@@ -830,6 +863,92 @@ int brm::numeric_async(brm_context ctx, brm_dtype dtype, const brm_csr *A, const
 }
 
 int brm::read_device_error(brm_context ctx) { return read_err(ctx); }
+
+int brm::device_status(int err) { return device_err_status(err); }
+
+const brm::Counters *brm::context_counters(brm_context ctx) { return ctx->plan.cnt; }
+
+brm::Counters brm::last_plan_counters(brm_context ctx) { return *ctx->h_cnt; }
+
+int brm::reserve_pipe(brm_context ctx, brm_dtype dtype, const brm::PipeCaps &c)
+{
+    if (c.rows < 1 || c.rows >= INT_MAX || c.nnz_a > INT_MAX || c.products > INT_MAX ||
+        c.seg_slots < 0 || c.table < 0 || c.spill_bytes < 0)
+        return BRM_ERR_CAPACITY;
+    BRM_TRY(ensure_workspace(ctx, (int)c.rows));
+    BRM_TRY(ensure_ameta(ctx, (int)c.nnz_a));
+    {
+        const size_t cap = (size_t)c.seg_slots + 1;
+        const size_t b_run = a256(cap * sizeof(brm::SegRun));
+        BRM_TRY(grow(ctx->segbuf, b_run + cap * (sizeof(brm::SegDesc) + sizeof(int))));
+        ctx->plan.run = (brm::SegRun *)ctx->segbuf.p;
+        ctx->plan.seg = (brm::SegDesc *)((unsigned char *)ctx->segbuf.p + b_run);
+        ctx->plan.seg_list = (int *)(ctx->plan.seg + cap);
+    }
+    {
+        const size_t n = (size_t)std::max(c.products, 1LL);
+        const size_t b_col = a256(4 * n);
+        BRM_TRY(grow(ctx->midbuf, b_col + vsize(dtype) * n));
+        ctx->mid_col = (int *)ctx->midbuf.p;
+        ctx->mid_val = (unsigned char *)ctx->midbuf.p + b_col;
+    }
+    BRM_TRY(grow(ctx->splitbuf, ((size_t)c.table + 1) * sizeof(int)));
+    BRM_TRY(grow(ctx->longbuf, long_bytes(std::min<long long>(c.products, kLongElems), dtype)));
+    if (c.spill_bytes)
+        BRM_TRY(grow(ctx->spill, (size_t)c.spill_bytes));
+    BRM_CK(cudaDeviceSynchronize());  // the buffers exist before any capture
+    return BRM_SUCCESS;
+}
+
+int brm::precise_pipe(brm_context ctx, brm_dtype dtype, const brm_csr *A, const brm_csr *B,
+                      int *crpt, int *ccol, void *cval, const brm::PipeCaps &caps)
+{
+    BRM_TRY(check_dtype(dtype));
+    BRM_TRY(check_pair(A, B));
+    if (A->M > caps.rows || A->nnz > caps.nnz_a || B->M > caps.b_rows || B->nnz > caps.nnz_b ||
+        B->N > caps.cols)
+        return BRM_ERR_CAPACITY;
+    brm::CsrDev a = to_dev(A), b = to_dev(B);
+    ctx->plan.M = A->M;
+    ctx->plan.r_lo = 0;
+    ctx->plan.r_hi = A->M;
+    ctx->plan.seg_range = nullptr;
+    ctx->planned = false;
+    const brm::PlanDev P = ctx->plan;
+    cudaStream_t s = ctx->stream;
+    BRM_CK(cudaMemsetAsync(P.cnt, 0, sizeof(brm::Counters), s));
+    brm::launch_analyze(a, b, P, s);
+    brm::launch_batches(P, A->M, ctx->scan_tmp, s);
+    brm::launch_pipe_admit(P, A->M, caps, 0, s);
+    const brm::Fork &fk = ctx->fork;
+    BRM_CK(cudaEventRecord(fk.fork, s));
+    BRM_CK(cudaStreamWaitEvent(fk.aux, fk.fork, 0));
+    if (dtype == BRM_F64)
+        brm::launch_mid_scratch_f64(a, b, P, ctx->mid_col, ctx->mid_val, ctx->num_sms, fk.aux,
+                                    brm::kMidGroups);
+    else
+        brm::launch_mid_scratch_f32(a, b, P, ctx->mid_col, ctx->mid_val, ctx->num_sms, fk.aux,
+                                    brm::kMidGroups);
+    BRM_CK(cudaEventRecord(fk.join, fk.aux));
+    brm::launch_symbolic(a, b, P, ctx->num_sms, false, true, s);
+    if (dtype == BRM_F64)
+        brm::launch_mid_scratch_f64(a, b, P, ctx->mid_col, ctx->mid_val, ctx->num_sms, s,
+                                    brm::kMidWarps);
+    else
+        brm::launch_mid_scratch_f32(a, b, P, ctx->mid_col, ctx->mid_val, ctx->num_sms, s,
+                                    brm::kMidWarps);
+    BRM_CK(cudaStreamWaitEvent(s, fk.join, 0));
+    brm::launch_scan_i32(P.nnz, crpt, A->M, P.cnt, ctx->scan_tmp, s);
+    brm::launch_pipe_admit(P, A->M, caps, 1, s);
+    BRM_CK(cudaGetLastError());
+    ctx->mid_ready = true;
+    NumSizes z;
+    z.table_cap = (unsigned long long)caps.table;
+    z.total_flop = (unsigned long long)caps.products;
+    z.spill_bytes = (unsigned long long)caps.spill_bytes;
+    // the plan's error bits (capacity, bad input) must survive the numeric phase
+    return numeric_launch(ctx, dtype, false, A, B, crpt, ccol, cval, true, RowPart(), false, &z);
+}
 
 std::mutex &brm::shared_context_mutex() { return g_mu; }
 

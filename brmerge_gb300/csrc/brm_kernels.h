@@ -28,9 +28,31 @@ int read_device_error(brm_context ctx);
 std::mutex &shared_context_mutex();
 int shared_context(brm_context *out);
 
+// Captured batch pipelines (brm_batch.cu): reserve_pipe grows every buffer
+// of ctx to the capacities (not capturable: it allocates); precise_pipe then
+// enqueues one whole Precise call on ctx's stream with no host
+// synchronisation and no allocation (capturable), the counts of each input
+// checked against the capacities on the device.  The mid rows are computed
+// with the plan.  Errors and nnz(C) stay in the device counters
+// (context_counters) for the caller to read after the stream.
+int reserve_pipe(brm_context ctx, brm_dtype dtype, const PipeCaps &caps);
+int precise_pipe(brm_context ctx, brm_dtype dtype, const brm_csr *A, const brm_csr *B, int *crpt,
+                 int *ccol, void *cval, const PipeCaps &caps);
+const Counters *context_counters(brm_context ctx);
+// The counters the last planning left on the host (after a synchronised call).
+Counters last_plan_counters(brm_context ctx);
+// Device-side capacity check of a captured pipeline: stage 0 after the row
+// analysis and the mid-row prefix sums, stage 1 after the symbolic phase.
+void launch_pipe_admit(const PlanDev &P, int M, const PipeCaps &caps, int stage, cudaStream_t s);
+int device_status(int err);
+
 // Counts one kernel launch of this library (brm_kernel_launches reports the
 // process-wide total); every launch site calls it right after <<<...>>>.
 void count_launch();
+// Adds n kernel launches (the kernels of a captured graph at each launch),
+// and the process-wide count so far.
+void count_launches(long long n);
+long long launches_so_far();
 
 // Row analysis: products per row, row bins and lists, total products
 // (replaces compute_flop and the static load balance, spgemm.h:31-56, :496-503).

@@ -413,6 +413,8 @@ template <typename T, bool UPPER, bool SCRATCH = false>
 __global__ void __launch_bounds__(kMidThreads) k_mid_numeric(CsrDev A, CsrDev B, PlanDev P,
                                                              const int *crpt, int *ccol, T *cval)
 {
+    if (P.cnt->abort)  // a capacity check of a captured pipeline failed
+        return;
     constexpr int NT = kMidThreads;
     using L = MidNumLayout<T>;
     extern __shared__ __align__(16) unsigned char smem[];
@@ -617,6 +619,8 @@ __global__ void __launch_bounds__(256) k_mid_compact(PlanDev P, int M, const int
                                                      const T *__restrict__ sval, const int *crpt,
                                                      int *__restrict__ ccol, T *__restrict__ cval)
 {
+    if (P.cnt->abort)  // a capacity check of a captured pipeline failed
+        return;
     const int lane = threadIdx.x & 31;
     const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nwarps = (gridDim.x * blockDim.x) >> 5;

@@ -345,6 +345,8 @@ template <typename T, int MODE, int SID>
 __global__ void __launch_bounds__(mw_threads<SID>(), 2) k_mid_warp(CsrDev A, CsrDev B, PlanDev P,
                                                                const int *crpt, int *ccol, T *cval)
 {
+    if (P.cnt->abort)  // a capacity check of a captured pipeline failed
+        return;
     using S = MwShape<SID>;
     using L = MidWarpLayout<SID>;
     constexpr int G = S::G;
@@ -542,6 +544,8 @@ template <typename T, int MODE, int KPL>
 __global__ void __launch_bounds__(kMwThreads, 2) k_mid_tile(CsrDev A, CsrDev B, PlanDev P,
                                                          const int *crpt, int *ccol, T *cval)
 {
+    if (P.cnt->abort)  // a capacity check of a captured pipeline failed
+        return;
     using S = MtShape<KPL>;
     using TL = MidTileLayout<S::FM>;
     constexpr int TW = kMtTW, IDX = S::IDX, kMtF = S::FM;

@@ -82,6 +82,7 @@ enum DevErr : int {
     kErrSpillCapacity = 4,   // spill scratch smaller than a spill row needs
     kErrOverflow = 8,        // an int32 quantity overflowed
     kErrBadInput = 16,       // an index out of range seen by a kernel
+    kErrCapacity = 32,       // a batch exceeded a captured pipeline's capacities
 };
 
 // Row classes assigned by the analysis kernel.
@@ -124,6 +125,10 @@ struct Counters {
     // long columns of the segment kernel handed to the column reducer:
     // (columns << 40) | elements reserved so far
     unsigned long long long_used;
+    // set by the capacity checks of a captured batch pipeline when the batch
+    // does not fit its buffers; every kernel that writes at data-dependent
+    // offsets then returns at once (the call reports BRM_ERR_CAPACITY)
+    int abort;
 };
 
 // Descriptor slots reserved for a heavy row with F products and the cut
@@ -227,6 +232,21 @@ struct PlanDev {
     int seg_cut;
     int mid_limit;
     Counters *cnt;
+};
+
+// Capacities of a captured batch pipeline: every buffer sized by a count the
+// planning computes on the device is grown to these once, and admission
+// kernels compare each batch's counts with them (Counters::abort).
+struct PipeCaps {
+    long long rows;         // rows of the stacked A (and of C)
+    long long nnz_a;        // entries of the stacked A
+    long long b_rows;       // rows of the stacked B
+    long long nnz_b;        // entries of the stacked B
+    long long cols;         // columns of the stacked B
+    long long products;     // intermediate products (bounds nnz(C) and the mid-row scratch)
+    long long seg_slots;    // heavy-row segment descriptors
+    long long table;        // split-table entries
+    long long spill_bytes;  // spill scratch
 };
 
 struct CsrDev {

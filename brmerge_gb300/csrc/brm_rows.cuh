@@ -205,6 +205,8 @@ __host__ __device__ __forceinline__ unsigned long long spill_row_bytes(long long
 template <bool ONLY_HEAVY>
 __global__ void __launch_bounds__(kRowThreads) k_rows_symbolic(CsrDev A, CsrDev B, PlanDev P)
 {
+    if (P.cnt->abort)  // a capacity check of a captured pipeline failed
+        return;
     constexpr int NT = kRowThreads;
     extern __shared__ __align__(16) unsigned char smem[];
     unsigned *bm = (unsigned *)(smem + SymLayout::o_bm);
@@ -608,6 +610,8 @@ template <typename T, bool UPPER>
 __global__ void __launch_bounds__(kRowThreads, 1)
     k_rows_numeric(CsrDev A, CsrDev B, PlanDev P, const int *crpt, int *ccol, T *cval)
 {
+    if (P.cnt->abort)  // a capacity check of a captured pipeline failed
+        return;
     extern __shared__ __align__(16) unsigned char smem[];
     int *misc = (int *)(smem + NumLayout<T>::o_misc);
     const int M = A.M;
@@ -712,6 +716,8 @@ template <typename T, bool UPPER>
 __global__ void __launch_bounds__(256) k_warp_numeric(CsrDev A, CsrDev B, PlanDev P,
                                                       const int *crpt, int *ccol, T *cval)
 {
+    if (P.cnt->abort)  // a capacity check of a captured pipeline failed
+        return;
     const int lane = threadIdx.x & 31;
     const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nwarps = (gridDim.x * blockDim.x) >> 5;
@@ -794,6 +800,8 @@ __global__ void __launch_bounds__(256) k_copy_numeric(CsrDev A, CsrDev B, PlanDe
                                                       const int *crpt, int *__restrict__ ccol,
                                                       T *__restrict__ cval)
 {
+    if (P.cnt->abort)  // a capacity check of a captured pipeline failed
+        return;
     const int lane = threadIdx.x & 31;
     const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nwarps = (gridDim.x * blockDim.x) >> 5;
@@ -844,6 +852,8 @@ __global__ void __launch_bounds__(32) k_spill_numeric(CsrDev A, CsrDev B, PlanDe
                                                       unsigned char *scratch,
                                                       unsigned long long scratch_bytes)
 {
+    if (P.cnt->abort)  // a capacity check of a captured pipeline failed
+        return;
     if (threadIdx.x != 0)
         return;
     const int n = P.cnt->spill_count;

@@ -179,6 +179,8 @@ __device__ __forceinline__ void plan_group_starts(int g, unsigned h, unsigned ph
 template <int UNUSED = 0>
 __global__ void __launch_bounds__(kPlanThreads) k_heavy_plan(CsrDev A, CsrDev B, PlanDev P)
 {
+    if (P.cnt->abort)  // a capacity check of a captured pipeline failed
+        return;
     constexpr int NT = kPlanThreads;
     extern __shared__ __align__(16) unsigned char smem[];
     unsigned *bm = (unsigned *)(smem + PlanLayout::o_bm);
@@ -459,6 +461,8 @@ __global__ void __launch_bounds__(kPlanThreads) k_heavy_plan(CsrDev A, CsrDev B,
 template <int UNUSED = 0>
 __global__ void __launch_bounds__(256) k_split(CsrDev A, CsrDev B, PlanDev P)
 {
+    if (P.cnt->abort)  // a capacity check of a captured pipeline failed
+        return;
     const int i0 = P.seg_range ? P.seg_range[0] : 0;
     const int nsegs = P.seg_range ? P.seg_range[1] : P.cnt->n_seg;
     const int *__restrict__ bcol = B.col;
@@ -543,6 +547,8 @@ template <typename T, bool UPPER>
 __global__ void __launch_bounds__(kSegThreads, 512 / kSegThreads) k_seg_numeric(CsrDev A, CsrDev B, PlanDev P,
                                                              const int *crpt, int *ccol, T *cval)
 {
+    if (P.cnt->abort)  // a capacity check of a captured pipeline failed
+        return;
     constexpr int NT = kSegThreads;
     using L = SegLayout<T>;
     extern __shared__ __align__(16) unsigned char smem[];
@@ -1129,6 +1135,8 @@ __device__ __forceinline__ bool long_by_thread(const LongCol &c, int last)
 template <typename T>
 __global__ void __launch_bounds__(128) k_long_reduce(PlanDev P, int *ccol, T *cval)
 {
+    if (P.cnt->abort)  // a capacity check of a captured pipeline failed
+        return;
     const unsigned long long used = P.cnt->long_used;
     const long long n = min((long long)(used >> 40), P.long_cap_cols);
     const T *__restrict__ lval = (const T *)P.long_val;
@@ -1155,6 +1163,8 @@ __global__ void __launch_bounds__(128) k_long_reduce(PlanDev P, int *ccol, T *cv
 template <typename T>
 __global__ void __launch_bounds__(128) k_long_warp(PlanDev P, int *ccol, T *cval)
 {
+    if (P.cnt->abort)  // a capacity check of a captured pipeline failed
+        return;
     __shared__ int s_cnt[4][32];
     __shared__ T s_val[4][32];
     const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;

@@ -362,6 +362,14 @@ class Context:
         be recomputed with one CUDA-graph launch (BatchGraph.launch)."""
         return BatchGraph(self, pairs)
 
+    def batch_pipe(self, pairs=None, headroom: float = 1.25, caps: dict | None = None,
+                   dtype=None) -> "BatchPipe":
+        """brm_batch_pipe_create: a batch pipeline captured once and run once
+        per new batch (BatchPipe.run).  Capacities from `caps` (a dict of
+        brm_batch_caps fields) or from a sample list of pairs scaled by
+        headroom."""
+        return BatchPipe(self, pairs, headroom, caps, dtype)
+
     def batch_precise(self, pairs) -> list:
         """brm_batch_precise: C_i = A_i * B_i for a list of (A_i, B_i)
         DeviceCSR pairs of one value type, in one pipeline.  Returns the C_i
@@ -497,6 +505,85 @@ class BatchGraph:
         if self._h:
             self.results = []
             self._L.brm_batch_graph_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class BatchPipe:
+    """A captured batch pipeline (brm_batch_pipe_*).  `run(pairs)` computes a
+    new batch with one graph launch and returns the C_i as DeviceCSR views of
+    the pipe's own arrays, valid until the next run or close."""
+
+    def __init__(self, ctx: "Context", pairs, headroom: float, caps: dict | None, dtype):
+        import torch
+        self._L = _native.lib()
+        self._h = C.c_void_p()
+        if caps is None:
+            n = len(pairs)
+            dt = pairs[0][0].val.dtype
+            self._code = _dtype_code(np.float64 if dt == torch.float64 else np.float32)
+            As = (_native.CsrC * n)(*[a.c() for a, _ in pairs])
+            Bs = (_native.CsrC * n)(*[b.c() for _, b in pairs])
+            cc = _native.BatchCapsC()
+            _native.check(self._L.brm_batch_caps_for(ctx._h, self._code, n, As, Bs,
+                                                     float(headroom), C.byref(cc)),
+                          "brm_batch_caps_for")
+        else:
+            self._code = _dtype_code(dtype or np.float64)
+            cc = _native.BatchCapsC(**caps)
+        _native.check(self._L.brm_batch_pipe_create(ctx._h, self._code, C.byref(cc),
+                                                    C.byref(self._h)), "brm_batch_pipe_create")
+
+    def caps(self) -> dict:
+        cc = _native.BatchCapsC()
+        _native.check(self._L.brm_batch_pipe_caps(self._h, C.byref(cc)), "brm_batch_pipe_caps")
+        return {f: getattr(cc, f) for f, _ in cc._fields_}
+
+    def run_raw(self, pairs, stream=None):
+        """(ccol, cval, row_off, nnz_off, rpt_local, nnz) of the batch, views
+        of the pipe's arrays (valid until the next run)."""
+        import torch
+        n = len(pairs)
+        dt = pairs[0][0].val.dtype
+        As = (_native.CsrC * n)(*[a.c() for a, _ in pairs])
+        Bs = (_native.CsrC * n)(*[b.c() for _, b in pairs])
+        ptr = None
+        if stream is not None:
+            ptr = stream.cuda_stream if hasattr(stream, "cuda_stream") else int(stream)
+        out = _native.BatchC()
+        _native.check(self._L.brm_batch_pipe_run(self._h, n, As, Bs, ptr, C.byref(out)),
+                      "brm_batch_pipe_run")
+        dev = pairs[0][0].rpt.device
+        vt = "<f8" if dt == torch.float64 else "<f4"
+
+        def view(p, m, ts, tdt):
+            if m == 0 or not p:
+                return torch.empty(m, dtype=tdt, device=dev)
+            return torch.as_tensor(_RawDevice(p, m, ts), device=dev)
+
+        ccol = view(out.ccol, out.nnz, "<i4", torch.int32)
+        cval = view(out.cval, out.nnz, vt, dt)
+        lrpt = view(out.rpt_local, out.rows + n, "<i4", torch.int32)
+        roff = np.ctypeslib.as_array(out.row_off, shape=(n + 1,)).copy()
+        noff = np.ctypeslib.as_array(out.nnz_off, shape=(n + 1,)).copy()
+        return ccol, cval, roff, noff, lrpt, int(out.nnz)
+
+    def run(self, pairs, stream=None) -> list:
+        ccol, cval, roff, noff, lrpt, _ = self.run_raw(pairs, stream)
+        res = []
+        for i, (a, b) in enumerate(pairs):
+            r0, r1, n0, n1 = int(roff[i]), int(roff[i + 1]), int(noff[i]), int(noff[i + 1])
+            res.append(DeviceCSR(a.M, b.N, lrpt[r0 + i:r1 + i + 1], ccol[n0:n1], cval[n0:n1]))
+        return res
+
+    def close(self):
+        if self._h:
+            self._L.brm_batch_pipe_destroy(self._h)
             self._h = C.c_void_p()
 
     def __del__(self):

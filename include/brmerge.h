@@ -268,6 +268,52 @@ int brm_batch_graph_create(brm_context ctx, brm_dtype dtype, int n, const brm_cs
 int brm_batch_graph_launch(brm_batch_graph graph, void *stream);
 int brm_batch_graph_destroy(brm_batch_graph graph);
 
+/* A batch pipeline: brm_batch_precise captured once as a CUDA graph with
+ * fixed capacities and launched once per NEW batch, whatever its structure
+ * (pairs, sizes, sparsity), as long as it fits the capacities.  Every buffer
+ * the batch needs is allocated at creation (the stacked operands padded to
+ * the capacities, C sized by the products, the planning's segment, split and
+ * scratch buffers), so a run allocates nothing and synchronises the host
+ * once: it uploads the batch's table, launches the graph and reads nnz(C),
+ * the per-pair offsets and the device error status.  The device compares each
+ * batch's products, heavy-row segments, split table and spill scratch with
+ * the capacities and stops the pipeline (BRM_ERR_CAPACITY) when one does not
+ * fit; so does the host for the pair count and the stacked sizes.  Each C_i
+ * is bit-identical to brm_precise_device(A_i, B_i).  No counterpart in the
+ * reference (one pair per call). */
+typedef struct brm_batch_caps {
+    int pairs;             /* pairs per batch */
+    long long rows;        /* sum of M_i (rows of all C_i) */
+    long long nnz_a;       /* sum of nnz(A_i) */
+    long long b_rows;      /* sum of K_i (rows of all B_i) */
+    long long nnz_b;       /* sum of nnz(B_i) */
+    int cols;              /* largest N_i */
+    long long products;    /* sum of intermediate products, <= INT_MAX (bounds nnz of all C_i) */
+    long long seg_slots;   /* heavy-row segment descriptors */
+    long long table;       /* split-table entries of the heavy rows */
+    long long spill_bytes; /* scratch of rows merged in global memory */
+} brm_batch_caps;
+
+/* Capacities for batches like the sample (n pairs): the sample is planned
+ * and multiplied once on ctx, and every count is scaled by headroom (>= 1). */
+int brm_batch_caps_for(brm_context ctx, brm_dtype dtype, int n, const brm_csr *A,
+                       const brm_csr *B, double headroom, brm_batch_caps *caps);
+
+typedef struct brm_batch_pipe_s *brm_batch_pipe;
+/* Allocates the buffers and captures the graph (in a private context that
+ * copies ctx's tuning); all pairs of its batches have the value type dtype. */
+int brm_batch_pipe_create(brm_context ctx, brm_dtype dtype, const brm_batch_caps *caps,
+                          brm_batch_pipe *pipe);
+int brm_batch_pipe_caps(brm_batch_pipe pipe, brm_batch_caps *caps);
+/* Runs one batch of n pairs on `stream` (cudaStream_t as void*, NULL = the
+ * legacy default stream) and waits for it.  *out describes C like
+ * brm_batch_precise, but every array (device and host) belongs to the pipe
+ * and stays valid until its next run or its destruction: do not pass it to
+ * brm_batch_free.  One run at a time per pipe. */
+int brm_batch_pipe_run(brm_batch_pipe pipe, int n, const brm_csr *A, const brm_csr *B,
+                       void *stream, brm_batch *out);
+int brm_batch_pipe_destroy(brm_batch_pipe pipe);
+
 /* ---- serving: a request loop over batches ---------------------------------- */
 
 /* A server takes C = A * B requests (Precise, device CSR) from any thread.
