@@ -713,19 +713,13 @@ def batched_section(ctx, dev, stream, steps: int, dtype=np.float64, tune: bool =
     return res
 
 
-def served_section(dev, rate: float, nreq: int, seed: int = 11):
-    """Poisson request stream into brm_server (continuous batching under a
-    60 GiB cap): 70% uneven-batch sizes, 25% R-MAT n=2^16 degree 8, 5% R-MAT
-    n=2^20 degree 16; float64 and float32 mixed.  Latency = submit -> result
-    ready; the isolated latency of each class is one call on an idle GPU.
-    Every served result is checked against the same pair's isolated
-    brm_precise_device result through on-device digests (dev_digest),
-    compared after the stream so that the checks never stall the submitter
-    or hold results."""
-    import queue as q
+def served_pools(dev, seed: int = 11):
+    """Request pools of the served stream (70% uneven-batch sizes, 25% R-MAT
+    n=2^16 degree 8, 5% R-MAT n=2^20 degree 16; float64 and float32), the
+    isolated latency of each class (one call on an idle GPU) and the digest
+    of every pool entry's isolated result."""
     import torch
     import brmerge_gb300 as brm
-    rng = np.random.default_rng(seed)
     up = lambda X: brm.DeviceCSR.from_host(X, dev)
     small = [(up(A), up(B)) for A, B in make_batch(64, seed=seed)]
     small32 = [(up(A.astype(np.float32)), up(B.astype(np.float32)))
@@ -738,11 +732,8 @@ def served_section(dev, rate: float, nreq: int, seed: int = 11):
     r20_32 = [(up(big.astype(np.float32)),) * 2]
     del big
     classes = {"batch_size": (small, small32), "rmat16": (r16, r16_32), "rmat20": (r20, r20_32)}
-    prob = [("batch_size", 0.70), ("rmat16", 0.25), ("rmat20", 0.05)]
-    flops = {}
+    flops, iso, alone = {}, {}, {}
     ctx = brm.Context()
-    iso = {}
-    alone = {}  # (class, f32, index) -> digest of the isolated result
     for name, pools in classes.items():
         _, bound = ctx.upper_bound(*pools[0][0])
         if bound > (60 << 30):
@@ -762,7 +753,7 @@ def served_section(dev, rate: float, nreq: int, seed: int = 11):
             iso[name] = f"rejected: upper bound {bound / 2**30:.0f} GiB > 60 GiB cap"
             continue
         ts = []
-        for _ in range(3):
+        for _ in range(5):
             torch.cuda.synchronize(dev)
             t0 = time.perf_counter()
             try:
@@ -776,12 +767,28 @@ def served_section(dev, rate: float, nreq: int, seed: int = 11):
         if name not in iso:
             iso[name] = round(statistics.median(ts) * 1e3, 3)
     ctx.close()
-    # the stream
+    return SimpleNamespace(classes=classes, flops=flops, iso=iso, alone=alone)
+
+
+def served_run(dev, pools, rate: float, nreq: int, seed: int = 11, workers: int = 2,
+               express: int = 1):
+    """A Poisson request stream at `rate` into brm_server (continuous
+    batching under a 60 GiB cap, `workers` general and `express` small-request
+    workers).  Latency = submit -> result ready.  Every served result is
+    checked against the same pair's isolated brm_precise_device result
+    through on-device digests (dev_digest), compared after the stream so that
+    the checks never stall the submitter or hold results."""
+    import queue as q
+    import torch
+    import brmerge_gb300 as brm
+    rng = np.random.default_rng(seed)
+    classes, flops, iso, alone = pools.classes, pools.flops, pools.iso, pools.alone
+    prob = [("batch_size", 0.70), ("rmat16", 0.25), ("rmat20", 0.05)]
     names = [p[0] for p in prob]
     kinds = rng.choice(len(names), size=nreq, p=[p[1] for p in prob])
     f32 = rng.random(nreq) < 0.5
     arrivals = np.cumsum(rng.exponential(1.0 / rate, nreq))
-    srv = brm.Server(mem_cap_bytes=60 << 30, workers=2)
+    srv = brm.Server(mem_cap_bytes=60 << 30, workers=workers, express_workers=express)
     tickets = q.Queue()
     rejected = {n: 0 for n in names}
     t_start = time.perf_counter()
@@ -795,10 +802,7 @@ def served_section(dev, rate: float, nreq: int, seed: int = 11):
             pool = classes[name][1 if f32[i] else 0]
             j = int(rng.integers(len(pool)))
             a, b = pool[j]
-            try:
-                tickets.put((i, name, (name, int(f32[i]), j), srv.submit(a, b)))
-            except brm.BrmError:
-                rejected[name] += 1
+            tickets.put((i, name, (name, int(f32[i]), j), srv.submit(a, b)))
         tickets.put(None)
 
     lat = {n: [] for n in names}
@@ -813,7 +817,11 @@ def served_section(dev, rate: float, nreq: int, seed: int = 11):
         if item is None:
             break
         i, name, key, t = item
-        C, st = srv.wait(t, timeout=600.0)
+        try:
+            C, st = srv.wait(t, timeout=600.0)
+        except brm.BrmError:  # refused at admission (bound above the cap)
+            rejected[name] += 1
+            continue
         digests.append((key, dev_digest(C)))
         ev = torch.cuda.Event()
         ev.record()
@@ -835,16 +843,32 @@ def served_section(dev, rate: float, nreq: int, seed: int = 11):
     pct = lambda v, p: round(float(np.percentile(v, p)), 3) if v else None
     per_class = {n: {"n": len(v), "p50_ms": pct(v, 50), "p99_ms": pct(v, 99),
                      "isolated_ms": iso[n], "rejected": rejected[n]} for n, v in lat.items()}
+    for n, c in per_class.items():
+        if c["p99_ms"] is not None and isinstance(c["isolated_ms"], float):
+            c["p99_over_isolated"] = round(c["p99_ms"] / c["isolated_ms"], 2)
     return {
         "offered_rate_per_s": rate, "requests": nreq, "completed": len(allv),
         "wall_s": round(wall, 3), "throughput_req_per_s": round(len(allv) / wall, 1),
         "gflops": round(done_flop / wall / 1e9, 3),
         "p50_ms": pct(allv, 50), "p99_ms": pct(allv, 99),
         "mean_batch": round(float(np.mean(batch_sizes)), 2) if batch_sizes else None,
-        "classes": per_class, "mem_cap_gib": 60, "workers": 2,
+        "classes": per_class, "mem_cap_gib": 60, "workers": workers, "express_workers": express,
         "verified": mismatches == 0,
         "checks": {"served_results_vs_isolated_call_mismatches": mismatches},
     }
+
+
+def served_section(dev, nreq: int, rates=(2000.0, 1000.0, 600.0, 400.0, 250.0, 150.0)):
+    """The served stream at several offered rates, and the largest rate at
+    which the small class (uneven-batch sizes) keeps p99 within 2x its
+    isolated latency."""
+    pools = served_pools(dev)
+    runs = [served_run(dev, pools, r, nreq) for r in rates]
+    ok = [r["offered_rate_per_s"] for r in runs
+          if r["classes"]["batch_size"].get("p99_over_isolated", 1e9) <= 2.0]
+    return {"runs": runs,
+            "small_class_max_rate_p99_within_2x_isolated": max(ok) if ok else None,
+            "verified": all(r["verified"] for r in runs)}
 
 
 def run_ours(args):
@@ -960,8 +984,7 @@ def run_ours(args):
         side["batched_f32"] = batched_section(ctx, dev, stream, steps=max(1, min(args.steps, 3)),
                                               dtype=np.float32, tune=False)
     if "served" in sections:
-        side["served"] = [served_section(dev, rate, args.serve_requests)
-                          for rate in (2000.0, 400.0, 150.0)]
+        side["served"] = served_section(dev, args.serve_requests)
     if rank != 0:
         return
     # the oracle on the host cores: the check of the headline result and,

@@ -59,7 +59,8 @@ class BatchCapsC(C.Structure):
 
 class ServerConfigC(C.Structure):
     """Mirror of brm_server_config."""
-    _fields_ = [("mem_cap_bytes", C.c_longlong), ("max_batch", C.c_int), ("workers", C.c_int)]
+    _fields_ = [("mem_cap_bytes", C.c_longlong), ("max_batch", C.c_int), ("workers", C.c_int),
+                ("express_workers", C.c_int), ("express_bytes", C.c_longlong)]
 
 
 class ServerResultC(C.Structure):

@@ -868,6 +868,24 @@ int brm::device_status(int err) { return device_err_status(err); }
 
 const brm::Counters *brm::context_counters(brm_context ctx) { return ctx->plan.cnt; }
 
+int brm::set_context_priority(brm_context ctx, int priority)
+{
+    cudaStream_t s = nullptr;
+    BRM_CK(cudaStreamCreateWithPriority(&s, cudaStreamNonBlocking, priority));
+    if (ctx->fork.aux) {
+        cudaStreamSynchronize(ctx->fork.aux);
+        cudaStreamDestroy(ctx->fork.aux);
+    }
+    ctx->fork.aux = s;
+    return BRM_SUCCESS;
+}
+
+long long brm::upper_bound_bytes(brm_dtype dtype, int M, long long products)
+{
+    const long long s = (long long)vsize(dtype);
+    return 2 * products * (4 + s) + 4LL * ((long long)M + 1) + (long long)workspace_bytes(M);
+}
+
 brm::Counters brm::last_plan_counters(brm_context ctx) { return *ctx->h_cnt; }
 
 int brm::reserve_pipe(brm_context ctx, brm_dtype dtype, const brm::PipeCaps &c)
@@ -1436,8 +1454,7 @@ int brm_upper_bound(brm_context ctx, brm_dtype dtype, const brm_csr *A, const br
     BRM_TRY(brm_compute_flop(ctx, A, B, &f));
     if (products)
         *products = f;
-    const long long s = (long long)vsize(dtype);
-    *bytes = 2 * f * (4 + s) + 4LL * ((long long)A->M + 1) + (long long)workspace_bytes(A->M);
+    *bytes = brm::upper_bound_bytes(dtype, A->M, f);
     return BRM_SUCCESS;
 }
 

@@ -41,6 +41,12 @@ int precise_pipe(brm_context ctx, brm_dtype dtype, const brm_csr *A, const brm_c
 const Counters *context_counters(brm_context ctx);
 // The counters the last planning left on the host (after a synchronised call).
 Counters last_plan_counters(brm_context ctx);
+// Gives the context's internal second stream the CUDA stream priority
+// `priority` (the caller sets the main stream with brm_set_stream), and the
+// device bytes an Upper call on an M-row A with `products` products needs at
+// most (brm_upper_bound's estimate).
+int set_context_priority(brm_context ctx, int priority);
+long long upper_bound_bytes(brm_dtype dtype, int M, long long products);
 // Device-side capacity check of a captured pipeline: stage 0 after the row
 // analysis and the mid-row prefix sums, stage 1 after the symbolic phase.
 void launch_pipe_admit(const PlanDev &P, int M, const PipeCaps &caps, int stage, cudaStream_t s);

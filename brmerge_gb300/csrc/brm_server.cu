@@ -1,19 +1,25 @@
 // brm_server.cu -- a request loop for many independent SpGEMM requests.
 //
 // Callers submit C = A * B requests (device CSR, Precise) from any thread and
-// wait for them by ticket.  Worker threads, each with its own context and
-// non-blocking stream, take whatever is queued (same value type, in arrival
-// order), admit requests while the summed upper-bound bytes of everything
-// admitted and not yet released stay under the memory cap, and run them as
-// one batch (brm_batch_precise: one stacked-operand pipeline).  Requests that
-// arrive while batches are on the GPU wait for the next free worker, so the
-// batches of different workers overlap on the device.  A result stays in
-// the batch's device arrays until the caller releases it; the batch's memory
-// goes back when its last result is released.
+// wait for them by ticket.  A submit only queues the request.  An admission
+// thread takes every newly queued request at once, counts their products
+// with one kernel on a high-priority stream (no per-request synchronisation,
+// no shared context), turns them into upper-bound bytes, rejects those whose
+// bound alone exceeds the memory cap and passes the others on.  Worker
+// threads, each with its own context and non-blocking stream, take whatever
+// is admitted (same value type, in arrival order, bounds within kSizeRatio of
+// the oldest one's), reserve the summed bounds under the cap, and run them as
+// one batch (brm_batch_precise: one stacked-operand pipeline).  Express
+// workers take only small requests (bound up to express_bytes) and run them
+// on the device's highest-priority streams, so small batches are scheduled
+// ahead of the pending blocks of large ones.  A result stays in the batch's
+// device arrays until the caller releases it; the batch's memory goes back
+// when its last result is released.
 //
 // No counterpart in the reference (a library call per product).
 #include <algorithm>
 #include <chrono>
+#include <climits>
 #include <condition_variable>
 #include <cstring>
 #include <deque>
@@ -25,11 +31,15 @@
 
 #include <cuda_runtime.h>
 
+#include "brm_common.cuh"
+#include "brm_kernels.h"
 #include "brmerge.h"
 
 namespace {
 
 constexpr long long kSizeRatio = 16;  // largest bound ratio within one batch
+constexpr int kAdmitThreads = 256;
+constexpr int kAdmitChunk = kAdmitThreads * 8;  // A entries a block counts
 
 double now_s()
 {
@@ -68,15 +78,72 @@ struct Request {
     int batch_size = 0;
 };
 
+// One request of an admission round: its A columns and B row pointers.
+struct AdmitItem {
+    const int *acol;
+    const int *brpt;
+    int nnz_a;
+    int K;
+};
+
+// Products of every request of a round (compute_flop, spgemm.h:31-56):
+// blockIdx.y is the request, blockIdx.x a chunk of its A entries.  out[2i]
+// collects the products, out[2i+1] a flag for a column or a B row pointer
+// that is not valid CSR.
+__global__ void __launch_bounds__(kAdmitThreads) k_admit_count(const AdmitItem *items,
+                                                              unsigned long long *out)
+{
+    const AdmitItem it = items[blockIdx.y];
+    const long long j0 = (long long)blockIdx.x * kAdmitChunk;
+    if (j0 >= it.nnz_a)
+        return;
+    const int j1 = (int)(j0 + kAdmitChunk < it.nnz_a ? j0 + kAdmitChunk : it.nnz_a);
+    unsigned long long f = 0;
+    bool bad = false;
+    for (int j = (int)j0 + threadIdx.x; j < j1; j += kAdmitThreads) {
+        const int c = it.acol[j];
+        if ((unsigned)c < (unsigned)it.K) {
+            const int b0 = it.brpt[c], b1 = it.brpt[c + 1];
+            if (b0 < 0 || b1 < b0)
+                bad = true;
+            else
+                f += (unsigned long long)(b1 - b0);
+        } else {
+            bad = true;
+        }
+    }
+    __shared__ unsigned long long s_f[kAdmitThreads / 32];
+    __shared__ int s_bad;
+    if (threadIdx.x == 0)
+        s_bad = 0;
+    f = brm::warp_sum(f);
+    if ((threadIdx.x & 31) == 0)
+        s_f[threadIdx.x >> 5] = f;
+    __syncthreads();
+    if (bad)
+        s_bad = 1;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned long long t = 0;
+        for (int w = 0; w < kAdmitThreads / 32; w++)
+            t += s_f[w];
+        atomicAdd(&out[2 * blockIdx.y], t);
+        if (s_bad)
+            atomicOr(&out[2 * blockIdx.y + 1], 1ull);
+    }
+}
+
 }  // namespace
 
 struct brm_server_s {
     int device = 0;
     long long cap = 0;
     int max_batch = 0;
+    long long express_bytes = 0;
     std::mutex mu;
-    std::condition_variable cv_work, cv_done;
-    std::deque<Request *> queue;
+    std::condition_variable cv_work, cv_done, cv_admit;
+    std::deque<Request *> pending;  // submitted, bound not yet known
+    std::deque<Request *> queue;    // admitted to the work queue
     std::unordered_map<long long, Request *> all;
     long long next_ticket = 1;
     long long reserved = 0;  // bytes of admitted, unreleased requests
@@ -84,37 +151,151 @@ struct brm_server_s {
     std::vector<std::thread> workers;
     std::vector<brm_context> ctxs;
     std::vector<cudaStream_t> streams;
-    brm_context admit_ctx = nullptr;  // upper-bound estimates at submit
-    std::mutex admit_mu;
+    std::vector<char> express;  // per worker: takes only small requests
+    std::thread admitter;
+    cudaStream_t admit_stream = nullptr;
 
     void work(int w);
+    void admit();
+    void finish(Request *r, int status);
 };
+
+// Marks a request done without running it (rejected at admission); mu held.
+void brm_server_s::finish(Request *r, int status)
+{
+    r->status = status;
+    r->t_start = r->t_done = now_s();
+    r->done = true;
+}
+
+void brm_server_s::admit()
+{
+    cudaSetDevice(device);
+    AdmitItem *d_items = nullptr, *h_items = nullptr;
+    unsigned long long *d_out = nullptr, *h_out = nullptr;
+    int cap_items = 0;
+    for (;;) {
+        std::vector<Request *> round;
+        {
+            std::unique_lock<std::mutex> lk(mu);
+            cv_admit.wait(lk, [&] { return stop || !pending.empty(); });
+            if (pending.empty() && stop)
+                break;
+            while (!pending.empty() && round.size() < 65535) {
+                round.push_back(pending.front());
+                pending.pop_front();
+            }
+        }
+        const int n = (int)round.size();
+        int st = BRM_SUCCESS;
+        if (n > cap_items) {
+            cudaFree(d_items);
+            cudaFreeHost(h_items);
+            cudaFree(d_out);
+            cudaFreeHost(h_out);
+            d_items = h_items = nullptr;
+            d_out = h_out = nullptr;
+            cap_items = std::max(n, 256);
+            if (cudaMalloc(&d_items, sizeof(AdmitItem) * cap_items) != cudaSuccess ||
+                cudaMallocHost(&h_items, sizeof(AdmitItem) * cap_items) != cudaSuccess ||
+                cudaMalloc(&d_out, 16 * (size_t)cap_items) != cudaSuccess ||
+                cudaMallocHost(&h_out, 16 * (size_t)cap_items) != cudaSuccess) {
+                (void)cudaGetLastError();
+                cap_items = 0;
+                st = BRM_ERR_ALLOC;
+            }
+        }
+        int max_nnz = 0;
+        if (st == BRM_SUCCESS) {
+            for (int i = 0; i < n; i++) {
+                const Request *r = round[(size_t)i];
+                h_items[i] = AdmitItem{r->A.col, r->B.rpt, r->A.nnz, r->B.M};
+                max_nnz = std::max(max_nnz, r->A.nnz);
+            }
+            const dim3 grid((unsigned)std::max(1, (max_nnz + kAdmitChunk - 1) / kAdmitChunk),
+                            (unsigned)n);
+            cudaError_t e = cudaMemcpyAsync(d_items, h_items, sizeof(AdmitItem) * (size_t)n,
+                                            cudaMemcpyHostToDevice, admit_stream);
+            if (e == cudaSuccess)
+                e = cudaMemsetAsync(d_out, 0, 16 * (size_t)n, admit_stream);
+            if (e == cudaSuccess) {
+                k_admit_count<<<grid, kAdmitThreads, 0, admit_stream>>>(d_items, d_out);
+                e = cudaGetLastError();
+            }
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync(h_out, d_out, 16 * (size_t)n, cudaMemcpyDeviceToHost,
+                                    admit_stream);
+            if (e == cudaSuccess)
+                e = cudaStreamSynchronize(admit_stream);
+            if (e != cudaSuccess) {
+                (void)cudaGetLastError();
+                st = BRM_ERR_CUDA;
+            }
+        }
+        {
+            std::lock_guard<std::mutex> lk(mu);
+            for (int i = 0; i < n; i++) {
+                Request *r = round[(size_t)i];
+                if (st != BRM_SUCCESS) {
+                    finish(r, st);
+                    continue;
+                }
+                if (h_out[2 * i + 1]) {
+                    finish(r, BRM_ERR_INVALID_CSR);
+                    continue;
+                }
+                const long long prod = (long long)h_out[2 * i];
+                const long long vb = r->dtype == BRM_F64 ? 8 : 4;
+                // the Upper bound of C plus the operands' stacked copies
+                r->bound = brm::upper_bound_bytes(r->dtype, r->A.M, prod) +
+                           2 * ((long long)r->A.nnz * (4 + vb) + (long long)r->B.nnz * (4 + vb) +
+                                4ll * ((long long)r->A.M + r->B.M + 2));
+                if (r->bound > cap)
+                    finish(r, BRM_ERR_CAPACITY);
+                else
+                    queue.push_back(r);
+            }
+        }
+        cv_work.notify_all();
+        cv_done.notify_all();
+    }
+    cudaFree(d_items);
+    cudaFreeHost(h_items);
+    cudaFree(d_out);
+    cudaFreeHost(h_out);
+}
 
 void brm_server_s::work(int w)
 {
     cudaSetDevice(device);
     brm_context ctx = ctxs[(size_t)w];
+    const bool small_only = express[(size_t)w] != 0;
     for (;;) {
         std::vector<Request *> batch;
         {
             std::unique_lock<std::mutex> lk(mu);
             for (;;) {
-                if (stop && queue.empty())
+                if (stop && queue.empty() && pending.empty())
                     return;
-                if (!queue.empty()) {
-                    // first fit in arrival order: the head's value type, while
-                    // the admitted bytes stay under the cap (the head is always
-                    // admitted when nothing else is in flight)
-                    // requests whose bounds differ from the head's by more
-                    // than kSizeRatio wait for a batch of their own size, so a
-                    // small request does not wait for a large one's batch
-                    const brm_dtype dt = queue.front()->dtype;
-                    const long long hb = std::max(queue.front()->bound, 1LL);
-                    for (auto it = queue.begin();
-                         it != queue.end() && (int)batch.size() < max_batch;) {
+                // first fit in arrival order: the head's value type, while
+                // the admitted bytes stay under the cap (the head is always
+                // admitted when nothing else is in flight); requests whose
+                // bounds differ from the head's by more than kSizeRatio wait
+                // for a batch of their own size, so a small request does not
+                // wait for a large one's batch.  An express worker's head is
+                // the oldest small request.
+                auto head = queue.begin();
+                if (small_only)
+                    while (head != queue.end() && (*head)->bound > express_bytes)
+                        ++head;
+                if (head != queue.end()) {
+                    const brm_dtype dt = (*head)->dtype;
+                    const long long hb = std::max((*head)->bound, 1LL);
+                    for (auto it = head; it != queue.end() && (int)batch.size() < max_batch;) {
                         Request *r = *it;
                         const long long rb = std::max(r->bound, 1LL);
-                        if (r->dtype != dt || rb > hb * kSizeRatio || rb * kSizeRatio < hb) {
+                        if (r->dtype != dt || rb > hb * kSizeRatio || rb * kSizeRatio < hb ||
+                            (small_only && r->bound > express_bytes)) {
                             ++it;
                             continue;
                         }
@@ -173,35 +354,47 @@ int brm_server_create(const brm_server_config *cfg, brm_server *out)
     srv->cap = (cfg && cfg->mem_cap_bytes > 0) ? cfg->mem_cap_bytes : (60ll << 30);
     srv->max_batch = (cfg && cfg->max_batch > 0) ? cfg->max_batch : 4096;
     const int nw = (cfg && cfg->workers > 0) ? std::min(cfg->workers, 16) : 2;
+    const int nx = cfg ? (cfg->express_workers < 0 ? 0 : std::min(cfg->express_workers, 16)) : 1;
+    srv->express_bytes = (cfg && cfg->express_bytes > 0) ? cfg->express_bytes : (64ll << 20);
     cudaGetDevice(&srv->device);
-    int st = brm_create(&srv->admit_ctx);
-    for (int w = 0; w < nw && st == BRM_SUCCESS; w++) {
+    int lo = 0, hi = 0;  // stream priorities: hi is the most urgent (numerically lowest)
+    int st = cudaDeviceGetStreamPriorityRange(&lo, &hi) == cudaSuccess ? BRM_SUCCESS : BRM_ERR_CUDA;
+    if (st == BRM_SUCCESS &&
+        cudaStreamCreateWithPriority(&srv->admit_stream, cudaStreamNonBlocking, hi) != cudaSuccess)
+        st = BRM_ERR_CUDA;
+    for (int w = 0; w < nw + nx && st == BRM_SUCCESS; w++) {
+        const bool xw = w >= nw;
         brm_context c = nullptr;
         cudaStream_t s = nullptr;
         st = brm_create(&c);
         if (st != BRM_SUCCESS)
             break;
-        if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess) {
+        if (cudaStreamCreateWithPriority(&s, cudaStreamNonBlocking, xw ? hi : lo) != cudaSuccess) {
             (void)cudaGetLastError();
             brm_destroy(c);
             st = BRM_ERR_CUDA;
             break;
         }
         brm_set_stream(c, s);
+        if (xw)
+            st = brm::set_context_priority(c, hi);
         srv->ctxs.push_back(c);
         srv->streams.push_back(s);
+        srv->express.push_back(xw ? 1 : 0);
     }
     if (st != BRM_SUCCESS) {
+        (void)cudaGetLastError();
         for (brm_context c : srv->ctxs)
             brm_destroy(c);
         for (cudaStream_t s : srv->streams)
             cudaStreamDestroy(s);
-        if (srv->admit_ctx)
-            brm_destroy(srv->admit_ctx);
+        if (srv->admit_stream)
+            cudaStreamDestroy(srv->admit_stream);
         delete srv;
         return st;
     }
-    for (int w = 0; w < nw; w++)
+    srv->admitter = std::thread([srv] { srv->admit(); });
+    for (int w = 0; w < nw + nx; w++)
         srv->workers.emplace_back([srv, w] { srv->work(w); });
     *out = srv;
     return BRM_SUCCESS;
@@ -212,7 +405,8 @@ int brm_server_submit(brm_server srv, brm_dtype dtype, const brm_csr *A, const b
 {
     if (!srv || !A || !B || !ticket || (dtype != BRM_F64 && dtype != BRM_F32))
         return BRM_ERR_INVALID_VALUE;
-    if (A->N != B->M || A->M < 0 || B->N < 0)
+    if (A->N != B->M || A->M < 0 || B->M < 0 || B->N < 0 || A->nnz < 0 || B->nnz < 0 ||
+        !A->rpt || !B->rpt || (A->nnz > 0 && !A->col))
         return BRM_ERR_INVALID_VALUE;
     auto *r = new (std::nothrow) Request();
     if (!r)
@@ -222,23 +416,6 @@ int brm_server_submit(brm_server srv, brm_dtype dtype, const brm_csr *A, const b
     r->A = *A;
     r->B = *B;
     {
-        // admission estimate: the Upper bound of C plus the operands' copies
-        std::lock_guard<std::mutex> g(srv->admit_mu);
-        long long prod = 0, bytes = 0;
-        const int st = brm_upper_bound(srv->admit_ctx, dtype, A, B, &prod, &bytes);
-        if (st != BRM_SUCCESS) {
-            delete r;
-            return st;
-        }
-        const long long vb = dtype == BRM_F64 ? 8 : 4;
-        r->bound = bytes + 2 * ((long long)A->nnz * (4 + vb) + (long long)B->nnz * (4 + vb) +
-                                4ll * ((long long)A->M + B->M + 2));
-    }
-    if (r->bound > srv->cap) {
-        delete r;
-        return BRM_ERR_CAPACITY;
-    }
-    {
         std::lock_guard<std::mutex> lk(srv->mu);
         if (srv->stop) {
             delete r;
@@ -246,10 +423,10 @@ int brm_server_submit(brm_server srv, brm_dtype dtype, const brm_csr *A, const b
         }
         r->ticket = srv->next_ticket++;
         srv->all[r->ticket] = r;
-        srv->queue.push_back(r);
+        srv->pending.push_back(r);
         *ticket = r->ticket;
     }
-    srv->cv_work.notify_one();
+    srv->cv_admit.notify_one();
     return BRM_SUCCESS;
 }
 
@@ -314,6 +491,8 @@ int brm_server_destroy(brm_server srv)
         std::lock_guard<std::mutex> lk(srv->mu);
         srv->stop = true;
     }
+    srv->cv_admit.notify_all();
+    srv->admitter.join();  // every pending request is admitted or rejected
     srv->cv_work.notify_all();
     for (auto &t : srv->workers)
         t.join();
@@ -324,7 +503,7 @@ int brm_server_destroy(brm_server srv)
         brm_destroy(c);
     for (cudaStream_t s : srv->streams)
         cudaStreamDestroy(s);
-    brm_destroy(srv->admit_ctx);
+    cudaStreamDestroy(srv->admit_stream);
     delete srv;
     return BRM_SUCCESS;
 }

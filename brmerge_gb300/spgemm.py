@@ -610,13 +610,18 @@ class _ServerBlock(_RawDevice):
 
 
 class Server:
-    """brm_server: C = A * B requests from any thread, batched by worker
-    threads under a memory cap (one stacked-operand pipeline per batch)."""
+    """brm_server: C = A * B requests from any thread, admitted in rounds on
+    the device and batched by worker threads under a memory cap (one
+    stacked-operand pipeline per batch); express workers take the small
+    requests on high-priority streams.  A rejected request raises from
+    wait()."""
 
-    def __init__(self, mem_cap_bytes: int = 0, max_batch: int = 0, workers: int = 0):
+    def __init__(self, mem_cap_bytes: int = 0, max_batch: int = 0, workers: int = 0,
+                 express_workers: int = 1, express_bytes: int = 0):
         self._L = _native.lib()
         self._h = C.c_void_p()
-        cfg = _native.ServerConfigC(mem_cap_bytes, max_batch, workers)
+        cfg = _native.ServerConfigC(mem_cap_bytes, max_batch, workers,
+                                    express_workers if express_workers > 0 else -1, express_bytes)
         _native.check(self._L.brm_server_create(C.byref(cfg), C.byref(self._h)),
                       "brm_server_create")
         self._inputs = {}  # ticket -> (A, B): kept alive until the result is waited for

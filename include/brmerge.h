@@ -317,22 +317,31 @@ int brm_batch_pipe_destroy(brm_batch_pipe pipe);
 /* ---- serving: a request loop over batches ---------------------------------- */
 
 /* A server takes C = A * B requests (Precise, device CSR) from any thread.
- * Worker threads, each with its own context and stream, take whatever is
- * queued (one value type per batch, arrival order, bounds within 16x of the
- * oldest queued request's, so small requests do not wait behind large
- * ones), admit requests while the
- * summed upper-bound bytes (brm_upper_bound plus the operands' copies) of
- * everything admitted and not yet released stay under mem_cap_bytes, and run
- * them as one brm_batch_precise.  Requests that arrive while batches run wait
- * for the next free worker; the batches of different workers overlap on the
- * device.  Every result is bit-identical to brm_precise_device on its pair.
- * No counterpart in the reference (one library call per product). */
+ * A submit only queues the request.  An admission thread takes all newly
+ * queued requests at once, counts their products with one kernel on a
+ * high-priority stream, and rejects a request whose upper-bound bytes
+ * (brm_upper_bound plus the operands' copies) alone exceed mem_cap_bytes
+ * (its wait returns BRM_ERR_CAPACITY; BRM_ERR_INVALID_CSR for a column or a
+ * B row pointer that is not valid CSR).  Worker threads, each with its own
+ * context and stream, take whatever is admitted (one value type per batch,
+ * arrival order, bounds within 16x of the oldest one's, so small requests do
+ * not wait behind large ones), reserve the summed bounds while they stay
+ * under the cap, and run them as one brm_batch_precise; requests that arrive
+ * while batches run wait for the next free worker, and the batches of
+ * different workers overlap on the device.  Express workers take only
+ * requests whose bound is at most express_bytes and run on the device's
+ * highest-priority streams, so small batches are scheduled ahead of the
+ * pending blocks of large ones.  A request completes when its batch does.
+ * Every result is bit-identical to brm_precise_device on its pair.  No
+ * counterpart in the reference (one library call per product). */
 typedef struct brm_server_s *brm_server;
 
 typedef struct brm_server_config {
-    long long mem_cap_bytes; /* <= 0: 60 GiB */
-    int max_batch;           /* requests per batch, <= 0: 4096 */
-    int workers;             /* concurrent batches, <= 0: 2 (at most 16) */
+    long long mem_cap_bytes;  /* <= 0: 60 GiB */
+    int max_batch;            /* requests per batch, <= 0: 4096 */
+    int workers;              /* concurrent batches of any size, <= 0: 2 (at most 16) */
+    int express_workers;      /* small-request workers, < 0: none (NULL cfg: 1; at most 16) */
+    long long express_bytes;  /* largest bound an express worker takes, <= 0: 64 MiB */
 } brm_server_config;
 
 typedef struct brm_server_result {
@@ -348,8 +357,8 @@ typedef struct brm_server_result {
 
 /* On the current device; cfg may be NULL. */
 int brm_server_create(const brm_server_config *cfg, brm_server *srv);
-/* A and B must stay valid until the request is done.  Rejects a request
- * whose bound alone exceeds the cap with BRM_ERR_CAPACITY. */
+/* A and B must stay valid until the request is done.  Returns at once;
+ * admission (and a BRM_ERR_CAPACITY rejection) follows asynchronously. */
 int brm_server_submit(brm_server srv, brm_dtype dtype, const brm_csr *A, const brm_csr *B,
                       long long *ticket);
 /* Waits up to timeout_s (< 0: forever; BRM_ERR_TIMEOUT when not done) and

@@ -89,8 +89,63 @@ def test_server_admission_under_small_cap():
 
 
 def test_server_rejects_request_above_cap():
+    """Admission is asynchronous: the submit returns, the wait reports
+    BRM_ERR_CAPACITY, and a request that fits still runs afterwards."""
     A = brm.DeviceCSR.from_host(brm.gen_rmat(12, 8 * 4096, seed=5))
+    small = brm.gen_er(256, 4, seed=6)
+    S = brm.DeviceCSR.from_host(small)
     srv = brm.Server(mem_cap_bytes=1 << 20, workers=1)
-    with pytest.raises(brm.BrmError):
-        srv.submit(A, A)
+    t = srv.submit(A, A)
+    with pytest.raises(brm.BrmError) as e:
+        srv.wait(t, timeout=60.0)
+    assert e.value.status == 10  # BRM_ERR_CAPACITY
+    C, _ = srv.wait(srv.submit(S, S), timeout=60.0)
+    ctx = brm.Context()
+    assert_same_csr(C.to_host(), ctx.precise_device(S, S).to_host(), "after a rejection")
+    del C
     srv.close()
+    ctx.close()
+
+
+def test_server_rejects_invalid_columns_at_admission():
+    """A column of A outside B's rows is found by the admission kernel (it
+    checks every column before it reads B's row pointers): the request fails
+    with BRM_ERR_INVALID_CSR and the server keeps serving."""
+    import torch
+    B = brm.gen_er(64, 4, seed=7)
+    dB = brm.DeviceCSR.from_host(B)
+    rpt = torch.tensor([0, 2, 3], dtype=torch.int32, device="cuda")
+    col = torch.tensor([1, 64, 5], dtype=torch.int32, device="cuda")  # 64 >= K = 64
+    val = torch.ones(3, dtype=torch.float64, device="cuda")
+    bad = brm.DeviceCSR(2, 64, rpt, col, val)
+    srv = brm.Server(workers=1, express_workers=1)
+    t = srv.submit(bad, dB)
+    with pytest.raises(brm.BrmError) as e:
+        srv.wait(t, timeout=60.0)
+    assert e.value.status == 2  # BRM_ERR_INVALID_CSR
+    C, _ = srv.wait(srv.submit(dB, dB), timeout=60.0)
+    ctx = brm.Context()
+    assert_same_csr(C.to_host(), ctx.precise_device(dB, dB).to_host(), "after invalid input")
+    del C
+    srv.close()
+    ctx.close()
+
+
+@pytest.mark.parametrize("express", [0, 2])
+def test_server_express_workers_same_results(oracle_mod, express):
+    """With no express workers, or with two beside one general worker, every
+    result is the same as alone; small and large requests are mixed."""
+    import torch
+    reqs = _requests(31, 24)
+    dev = [(brm.DeviceCSR.from_host(A), brm.DeviceCSR.from_host(B)) for A, B in reqs]
+    ctx = brm.Context()
+    alone = [ctx.precise_device(a, b).to_host() for a, b in dev]
+    srv = brm.Server(workers=1, express_workers=express, express_bytes=8 << 20)
+    tickets = [srv.submit(a, b) for a, b in dev]
+    for i, t in enumerate(tickets):
+        C, _ = srv.wait(t, timeout=120.0)
+        assert_same_csr(C.to_host(), alone[i], f"request {i}")
+        del C
+    torch.cuda.synchronize()
+    srv.close()
+    ctx.close()
