@@ -822,7 +822,7 @@ def served_run(dev, pools, rate: float, nreq: int, seed: int = 11, workers: int 
         except brm.BrmError:  # refused at admission (bound above the cap)
             rejected[name] += 1
             continue
-        digests.append((key, dev_digest(C)))
+        digests.append((key, dev_digest(C), st["batch_size"], C.nnz))
         ev = torch.cuda.Event()
         ev.record()
         held.append((ev, C))
@@ -837,8 +837,9 @@ def served_run(dev, pools, rate: float, nreq: int, seed: int = 11, workers: int 
     th.join()
     wall = time.perf_counter() - t_start
     srv.close()
-    mismatches = sum(1 for key, d in digests
-                     if key not in alone or not torch.equal(d, alone[key]))
+    bad = [(key, bs, nnz) for key, d, bs, nnz in digests
+           if key not in alone or not torch.equal(d, alone[key])]
+    mismatches = len(bad)
     allv = [x for v in lat.values() for x in v]
     pct = lambda v, p: round(float(np.percentile(v, p)), 3) if v else None
     per_class = {n: {"n": len(v), "p50_ms": pct(v, 50), "p99_ms": pct(v, 99),
@@ -854,7 +855,9 @@ def served_run(dev, pools, rate: float, nreq: int, seed: int = 11, workers: int 
         "mean_batch": round(float(np.mean(batch_sizes)), 2) if batch_sizes else None,
         "classes": per_class, "mem_cap_gib": 60, "workers": workers, "express_workers": express,
         "verified": mismatches == 0,
-        "checks": {"served_results_vs_isolated_call_mismatches": mismatches},
+        "checks": {"served_results_vs_isolated_call_mismatches": mismatches,
+                   "first_mismatches (class, f32, pool index, batch size, nnz)":
+                       [list(k) + [bs, nnz] for k, bs, nnz in bad[:8]]},
     }
 
 

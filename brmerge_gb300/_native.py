@@ -38,7 +38,7 @@ class CsrC(C.Structure):
 
 class TuningC(C.Structure):
     """Mirror of brm_tuning."""
-    _fields_ = [("seg_cut", C.c_int), ("mid_flop", C.c_int)]
+    _fields_ = [("seg_cut", C.c_int), ("mid_flop", C.c_int), ("long_scratch", C.c_longlong)]
 
 
 class BatchC(C.Structure):

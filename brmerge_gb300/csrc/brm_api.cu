@@ -110,6 +110,7 @@ struct brm_context_s {
     // planning, and the copy, warp and mid rows beside the segments
     brm::Fork fork;
     cudaEvent_t ev[kNumEvents] = {};
+    long long long_scratch = kLongElems;  // products the long-column scratch holds
 };
 
 namespace {
@@ -521,7 +522,7 @@ int numeric_launch(brm_context ctx, brm_dtype dtype, bool upper, const brm_csr *
     {
         // long-column scratch: at most kLongElems products (columns beyond it
         // are reduced inside the segment kernel)
-        const long long elems = std::min<long long>((long long)sz.total_flop, kLongElems);
+        const long long elems = std::min<long long>((long long)sz.total_flop, ctx->long_scratch);
         const long long cols = elems / 8 + 1024;
         const size_t b_col = a256(sizeof(brm::LongCol) * (size_t)cols);
         const size_t b_leaf = a256(2 * (size_t)elems + 2);
@@ -911,7 +912,7 @@ int brm::reserve_pipe(brm_context ctx, brm_dtype dtype, const brm::PipeCaps &c)
         ctx->mid_val = (unsigned char *)ctx->midbuf.p + b_col;
     }
     BRM_TRY(grow(ctx->splitbuf, ((size_t)c.table + 1) * sizeof(int)));
-    BRM_TRY(grow(ctx->longbuf, long_bytes(std::min<long long>(c.products, kLongElems), dtype)));
+    BRM_TRY(grow(ctx->longbuf, long_bytes(std::min<long long>(c.products, ctx->long_scratch), dtype)));
     if (c.spill_bytes)
         BRM_TRY(grow(ctx->spill, (size_t)c.spill_bytes));
     BRM_CK(cudaDeviceSynchronize());  // the buffers exist before any capture
@@ -1123,11 +1124,13 @@ int brm_set_tuning(brm_context ctx, const brm_tuning *t)
         return BRM_ERR_INVALID_VALUE;
     const int cut = t ? t->seg_cut : brm::kSegCut;
     const int mid = t ? t->mid_flop : brm::kMidFlop;
+    const long long ls = (t && t->long_scratch) ? t->long_scratch : kLongElems;
     if (cut < brm::kMinSegCut || cut > brm::kSegCut || mid < brm::kMinMidFlop ||
-        mid > brm::kMidFlop)
+        mid > brm::kMidFlop || ls < 1 || ls > (1ll << 31))
         return BRM_ERR_INVALID_VALUE;
     ctx->plan.seg_cut = cut;
     ctx->plan.mid_limit = mid;
+    ctx->long_scratch = ls;
     ctx->planned = false;  // a plan made under other knobs is not reused
     return BRM_SUCCESS;
 }
@@ -1138,6 +1141,7 @@ int brm_get_tuning(brm_context ctx, brm_tuning *t)
         return BRM_ERR_INVALID_VALUE;
     t->seg_cut = ctx->plan.seg_cut;
     t->mid_flop = ctx->plan.mid_limit;
+    t->long_scratch = ctx->long_scratch == kLongElems ? 0 : ctx->long_scratch;
     return BRM_SUCCESS;
 }
 
@@ -1172,11 +1176,11 @@ int brm_autotune(brm_context ctx, brm_dtype dtype, int n, const brm_csr *A, cons
     double warm = 0;
     BRM_TRY(brm_set_tuning(ctx, nullptr));
     BRM_TRY(run_once(&warm));  // allocations and caches out of the timed runs
-    brm_tuning pick = {brm::kSegCut, brm::kMidFlop};
+    brm_tuning pick = {brm::kSegCut, brm::kMidFlop, keep.long_scratch};
     double pick_s = 1e300;
     for (const int cut : kTuneSegCut) {
         for (const int mid : kTuneMidFlop) {
-            brm_tuning t = {cut, mid};
+            brm_tuning t = {cut, mid, keep.long_scratch};
             BRM_TRY(brm_set_tuning(ctx, &t));
             double s = 1e300;
             for (int rep = 0; rep < 2; rep++) {  // best of two

@@ -240,20 +240,22 @@ class Context:
     def set_validate(self, on: bool):
         _native.check(self._L.brm_set_validate(self._h, 1 if on else 0), "brm_set_validate")
 
-    def set_tuning(self, seg_cut: int | None = None, mid_flop: int | None = None):
+    def set_tuning(self, seg_cut: int | None = None, mid_flop: int | None = None,
+                   long_scratch: int | None = None):
         """brm_set_tuning; no arguments restores the defaults."""
-        if seg_cut is None and mid_flop is None:
+        if seg_cut is None and mid_flop is None and long_scratch is None:
             _native.check(self._L.brm_set_tuning(self._h, None), "brm_set_tuning")
             return
         cur = self.tuning()
         t = _native.TuningC(seg_cut if seg_cut is not None else cur["seg_cut"],
-                            mid_flop if mid_flop is not None else cur["mid_flop"])
+                            mid_flop if mid_flop is not None else cur["mid_flop"],
+                            long_scratch if long_scratch is not None else cur["long_scratch"])
         _native.check(self._L.brm_set_tuning(self._h, C.byref(t)), "brm_set_tuning")
 
     def tuning(self) -> dict:
         t = _native.TuningC()
         _native.check(self._L.brm_get_tuning(self._h, C.byref(t)), "brm_get_tuning")
-        return {"seg_cut": t.seg_cut, "mid_flop": t.mid_flop}
+        return {"seg_cut": t.seg_cut, "mid_flop": t.mid_flop, "long_scratch": t.long_scratch}
 
     def autotune(self, pairs) -> dict:
         """brm_autotune on a list of (A, B) DeviceCSR pairs (one pair: the
@@ -266,7 +268,7 @@ class Context:
         Bs = (_native.CsrC * n)(*[b.c() for _, b in pairs])
         t = _native.TuningC()
         _native.check(self._L.brm_autotune(self._h, code, n, As, Bs, C.byref(t)), "brm_autotune")
-        return {"seg_cut": t.seg_cut, "mid_flop": t.mid_flop}
+        return {"seg_cut": t.seg_cut, "mid_flop": t.mid_flop, "long_scratch": t.long_scratch}
 
     @property
     def last_device_error(self) -> int:

@@ -128,9 +128,14 @@ int brm_set_validate(brm_context ctx, int on);
 typedef struct brm_tuning {
     int seg_cut;
     int mid_flop;
+    /* products the long-column scratch holds (columns of heavy-row segments
+     * with more than eight products, reduced by separate kernels); columns
+     * beyond it are reduced inside the segment kernel.  0: 16 Mi, the default;
+     * otherwise 1 .. 2^31. */
+    long long long_scratch;
 } brm_tuning;
 
-/* NULL restores the defaults (1536, 2048); out-of-range values are
+/* NULL restores the defaults (1536, 2048, 0); out-of-range values are
  * BRM_ERR_INVALID_VALUE. */
 int brm_set_tuning(brm_context ctx, const brm_tuning *t);
 int brm_get_tuning(brm_context ctx, brm_tuning *t);

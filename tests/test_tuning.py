@@ -47,13 +47,13 @@ def test_every_setting_gives_the_same_result(ctx, oracle_mod, name, A, B):
     dA, dB = brm.DeviceCSR.from_host(A), brm.DeviceCSR.from_host(B)
     for cut, mid in _settings():
         ctx.set_tuning(seg_cut=cut, mid_flop=mid)
-        assert ctx.tuning() == {"seg_cut": cut, "mid_flop": mid}
+        assert ctx.tuning() == {"seg_cut": cut, "mid_flop": mid, "long_scratch": 0}
         assert_same_csr(ctx.precise_device(dA, dB).to_host(), R, f"{name} precise {cut}/{mid}")
         assert_same_csr(ctx.precise(dA, dB).to_host(), R, f"{name} split {cut}/{mid}")
         assert_same_csr(ctx.upper(dA, dB).to_host(), R, f"{name} upper {cut}/{mid}")
     ctx.set_tuning()
     cut, mid = _defaults()
-    assert ctx.tuning() == {"seg_cut": cut, "mid_flop": mid}
+    assert ctx.tuning() == {"seg_cut": cut, "mid_flop": mid, "long_scratch": 0}
 
 
 def test_out_of_range_rejected(ctx):
@@ -61,7 +61,7 @@ def test_out_of_range_rejected(ctx):
     for c, m in [(100, mid), (cut + 1, mid), (cut, 2 * mid), (cut, 64)]:
         with pytest.raises(brm.BrmError):
             ctx.set_tuning(seg_cut=c, mid_flop=m)
-    assert ctx.tuning() == {"seg_cut": cut, "mid_flop": mid}
+    assert ctx.tuning() == {"seg_cut": cut, "mid_flop": mid, "long_scratch": 0}
 
 
 def test_autotune_single_and_batch(ctx, oracle_mod):
@@ -80,4 +80,22 @@ def test_autotune_single_and_batch(ctx, oracle_mod):
     assert ctx.tuning() == t2
     for (a, b), C in zip(pairs, ctx.batch_precise(dp)):
         assert_same_csr(C.to_host(), oracle_mod.precise(a, b), "tuned batch")
+    ctx.set_tuning()
+
+
+@pytest.mark.parametrize("long_scratch", [1, 64, 4096])
+def test_long_column_scratch_overflow_gives_the_same_result(ctx, oracle_mod, long_scratch):
+    """Heavy-row segments hand their columns of more than eight products to
+    separate reducers through a scratch of bounded size; columns beyond it are
+    reduced inside the segment kernel.  A tiny scratch forces that path for
+    almost every long column: the result must not change."""
+    cases = [brm.gen_rmat(14, 8 << 14, seed=47),
+             brm.gen_uniform(60, 3000, 500, seed=48)]
+    for A in cases:
+        B = A if A.M == A.N else brm.gen_uniform(3000, 4000, 80, seed=49)
+        R = oracle_mod.precise(A, B)
+        dA, dB = brm.DeviceCSR.from_host(A), brm.DeviceCSR.from_host(B)
+        ctx.set_tuning(long_scratch=long_scratch)
+        assert_same_csr(ctx.precise_device(dA, dB).to_host(), R, f"long scratch {long_scratch}")
+        assert_same_csr(ctx.upper(dA, dB).to_host(), R, f"upper, long scratch {long_scratch}")
     ctx.set_tuning()
