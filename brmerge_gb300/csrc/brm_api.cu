@@ -9,6 +9,7 @@
 #include <atomic>
 #include <chrono>
 #include <climits>
+#include <cstddef>
 #include <cstdlib>
 #include <cstring>
 #include <mutex>
@@ -533,7 +534,10 @@ int numeric_launch(brm_context ctx, brm_dtype dtype, bool upper, const brm_csr *
         P.long_val = q + b_col + b_leaf;
         P.long_cap_cols = cols;
         P.long_cap_elems = elems;
-        BRM_CK(cudaMemsetAsync(&P.cnt->long_used, 0, sizeof(unsigned long long), s));
+        static_assert(offsetof(brm::Counters, long_elems) ==
+                          offsetof(brm::Counters, long_cols) + sizeof(unsigned long long),
+                      "the two long-column counters are cleared together");
+        BRM_CK(cudaMemsetAsync(&P.cnt->long_cols, 0, 2 * sizeof(unsigned long long), s));
     }
     brm::CsrDev a = to_dev(A), b = to_dev(B);
     const int *mcol = mid ? ctx->mid_col : nullptr;

@@ -122,9 +122,11 @@ struct Counters {
     int work_plan;     // dynamic row counter of the heavy-row planning
     int n_huge;        // heavy rows above kHugeFlop products (listed from the end)
     int n_longk;       // rows the narrow analysis left to the warp-wide pass
-    // long columns of the segment kernel handed to the column reducer:
-    // (columns << 40) | elements reserved so far
-    unsigned long long long_used;
+    // long columns of the segment kernel handed to the column reducers:
+    // columns and elements reserved so far (two counters, so neither can
+    // overflow into the other however many columns a call has)
+    unsigned long long long_cols;
+    unsigned long long long_elems;
     // set by the capacity checks of a captured batch pipeline when the batch
     // does not fit its buffers; every kernel that writes at data-dependent
     // offsets then returns at once (the call reports BRM_ERR_CAPACITY)

@@ -965,18 +965,19 @@ __global__ void __launch_bounds__(kSegThreads, 512 / kSegThreads) k_seg_numeric(
               }
               const int ncol = __popc(__ballot_sync(kFull, lj < nlong));
               const int lincl = warp_incl_scan(mylen);
-              unsigned long long rsv = 0;
-              if (lane == 31)
-                  rsv = atomicAdd(&P.cnt->long_used,
-                                  ((unsigned long long)ncol << 40) | (unsigned long long)lincl);
-              rsv = __shfl_sync(kFull, rsv, 31);
+              unsigned long long rcol = 0, relem = 0;
+              if (lane == 31) {
+                  rcol = atomicAdd(&P.cnt->long_cols, (unsigned long long)ncol);
+                  relem = atomicAdd(&P.cnt->long_elems, (unsigned long long)lincl);
+              }
+              rcol = __shfl_sync(kFull, rcol, 31);
+              relem = __shfl_sync(kFull, relem, 31);
               for (int jc = 0; jc < ncol; jc++) {
                 const int u = __shfl_sync(kFull, myu, jc);
                 const int len = __shfl_sync(kFull, mylen, jc);
                 const int i0 = ucnt[u], i1 = i0 + len;
-                const long long lci = (long long)(rsv >> 40) + jc;
-                const long long leo = (long long)(rsv & ((1ull << 40) - 1ull)) +
-                                      __shfl_sync(kFull, lincl - mylen, jc);
+                const long long lci = (long long)rcol + jc;
+                const long long leo = (long long)relem + __shfl_sync(kFull, lincl - mylen, jc);
                 const bool handoff = lci < P.long_cap_cols && leo + len <= P.long_cap_elems;
                 for (int w = lane; w < nwp; w += 32)
                     bmp[w] = 0;
@@ -1137,8 +1138,7 @@ __global__ void __launch_bounds__(128) k_long_reduce(PlanDev P, int *ccol, T *cv
 {
     if (P.cnt->abort)  // a capacity check of a captured pipeline failed
         return;
-    const unsigned long long used = P.cnt->long_used;
-    const long long n = min((long long)(used >> 40), P.long_cap_cols);
+    const long long n = min((long long)P.cnt->long_cols, P.long_cap_cols);
     const T *__restrict__ lval = (const T *)P.long_val;
     const unsigned short *__restrict__ lleaf = P.long_leaf;
     for (long long i0 = (long long)blockIdx.x * blockDim.x; i0 < n;
@@ -1168,8 +1168,7 @@ __global__ void __launch_bounds__(128) k_long_warp(PlanDev P, int *ccol, T *cval
     __shared__ int s_cnt[4][32];
     __shared__ T s_val[4][32];
     const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const unsigned long long used = P.cnt->long_used;
-    const long long n = min((long long)(used >> 40), P.long_cap_cols);
+    const long long n = min((long long)P.cnt->long_cols, P.long_cap_cols);
     const T *__restrict__ lval = (const T *)P.long_val;
     const unsigned short *__restrict__ lleaf = P.long_leaf;
     for (long long i0 = (long long)blockIdx.x * blockDim.x; i0 < n;

@@ -112,3 +112,31 @@ def test_batch_graph_replays_new_values(ctx, oracle_mod, dtype):
             assert_same_csr(got, oracle_mod.precise(A, B), f"replay {it} pair {i}")
             assert_same_csr(got, fresh[i].to_host(), f"replay {it} pair {i} vs fresh")
     g.close()
+
+
+def _dev_equal(x, y):
+    import torch
+    if x.shape != y.shape or x.dtype != y.dtype:
+        return False
+    if x.dtype == torch.float64:
+        x, y = x.view(torch.int64), y.view(torch.int64)
+    return bool(torch.equal(x, y))
+
+
+def test_batch_with_more_than_2_pow_24_long_columns(ctx):
+    """Sixteen R-MAT n=2^16 degree-8 products in one batch (about 2e9
+    products) hand more than 2^24 columns of heavy-row segments to the column
+    reducers; every C_i must still equal its single call bit for bit
+    (compared on the device)."""
+    import torch
+    mats = [brm.gen_rmat(16, 8 << 16, seed=21 + i) for i in range(4)]
+    dev = [brm.DeviceCSR.from_host(A) for A in mats]
+    alone = [ctx.precise_device(d, d) for d in dev]
+    res = ctx.batch_precise([(dev[i % 4], dev[i % 4]) for i in range(16)])
+    for i, C in enumerate(res):
+        R = alone[i % 4]
+        assert C.nnz == R.nnz, i
+        assert (_dev_equal(C.rpt, R.rpt) and _dev_equal(C.col, R.col)
+                and _dev_equal(C.val, R.val)), f"pair {i}"
+    del res, alone
+    torch.cuda.synchronize()
