@@ -771,7 +771,7 @@ def served_pools(dev, seed: int = 11):
 
 
 def served_run(dev, pools, rate: float, nreq: int, seed: int = 11, workers: int = 2,
-               express: int = 1):
+               express: int = 1, express_sms: int = 0):
     """A Poisson request stream at `rate` into brm_server (continuous
     batching under a 60 GiB cap, `workers` general and `express` small-request
     workers).  Latency = submit -> result ready.  Every served result is
@@ -788,7 +788,9 @@ def served_run(dev, pools, rate: float, nreq: int, seed: int = 11, workers: int 
     kinds = rng.choice(len(names), size=nreq, p=[p[1] for p in prob])
     f32 = rng.random(nreq) < 0.5
     arrivals = np.cumsum(rng.exponential(1.0 / rate, nreq))
-    srv = brm.Server(mem_cap_bytes=60 << 30, workers=workers, express_workers=express)
+    srv = brm.Server(mem_cap_bytes=60 << 30, workers=workers, express_workers=express,
+                     express_sms=express_sms)
+    sm_split = srv.sms()
     tickets = q.Queue()
     rejected = {n: 0 for n in names}
     t_start = time.perf_counter()
@@ -854,6 +856,7 @@ def served_run(dev, pools, rate: float, nreq: int, seed: int = 11, workers: int 
         "p50_ms": pct(allv, 50), "p99_ms": pct(allv, 99),
         "mean_batch": round(float(np.mean(batch_sizes)), 2) if batch_sizes else None,
         "classes": per_class, "mem_cap_gib": 60, "workers": workers, "express_workers": express,
+        "sm_partition": {"express_sms": sm_split[0], "other_sms": sm_split[1]},
         "verified": mismatches == 0,
         "checks": {"served_results_vs_isolated_call_mismatches": mismatches,
                    "first_mismatches (class, f32, pool index, batch size, nnz)":

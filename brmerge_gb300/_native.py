@@ -60,7 +60,8 @@ class BatchCapsC(C.Structure):
 class ServerConfigC(C.Structure):
     """Mirror of brm_server_config."""
     _fields_ = [("mem_cap_bytes", C.c_longlong), ("max_batch", C.c_int), ("workers", C.c_int),
-                ("express_workers", C.c_int), ("express_bytes", C.c_longlong)]
+                ("express_workers", C.c_int), ("express_bytes", C.c_longlong),
+                ("express_sms", C.c_int)]
 
 
 class ServerResultC(C.Structure):
@@ -152,6 +153,7 @@ def lib() -> C.CDLL:
         _decl(L.brm_batch_precise, C.c_int, [vp, C.c_int, C.c_int, csrp, csrp, C.POINTER(BatchC)])
         _decl(L.brm_batch_free, C.c_int, [vp, C.POINTER(BatchC)])
         _decl(L.brm_server_create, C.c_int, [C.POINTER(ServerConfigC), ctxp])
+        _decl(L.brm_server_sms, C.c_int, [vp, c_int_p, c_int_p])
         _decl(L.brm_server_submit, C.c_int, [vp, C.c_int, csrp, csrp, C.POINTER(C.c_longlong)])
         _decl(L.brm_server_wait, C.c_int,
               [vp, C.c_longlong, C.c_double, C.POINTER(ServerResultC)])

@@ -145,17 +145,24 @@ int cuda_status(cudaError_t e)
 
 size_t a256(size_t x) { return (x + 255) & ~size_t(255); }
 
-int grow(DevBuf &b, size_t bytes)
+// Grows a context buffer to at least `bytes` (25 % headroom when it grows
+// again), stream-ordered on the context's stream: the old block is released
+// after the work queued before it, and neither call waits for the device, so
+// a context never stalls behind other contexts' kernels to grow.  Every use
+// of a buffer on the context's second stream is joined back into the main
+// stream before the next growth.
+int grow(brm_context ctx, DevBuf &b, size_t bytes)
 {
     if (bytes <= b.cap && b.p)
         return BRM_SUCCESS;
+    size_t want = bytes < 256 ? 256 : bytes;
     if (b.p) {
-        cudaFree(b.p);
+        want = std::max(want, b.cap + b.cap / 4);
+        cudaFreeAsync(b.p, ctx->stream);
         b.p = nullptr;
         b.cap = 0;
     }
-    size_t want = bytes < 256 ? 256 : bytes;
-    BRM_CK(cudaMalloc(&b.p, want));
+    BRM_CK(cudaMallocAsync(&b.p, want, ctx->stream));
     b.cap = want;
     return BRM_SUCCESS;
 }
@@ -201,12 +208,14 @@ int ensure_workspace(brm_context ctx, int M)
 {
     if (ctx->ws && M <= ctx->ws_M)
         return BRM_SUCCESS;
-    if (ctx->ws) {
-        cudaFree(ctx->ws);
+    if (ctx->ws) {  // stream-ordered, with headroom (see grow)
+        M = (int)std::min<long long>(INT_MAX - 1,
+                                     std::max<long long>(M, ctx->ws_M + (long long)ctx->ws_M / 4));
+        cudaFreeAsync(ctx->ws, ctx->stream);
         ctx->ws = nullptr;
     }
     size_t bytes = workspace_bytes(M);
-    BRM_CK(cudaMalloc(&ctx->ws, bytes));
+    BRM_CK(cudaMallocAsync(&ctx->ws, bytes, ctx->stream));
     ctx->ws_bytes = bytes;
     ctx->ws_M = M;
     size_t m = (size_t)(M > 0 ? M : 1);
@@ -244,7 +253,7 @@ int ensure_workspace(brm_context ctx, int M)
 int ensure_ameta(brm_context ctx, int nnzA)
 {
     const size_t n = (size_t)(nnzA > 0 ? nnzA : 1);
-    BRM_TRY(grow(ctx->ameta, 8 * n));
+    BRM_TRY(grow(ctx, ctx->ameta, 8 * n));
     ctx->plan.abs = (int *)ctx->ameta.p;
     ctx->plan.alen = (int *)ctx->ameta.p + n;
     return BRM_SUCCESS;
@@ -392,14 +401,14 @@ int plan_phase(brm_context ctx, const brm_csr *A, const brm_csr *B, int *crpt, b
         const long long tot = ctx->h_mid[0] + ctx->h_mid[1];
         const size_t n = (size_t)(tot > 0 ? tot : 1);
         const size_t b_col = a256(4 * n);
-        BRM_TRY(grow(ctx->midbuf, b_col + vsize((brm_dtype)fused_dtype) * n));
+        BRM_TRY(grow(ctx, ctx->midbuf, b_col + vsize((brm_dtype)fused_dtype) * n));
         ctx->mid_col = (int *)ctx->midbuf.p;
         ctx->mid_val = (unsigned char *)ctx->midbuf.p + b_col;
     }
     {
         const size_t cap = (size_t)ctx->h_cnt->seg_cap + 1;
         const size_t b_run = a256(cap * sizeof(brm::SegRun));
-        BRM_TRY(grow(ctx->segbuf, b_run + cap * (sizeof(brm::SegDesc) + sizeof(int))));
+        BRM_TRY(grow(ctx, ctx->segbuf, b_run + cap * (sizeof(brm::SegDesc) + sizeof(int))));
         P.run = (brm::SegRun *)ctx->segbuf.p;
         P.seg = (brm::SegDesc *)((unsigned char *)ctx->segbuf.p + b_run);
         P.seg_list = (int *)(P.seg + cap);
@@ -506,7 +515,7 @@ int numeric_launch(brm_context ctx, brm_dtype dtype, bool upper, const brm_csr *
     const bool mid = use_mid && ctx->mid_ready && !upper;
     const NumSizes sz = sizes ? *sizes : planned_sizes(ctx);
     if (sz.spill_bytes)
-        BRM_TRY(grow(ctx->spill, sz.spill_bytes));
+        BRM_TRY(grow(ctx, ctx->spill, sz.spill_bytes));
     cudaStream_t s = ctx->stream;
     brm::PlanDev P = ctx->plan;
     P.r_lo = part.r_lo;
@@ -517,7 +526,7 @@ int numeric_launch(brm_context ctx, brm_dtype dtype, bool upper, const brm_csr *
     // work_num and (unless the errors of earlier parts must survive) err
     BRM_CK(cudaMemsetAsync(&P.cnt->work_num, 0, (clear_err ? 2 : 1) * sizeof(int), s));
     BRM_CK(cudaMemsetAsync(&P.cnt->work_bnum, 0, 2 * sizeof(int), s));  // work_bnum, work_seg
-    BRM_TRY(grow(ctx->splitbuf, ((size_t)sz.table_cap + 1) * sizeof(int)));
+    BRM_TRY(grow(ctx, ctx->splitbuf, ((size_t)sz.table_cap + 1) * sizeof(int)));
     P.split = (int *)ctx->splitbuf.p;
     ctx->plan.split = P.split;
     {
@@ -527,7 +536,7 @@ int numeric_launch(brm_context ctx, brm_dtype dtype, bool upper, const brm_csr *
         const long long cols = elems / 8 + 1024;
         const size_t b_col = a256(sizeof(brm::LongCol) * (size_t)cols);
         const size_t b_leaf = a256(2 * (size_t)elems + 2);
-        BRM_TRY(grow(ctx->longbuf, long_bytes(elems, dtype)));
+        BRM_TRY(grow(ctx, ctx->longbuf, long_bytes(elems, dtype)));
         unsigned char *q = (unsigned char *)ctx->longbuf.p;
         P.long_col = (brm::LongCol *)q;
         P.long_leaf = (unsigned short *)(q + b_col);
@@ -569,8 +578,8 @@ int check_dtype(brm_dtype d) { return (d == BRM_F64 || d == BRM_F32) ? BRM_SUCCE
 int upper_numeric_into_bar(brm_context ctx, brm_dtype dtype, const brm_csr *A, const brm_csr *B)
 {
     unsigned long long tf = ctx->h_cnt->total_flop;
-    BRM_TRY(grow(ctx->bar_col, (size_t)tf * 4));
-    BRM_TRY(grow(ctx->bar_val, (size_t)tf * vsize(dtype)));
+    BRM_TRY(grow(ctx, ctx->bar_col, (size_t)tf * 4));
+    BRM_TRY(grow(ctx, ctx->bar_val, (size_t)tf * vsize(dtype)));
     return numeric_launch(ctx, dtype, true, A, B, nullptr, (int *)ctx->bar_col.p, ctx->bar_val.p);
 }
 
@@ -630,7 +639,7 @@ int numeric_by_parts(brm_context ctx, brm_dtype dtype, const brm_csr *A, const b
     // device: pb, cnt, fill, ranges, reordered segment list
     const int nseg = ctx->h_cnt->n_seg;
     const size_t b_small = a256(sizeof(int) * (size_t)(4 * brm::kMaxParts + 4));
-    BRM_TRY(grow(ctx->partbuf, b_small + sizeof(int) * (size_t)(nseg + 1)));
+    BRM_TRY(grow(ctx, ctx->partbuf, b_small + sizeof(int) * (size_t)(nseg + 1)));
     int *d_pb = (int *)ctx->partbuf.p;
     int *d_cnt = d_pb + (brm::kMaxParts + 1);
     int *d_fill = d_cnt + brm::kMaxParts;
@@ -717,13 +726,13 @@ int host_call(bool upper, const int *arpt, const int *acol, const T *aval, const
         return BRM_ERR_INVALID_VALUE;
     const bool same = (arpt == brpt && acol == bcol && aval == bval && M == K);
     const bool timed = pt || ut;
-    BRM_TRY(grow(ctx->io_arpt, 4 * ((size_t)M + 1)));
-    BRM_TRY(grow(ctx->io_acol, 4 * (size_t)nnzA));
-    BRM_TRY(grow(ctx->io_aval, sizeof(T) * (size_t)nnzA));
+    BRM_TRY(grow(ctx, ctx->io_arpt, 4 * ((size_t)M + 1)));
+    BRM_TRY(grow(ctx, ctx->io_acol, 4 * (size_t)nnzA));
+    BRM_TRY(grow(ctx, ctx->io_aval, sizeof(T) * (size_t)nnzA));
     if (!same) {
-        BRM_TRY(grow(ctx->io_brpt, 4 * ((size_t)K + 1)));
-        BRM_TRY(grow(ctx->io_bcol, 4 * (size_t)nnzB));
-        BRM_TRY(grow(ctx->io_bval, sizeof(T) * (size_t)nnzB));
+        BRM_TRY(grow(ctx, ctx->io_brpt, 4 * ((size_t)K + 1)));
+        BRM_TRY(grow(ctx, ctx->io_bcol, 4 * (size_t)nnzB));
+        BRM_TRY(grow(ctx, ctx->io_bval, sizeof(T) * (size_t)nnzB));
     }
     ev_record(ctx, timed, kEvIn);
     BRM_CK(cudaMemcpyAsync(ctx->io_arpt.p, arpt, 4 * ((size_t)M + 1), cudaMemcpyHostToDevice, s));
@@ -738,7 +747,7 @@ int host_call(bool upper, const int *arpt, const int *acol, const T *aval, const
         BRM_CK(cudaMemcpyAsync(ctx->io_bval.p, bval, sizeof(T) * (size_t)nnzB, cudaMemcpyHostToDevice, s));
         B = brm_csr{K, N, nnzB, (const int *)ctx->io_brpt.p, (const int *)ctx->io_bcol.p, ctx->io_bval.p};
     }
-    BRM_TRY(grow(ctx->io_crpt, 4 * ((size_t)M + 1)));
+    BRM_TRY(grow(ctx, ctx->io_crpt, 4 * ((size_t)M + 1)));
     double t_pre = now_sec();
     int cnnz = 0;
     bool copied = false;  // C already copied back part by part
@@ -757,8 +766,8 @@ int host_call(bool upper, const int *arpt, const int *acol, const T *aval, const
         R.val = (T *)brm::host_alloc(sizeof(T) * (size_t)(cnnz > 0 ? cnnz : 1));
         if (!R.rpt || !R.col || !R.val)
             return BRM_ERR_ALLOC;
-        BRM_TRY(grow(ctx->io_ccol, 4 * (size_t)cnnz));
-        BRM_TRY(grow(ctx->io_cval, sizeof(T) * (size_t)cnnz));
+        BRM_TRY(grow(ctx, ctx->io_ccol, 4 * (size_t)cnnz));
+        BRM_TRY(grow(ctx, ctx->io_cval, sizeof(T) * (size_t)cnnz));
         dcol = (int *)ctx->io_ccol.p;
         dval = ctx->io_cval.p;
         return BRM_SUCCESS;
@@ -873,6 +882,12 @@ int brm::device_status(int err) { return device_err_status(err); }
 
 const brm::Counters *brm::context_counters(brm_context ctx) { return ctx->plan.cnt; }
 
+int brm::set_context_sms(brm_context ctx, int sms)
+{
+    ctx->num_sms = std::max(1, sms);
+    return BRM_SUCCESS;
+}
+
 int brm::set_context_priority(brm_context ctx, int priority)
 {
     cudaStream_t s = nullptr;
@@ -903,7 +918,7 @@ int brm::reserve_pipe(brm_context ctx, brm_dtype dtype, const brm::PipeCaps &c)
     {
         const size_t cap = (size_t)c.seg_slots + 1;
         const size_t b_run = a256(cap * sizeof(brm::SegRun));
-        BRM_TRY(grow(ctx->segbuf, b_run + cap * (sizeof(brm::SegDesc) + sizeof(int))));
+        BRM_TRY(grow(ctx, ctx->segbuf, b_run + cap * (sizeof(brm::SegDesc) + sizeof(int))));
         ctx->plan.run = (brm::SegRun *)ctx->segbuf.p;
         ctx->plan.seg = (brm::SegDesc *)((unsigned char *)ctx->segbuf.p + b_run);
         ctx->plan.seg_list = (int *)(ctx->plan.seg + cap);
@@ -911,14 +926,14 @@ int brm::reserve_pipe(brm_context ctx, brm_dtype dtype, const brm::PipeCaps &c)
     {
         const size_t n = (size_t)std::max(c.products, 1LL);
         const size_t b_col = a256(4 * n);
-        BRM_TRY(grow(ctx->midbuf, b_col + vsize(dtype) * n));
+        BRM_TRY(grow(ctx, ctx->midbuf, b_col + vsize(dtype) * n));
         ctx->mid_col = (int *)ctx->midbuf.p;
         ctx->mid_val = (unsigned char *)ctx->midbuf.p + b_col;
     }
-    BRM_TRY(grow(ctx->splitbuf, ((size_t)c.table + 1) * sizeof(int)));
-    BRM_TRY(grow(ctx->longbuf, long_bytes(std::min<long long>(c.products, ctx->long_scratch), dtype)));
+    BRM_TRY(grow(ctx, ctx->splitbuf, ((size_t)c.table + 1) * sizeof(int)));
+    BRM_TRY(grow(ctx, ctx->longbuf, long_bytes(std::min<long long>(c.products, ctx->long_scratch), dtype)));
     if (c.spill_bytes)
-        BRM_TRY(grow(ctx->spill, (size_t)c.spill_bytes));
+        BRM_TRY(grow(ctx, ctx->spill, (size_t)c.spill_bytes));
     BRM_CK(cudaDeviceSynchronize());  // the buffers exist before any capture
     return BRM_SUCCESS;
 }
@@ -1311,8 +1326,8 @@ int brm_upper_device(brm_context ctx, brm_dtype dtype, const brm_csr *A, const b
     ctx->planned = false;
     BRM_TRY(plan_phase(ctx, A, B, nullptr, true, timed));
     double t1 = now_sec();
-    BRM_TRY(grow(ctx->bar_col, (size_t)ctx->h_cnt->total_flop * 4));
-    BRM_TRY(grow(ctx->bar_val, (size_t)ctx->h_cnt->total_flop * vsize(dtype)));
+    BRM_TRY(grow(ctx, ctx->bar_col, (size_t)ctx->h_cnt->total_flop * 4));
+    BRM_TRY(grow(ctx, ctx->bar_val, (size_t)ctx->h_cnt->total_flop * vsize(dtype)));
     double t2 = now_sec();
     int *crpt = nullptr;
     BRM_CK(cudaMallocAsync((void **)&crpt, 4 * ((size_t)A->M + 1), ctx->stream));

@@ -46,6 +46,9 @@ Counters last_plan_counters(brm_context ctx);
 // device bytes an Upper call on an M-row A with `products` products needs at
 // most (brm_upper_bound's estimate).
 int set_context_priority(brm_context ctx, int priority);
+// Sizes the context's persistent grids for `sms` SMs (a context whose streams
+// run on a partition of the device's SMs).
+int set_context_sms(brm_context ctx, int sms);
 long long upper_bound_bytes(brm_dtype dtype, int M, long long products);
 // Device-side capacity check of a captured pipeline: stage 0 after the row
 // analysis and the mid-row prefix sums, stage 1 after the symbolic phase.

@@ -29,6 +29,7 @@
 #include <unordered_map>
 #include <vector>
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include "brm_common.cuh"
@@ -133,6 +134,50 @@ __global__ void __launch_bounds__(kAdmitThreads) k_admit_count(const AdmitItem *
     }
 }
 
+// SM partitions (green contexts): the driver's entry points, looked up at
+// run time so that the library needs no link-time driver dependency.
+struct GreenApi {
+    CUresult (*dev_get)(CUdevice *, int) = nullptr;
+    CUresult (*get_res)(CUdevice, CUdevResource *, CUdevResourceType) = nullptr;
+    CUresult (*split)(CUdevResource *, unsigned *, const CUdevResource *, CUdevResource *,
+                      unsigned, unsigned) = nullptr;
+    CUresult (*gen_desc)(CUdevResourceDesc *, CUdevResource *, unsigned) = nullptr;
+    CUresult (*create)(CUgreenCtx *, CUdevResourceDesc, CUdevice, unsigned) = nullptr;
+    CUresult (*destroy)(CUgreenCtx) = nullptr;
+    CUresult (*to_ctx)(CUcontext *, CUgreenCtx) = nullptr;
+    CUresult (*set_current)(CUcontext) = nullptr;
+    CUresult (*get_current)(CUcontext *) = nullptr;
+
+    template <typename F>
+    static bool sym(const char *name, F &f)
+    {
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        void *p = nullptr;
+        if (cudaGetDriverEntryPointByVersion(name, &p, 13000, cudaEnableDefault, &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess || !p) {
+            (void)cudaGetLastError();
+            return false;
+        }
+        f = reinterpret_cast<F>(p);
+        return true;
+    }
+    bool load()
+    {
+        return sym("cuDeviceGet", dev_get) && sym("cuDeviceGetDevResource", get_res) &&
+               sym("cuDevSmResourceSplitByCount", split) &&
+               sym("cuDevResourceGenerateDesc", gen_desc) && sym("cuGreenCtxCreate", create) &&
+               sym("cuGreenCtxDestroy", destroy) && sym("cuCtxFromGreenCtx", to_ctx) &&
+               sym("cuCtxSetCurrent", set_current) && sym("cuCtxGetCurrent", get_current);
+    }
+};
+
+// One SM partition: a green context and its context handle.
+struct Partition {
+    CUgreenCtx green = nullptr;
+    CUcontext ctx = nullptr;
+    int sms = 0;
+};
+
 }  // namespace
 
 struct brm_server_s {
@@ -154,6 +199,35 @@ struct brm_server_s {
     std::vector<char> express;  // per worker: takes only small requests
     std::thread admitter;
     cudaStream_t admit_stream = nullptr;
+    // SM partitions: the express workers and the admission run on the SM set
+    // res[0], the other workers on res[1].  A green context may be current
+    // in one thread at a time, so every thread has one of its own (gctx[w]
+    // for worker w, gctx_admit for the admission thread).
+    GreenApi api;
+    CUdevice cu_dev = 0;
+    CUdevResource res[2] = {};
+    int part_sms[2] = {0, 0};
+    bool partitioned = false;
+    std::vector<Partition> gctx;
+    Partition gctx_admit;
+
+    bool make_partitions(int express_sms);
+    int new_green(int set, Partition *out);
+    void drop_green(Partition &p)
+    {
+        if (p.green)
+            api.destroy(p.green);
+        p = Partition{};
+    }
+    // Makes the calling thread run on its own green context (or the device's
+    // primary context when the SMs are not partitioned).
+    void enter(const Partition &p)
+    {
+        if (partitioned && p.ctx)
+            api.set_current(p.ctx);
+        else
+            cudaSetDevice(device);
+    }
 
     void work(int w);
     void admit();
@@ -168,9 +242,45 @@ void brm_server_s::finish(Request *r, int status)
     r->done = true;
 }
 
+// Splits the device's SMs into a partition of at least express_sms SMs (for
+// the express workers and the admission) and the rest (for the other
+// workers), one green context each.  False (nothing changed) when the driver
+// or the device cannot.
+bool brm_server_s::make_partitions(int express_sms)
+{
+    if (!api.load())
+        return false;
+    CUdevResource all{};
+    unsigned ng = 1;
+    if (api.dev_get(&cu_dev, device) != CUDA_SUCCESS ||
+        api.get_res(cu_dev, &all, CU_DEV_RESOURCE_TYPE_SM) != CUDA_SUCCESS ||
+        api.split(&res[0], &ng, &all, &res[1], 0, (unsigned)express_sms) != CUDA_SUCCESS ||
+        ng < 1 || res[0].sm.smCount == 0 || res[1].sm.smCount == 0)
+        return false;
+    part_sms[0] = (int)res[0].sm.smCount;
+    part_sms[1] = (int)res[1].sm.smCount;
+    partitioned = true;
+    return true;
+}
+
+// A green context over SM set `set` (0: express, 1: the rest).
+int brm_server_s::new_green(int set, Partition *out)
+{
+    *out = Partition{};
+    CUdevResourceDesc desc;
+    if (api.gen_desc(&desc, &res[set], 1) != CUDA_SUCCESS ||
+        api.create(&out->green, desc, cu_dev, CU_GREEN_CTX_DEFAULT_STREAM) != CUDA_SUCCESS ||
+        api.to_ctx(&out->ctx, out->green) != CUDA_SUCCESS) {
+        drop_green(*out);
+        return BRM_ERR_CUDA;
+    }
+    out->sms = part_sms[set];
+    return BRM_SUCCESS;
+}
+
 void brm_server_s::admit()
 {
-    cudaSetDevice(device);
+    enter(gctx_admit);
     AdmitItem *d_items = nullptr, *h_items = nullptr;
     unsigned long long *d_out = nullptr, *h_out = nullptr;
     int cap_items = 0;
@@ -267,9 +377,9 @@ void brm_server_s::admit()
 
 void brm_server_s::work(int w)
 {
-    cudaSetDevice(device);
-    brm_context ctx = ctxs[(size_t)w];
     const bool small_only = express[(size_t)w] != 0;
+    enter(gctx[(size_t)w]);
+    brm_context ctx = ctxs[(size_t)w];
     for (;;) {
         std::vector<Request *> batch;
         {
@@ -356,14 +466,37 @@ int brm_server_create(const brm_server_config *cfg, brm_server *out)
     const int nw = (cfg && cfg->workers > 0) ? std::min(cfg->workers, 16) : 2;
     const int nx = cfg ? (cfg->express_workers < 0 ? 0 : std::min(cfg->express_workers, 16)) : 1;
     srv->express_bytes = (cfg && cfg->express_bytes > 0) ? cfg->express_bytes : (64ll << 20);
+    const int xsms = cfg ? cfg->express_sms : 0;
     cudaGetDevice(&srv->device);
     int lo = 0, hi = 0;  // stream priorities: hi is the most urgent (numerically lowest)
     int st = cudaDeviceGetStreamPriorityRange(&lo, &hi) == cudaSuccess ? BRM_SUCCESS : BRM_ERR_CUDA;
-    if (st == BRM_SUCCESS &&
-        cudaStreamCreateWithPriority(&srv->admit_stream, cudaStreamNonBlocking, hi) != cudaSuccess)
-        st = BRM_ERR_CUDA;
+    // SM partitions for the express workers (when the driver offers them)
+    CUcontext caller = nullptr;
+    if (st == BRM_SUCCESS && nx > 0 && xsms >= 0 && srv->make_partitions(xsms > 0 ? xsms : 16))
+        srv->api.get_current(&caller);
+    srv->gctx.assign((size_t)(nw + nx), Partition{});
+    auto leave = [&] {
+        if (srv->partitioned)
+            srv->api.set_current(caller);
+    };
+    if (st == BRM_SUCCESS && srv->partitioned)
+        st = srv->new_green(0, &srv->gctx_admit);
+    if (st == BRM_SUCCESS) {
+        srv->enter(srv->gctx_admit);
+        if (cudaStreamCreateWithPriority(&srv->admit_stream, cudaStreamNonBlocking, hi) !=
+            cudaSuccess)
+            st = BRM_ERR_CUDA;
+    }
     for (int w = 0; w < nw + nx && st == BRM_SUCCESS; w++) {
         const bool xw = w >= nw;
+        if (srv->partitioned) {
+            st = srv->new_green(xw ? 0 : 1, &srv->gctx[(size_t)w]);
+            if (st != BRM_SUCCESS)
+                break;
+        }
+        // the worker's context, streams and events belong to its own
+        // context (green when partitioned)
+        srv->enter(srv->gctx[(size_t)w]);
         brm_context c = nullptr;
         cudaStream_t s = nullptr;
         st = brm_create(&c);
@@ -378,25 +511,43 @@ int brm_server_create(const brm_server_config *cfg, brm_server *out)
         brm_set_stream(c, s);
         if (xw)
             st = brm::set_context_priority(c, hi);
+        if (st == BRM_SUCCESS && srv->partitioned)
+            st = brm::set_context_sms(c, srv->gctx[(size_t)w].sms);
         srv->ctxs.push_back(c);
         srv->streams.push_back(s);
         srv->express.push_back(xw ? 1 : 0);
     }
     if (st != BRM_SUCCESS) {
         (void)cudaGetLastError();
-        for (brm_context c : srv->ctxs)
-            brm_destroy(c);
-        for (cudaStream_t s : srv->streams)
-            cudaStreamDestroy(s);
+        for (size_t w = 0; w < srv->ctxs.size(); w++) {
+            srv->enter(srv->gctx[w]);
+            brm_destroy(srv->ctxs[w]);
+            cudaStreamDestroy(srv->streams[w]);
+        }
+        srv->enter(srv->gctx_admit);
         if (srv->admit_stream)
             cudaStreamDestroy(srv->admit_stream);
+        leave();
+        for (Partition &p : srv->gctx)
+            srv->drop_green(p);
+        srv->drop_green(srv->gctx_admit);
         delete srv;
         return st;
     }
+    leave();
     srv->admitter = std::thread([srv] { srv->admit(); });
     for (int w = 0; w < nw + nx; w++)
         srv->workers.emplace_back([srv, w] { srv->work(w); });
     *out = srv;
+    return BRM_SUCCESS;
+}
+
+int brm_server_sms(brm_server srv, int *express_sms, int *other_sms)
+{
+    if (!srv || !express_sms || !other_sms)
+        return BRM_ERR_INVALID_VALUE;
+    *express_sms = srv->partitioned ? srv->part_sms[0] : 0;
+    *other_sms = srv->partitioned ? srv->part_sms[1] : 0;
     return BRM_SUCCESS;
 }
 
@@ -499,11 +650,22 @@ int brm_server_destroy(brm_server srv)
     for (auto &kv : srv->all)
         delete kv.second;
     srv->all.clear();
-    for (brm_context c : srv->ctxs)
-        brm_destroy(c);
-    for (cudaStream_t s : srv->streams)
-        cudaStreamDestroy(s);
+    CUcontext caller = nullptr;
+    if (srv->partitioned)
+        srv->api.get_current(&caller);
+    for (size_t w = 0; w < srv->ctxs.size(); w++) {
+        srv->enter(srv->gctx[w]);
+        brm_destroy(srv->ctxs[w]);
+        cudaStreamDestroy(srv->streams[w]);
+    }
+    srv->enter(srv->gctx_admit);
     cudaStreamDestroy(srv->admit_stream);
+    if (srv->partitioned) {
+        srv->api.set_current(caller);
+        for (Partition &p : srv->gctx)
+            srv->drop_green(p);
+        srv->drop_green(srv->gctx_admit);
+    }
     delete srv;
     return BRM_SUCCESS;
 }

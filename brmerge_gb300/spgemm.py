@@ -619,14 +619,21 @@ class Server:
     wait()."""
 
     def __init__(self, mem_cap_bytes: int = 0, max_batch: int = 0, workers: int = 0,
-                 express_workers: int = 1, express_bytes: int = 0):
+                 express_workers: int = 1, express_bytes: int = 0, express_sms: int = 0):
         self._L = _native.lib()
         self._h = C.c_void_p()
         cfg = _native.ServerConfigC(mem_cap_bytes, max_batch, workers,
-                                    express_workers if express_workers > 0 else -1, express_bytes)
+                                    express_workers if express_workers > 0 else -1, express_bytes,
+                                    express_sms)
         _native.check(self._L.brm_server_create(C.byref(cfg), C.byref(self._h)),
                       "brm_server_create")
         self._inputs = {}  # ticket -> (A, B): kept alive until the result is waited for
+
+    def sms(self) -> tuple:
+        """(express partition SMs, other workers' SMs); (0, 0) without partitions."""
+        x, o = C.c_int(0), C.c_int(0)
+        _native.check(self._L.brm_server_sms(self._h, C.byref(x), C.byref(o)), "brm_server_sms")
+        return x.value, o.value
 
     def submit(self, A: "DeviceCSR", B: "DeviceCSR") -> int:
         import torch

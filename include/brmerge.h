@@ -335,8 +335,11 @@ int brm_batch_pipe_destroy(brm_batch_pipe pipe);
  * while batches run wait for the next free worker, and the batches of
  * different workers overlap on the device.  Express workers take only
  * requests whose bound is at most express_bytes and run on the device's
- * highest-priority streams, so small batches are scheduled ahead of the
- * pending blocks of large ones.  A request completes when its batch does.
+ * highest-priority streams; where the driver offers SM partitions (green
+ * contexts), the express workers and the admission run on a set of
+ * express_sms SMs of their own and the other workers on the rest, so a large
+ * batch's kernels never hold the SMs a small request needs.  A request
+ * completes when its batch does.
  * Every result is bit-identical to brm_precise_device on its pair.  No
  * counterpart in the reference (one library call per product). */
 typedef struct brm_server_s *brm_server;
@@ -347,6 +350,7 @@ typedef struct brm_server_config {
     int workers;              /* concurrent batches of any size, <= 0: 2 (at most 16) */
     int express_workers;      /* small-request workers, < 0: none (NULL cfg: 1; at most 16) */
     long long express_bytes;  /* largest bound an express worker takes, <= 0: 64 MiB */
+    int express_sms;          /* SMs set apart for the express workers, 0: 16, < 0: none */
 } brm_server_config;
 
 typedef struct brm_server_result {
@@ -362,6 +366,9 @@ typedef struct brm_server_result {
 
 /* On the current device; cfg may be NULL. */
 int brm_server_create(const brm_server_config *cfg, brm_server *srv);
+/* SMs of the express partition and of the other workers' partition (both
+ * 0 when the server runs without SM partitions). */
+int brm_server_sms(brm_server srv, int *express_sms, int *other_sms);
 /* A and B must stay valid until the request is done.  Returns at once;
  * admission (and a BRM_ERR_CAPACITY rejection) follows asynchronously. */
 int brm_server_submit(brm_server srv, brm_dtype dtype, const brm_csr *A, const brm_csr *B,

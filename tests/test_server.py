@@ -131,16 +131,18 @@ def test_server_rejects_invalid_columns_at_admission():
     ctx.close()
 
 
-@pytest.mark.parametrize("express", [0, 2])
-def test_server_express_workers_same_results(oracle_mod, express):
-    """With no express workers, or with two beside one general worker, every
-    result is the same as alone; small and large requests are mixed."""
+@pytest.mark.parametrize("express,sms", [(0, 0), (2, 0), (1, -1), (1, 32)])
+def test_server_express_workers_same_results(oracle_mod, express, sms):
+    """With no express workers, with two beside one general worker (on an SM
+    partition of their own where the driver offers one), with an express
+    worker on shared SMs, and with a 32-SM express partition: every result
+    is the same as alone; small and large requests are mixed."""
     import torch
     reqs = _requests(31, 24)
     dev = [(brm.DeviceCSR.from_host(A), brm.DeviceCSR.from_host(B)) for A, B in reqs]
     ctx = brm.Context()
     alone = [ctx.precise_device(a, b).to_host() for a, b in dev]
-    srv = brm.Server(workers=1, express_workers=express, express_bytes=8 << 20)
+    srv = brm.Server(workers=1, express_workers=express, express_bytes=8 << 20, express_sms=sms)
     tickets = [srv.submit(a, b) for a, b in dev]
     for i, t in enumerate(tickets):
         C, _ = srv.wait(t, timeout=120.0)
