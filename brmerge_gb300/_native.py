@@ -119,6 +119,9 @@ def lib() -> C.CDLL:
         _decl(L.brm_set_validate, C.c_int, [vp, C.c_int])
         _decl(L.brm_last_device_error, C.c_int, [vp])
         _decl(L.brm_device_code_version, C.c_int, [c_int_p])
+        _decl(L.brm_checked_build, C.c_int, [])
+        _decl(L.brm_last_check_failure, C.c_int,
+              [vp, c_int_p, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)])
         _decl(L.brm_symbolic, C.c_int, [vp, csrp, csrp, vp, c_int_p])
         _decl(L.brm_numeric, C.c_int, [vp, C.c_int, csrp, csrp, vp, vp, vp])
         _decl(L.brm_precise_device, C.c_int,

@@ -109,14 +109,21 @@ def build_host() -> Path:
     return out
 
 
-def build(verbose: bool = False) -> None:
+def build(verbose: bool = False, checked: bool | None = None) -> None:
+    """Builds both libraries.  checked (default: the BRM_CHECKED environment
+    variable) compiles the device code with -DBRM_CHECKED: every
+    data-dependent index is checked against its bound, a failing access is
+    skipped and reported through the device error word (brm_checked_build,
+    brm_last_check_failure); a change of mode rebuilds every object."""
+    if checked is None:
+        checked = os.environ.get("BRM_CHECKED", "") not in ("", "0")
     with cf.ThreadPoolExecutor(max_workers=2) as ex:
-        f1 = ex.submit(build_cuda, verbose)
+        f1 = ex.submit(build_cuda, verbose, ["-DBRM_CHECKED"] if checked else None)
         f2 = ex.submit(build_host)
         f1.result()
         f2.result()
 
 
 if __name__ == "__main__":
-    build(verbose="-v" in sys.argv)
+    build(verbose="-v" in sys.argv, checked=True if "--checked" in sys.argv else None)
     print("built", PKG / "libbrmerge.so", PKG / "libbrm_host.so")

@@ -2,6 +2,7 @@
 #include <algorithm>
 #include <climits>
 
+#include "brm_check.cuh"
 #include "brm_common.cuh"
 #include "brm_kernels.h"
 
@@ -251,7 +252,8 @@ __global__ void __launch_bounds__(kAnaThreads) k_analyze(CsrDev A, CsrDev B, Pla
                 // the planning takes these first, so the longest rows do not
                 // start last and finish after every other block
                 const int h = atomicAdd(&P.cnt->n_huge, 1);
-                P.rows[(size_t)kBinHeavy * M + (M - 1 - h)] = row;
+                if (BRM_IN(P.cnt, M - 1 - h, M))
+                    P.rows[(size_t)kBinHeavy * M + (M - 1 - h)] = row;
                 bin = -2;
             }
             s_bin[slot] = bin;
@@ -287,7 +289,7 @@ __global__ void __launch_bounds__(kAnaThreads) k_analyze(CsrDev A, CsrDev B, Pla
     __syncthreads();
     for (int slot = threadIdx.x; slot < RPB; slot += kAnaThreads) {
         int bin = s_bin[slot];
-        if (bin > kBinEmpty && bin != kBinBatch)
+        if (bin > kBinEmpty && bin != kBinBatch && BRM_IN(P.cnt, s_base[bin] + s_idx[slot], M))
             P.rows[(size_t)bin * M + s_base[bin] + s_idx[slot]] =
                 LISTED ? P.longk_rows[row0 + slot] : row0 + slot;
     }
@@ -441,7 +443,7 @@ void launch_scan_i64(const int *in, long long *out, int n, void *tmp, cudaStream
 template <typename T>
 __global__ void __launch_bounds__(256) k_compact(int M, const long long *scan_flop, const int *len,
                                                  const int *bar_col, const T *bar_val,
-                                                 const int *crpt, int *ccol, T *cval)
+                                                 const int *crpt, int *ccol, T *cval, Counters *cnt)
 {
     const int lane = threadIdx.x & 31;
     const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -449,7 +451,10 @@ __global__ void __launch_bounds__(256) k_compact(int M, const long long *scan_fl
     for (int row = gw; row < M; row += nw) {
         const long long src = scan_flop[row];
         const int dst = crpt[row];
-        const int n = len[row];
+        int n = len[row];
+        if (n > 0 && !(BRM_IN(cnt, (long long)dst + n - 1, crpt[M]) &&
+                       BRM_IN(cnt, src + n - 1, (long long)cnt->total_flop)))
+            n = 0;  // checked build: a row outside C or C_bar is skipped
         for (int q = lane; q < n; q += 32) {
             ccol[dst + q] = bar_col[src + q];
             cval[dst + q] = bar_val[src + q];
@@ -467,11 +472,13 @@ void launch_compact(int dtype, const PlanDev &P, const int *bar_col, const void 
         grid = 65535 * 4;
     if (dtype == 0) {
         k_compact<double><<<grid, 256, 0, s>>>(P.M, P.scan_flop, P.nnz, bar_col,
-                                                (const double *)bar_val, crpt, ccol, (double *)cval);
+                                                (const double *)bar_val, crpt, ccol, (double *)cval,
+                                                P.cnt);
         count_launch();
     } else {
         k_compact<float><<<grid, 256, 0, s>>>(P.M, P.scan_flop, P.nnz, bar_col,
-                                               (const float *)bar_val, crpt, ccol, (float *)cval);
+                                               (const float *)bar_val, crpt, ccol, (float *)cval,
+                                               P.cnt);
         count_launch();
     }
 }

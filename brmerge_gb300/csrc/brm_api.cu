@@ -14,6 +14,7 @@
 #include <cstring>
 #include <mutex>
 
+#include "brm_check.cuh"
 #include "brm_hostpool.h"
 #include "brm_kernels.h"
 #include "brmerge.h"
@@ -404,6 +405,7 @@ int plan_phase(brm_context ctx, const brm_csr *A, const brm_csr *B, int *crpt, b
         BRM_TRY(grow(ctx, ctx->midbuf, b_col + vsize((brm_dtype)fused_dtype) * n));
         ctx->mid_col = (int *)ctx->midbuf.p;
         ctx->mid_val = (unsigned char *)ctx->midbuf.p + b_col;
+        P.mid_cap = ctx->plan.mid_cap = (long long)n;
     }
     {
         const size_t cap = (size_t)ctx->h_cnt->seg_cap + 1;
@@ -494,8 +496,9 @@ size_t long_bytes(long long elems, brm_dtype dtype)
 // the capacities of a captured pipeline (whose buffers are grown ahead).
 struct NumSizes {
     unsigned long long table_cap = 0;    // split-table entries
-    unsigned long long total_flop = 0;   // products (long-column scratch)
+    unsigned long long total_flop = 0;   // products (long-column scratch, C_bar of Upper)
     unsigned long long spill_bytes = 0;  // spill scratch
+    long long c_cap = 0;                 // entries of C (Precise)
 };
 
 NumSizes planned_sizes(brm_context ctx)
@@ -504,6 +507,7 @@ NumSizes planned_sizes(brm_context ctx)
     z.table_cap = ctx->h_cnt->table_cap;
     z.total_flop = ctx->h_cnt->total_flop;
     z.spill_bytes = ctx->spill_bytes;
+    z.c_cap = ctx->h_cnt->cnnz;
     return z;
 }
 
@@ -520,6 +524,7 @@ int numeric_launch(brm_context ctx, brm_dtype dtype, bool upper, const brm_csr *
     brm::PlanDev P = ctx->plan;
     P.r_lo = part.r_lo;
     P.r_hi = part.r_hi < 0 ? A->M : part.r_hi;
+    P.c_cap = upper ? (long long)sz.total_flop : sz.c_cap;
     P.seg_range = part.seg_range;
     if (part.seg_list)
         P.seg_list = (int *)part.seg_list;
@@ -566,6 +571,13 @@ int read_err(brm_context ctx)
     BRM_CK(cudaMemcpyAsync(&ctx->h_cnt->err, &ctx->plan.cnt->err, sizeof(int),
                            cudaMemcpyDeviceToHost, ctx->stream));
     BRM_CK(cudaStreamSynchronize(ctx->stream));
+    if (ctx->h_cnt->err & brm::kErrChecked) {  // where the checked build stopped an access
+        BRM_CK(cudaMemcpyAsync(&ctx->h_cnt->chk_line, &ctx->plan.cnt->chk_line,
+                               offsetof(brm::Counters, chk_bound) + sizeof(long long) -
+                                   offsetof(brm::Counters, chk_line),
+                               cudaMemcpyDeviceToHost, ctx->stream));
+        BRM_CK(cudaStreamSynchronize(ctx->stream));
+    }
     ctx->last_err = ctx->h_cnt->err;
     return device_err_status(ctx->h_cnt->err);
 }
@@ -929,6 +941,7 @@ int brm::reserve_pipe(brm_context ctx, brm_dtype dtype, const brm::PipeCaps &c)
         BRM_TRY(grow(ctx, ctx->midbuf, b_col + vsize(dtype) * n));
         ctx->mid_col = (int *)ctx->midbuf.p;
         ctx->mid_val = (unsigned char *)ctx->midbuf.p + b_col;
+        ctx->plan.mid_cap = (long long)n;
     }
     BRM_TRY(grow(ctx, ctx->splitbuf, ((size_t)c.table + 1) * sizeof(int)));
     BRM_TRY(grow(ctx, ctx->longbuf, long_bytes(std::min<long long>(c.products, ctx->long_scratch), dtype)));
@@ -984,6 +997,7 @@ int brm::precise_pipe(brm_context ctx, brm_dtype dtype, const brm_csr *A, const 
     z.table_cap = (unsigned long long)caps.table;
     z.total_flop = (unsigned long long)caps.products;
     z.spill_bytes = (unsigned long long)caps.spill_bytes;
+    z.c_cap = caps.products;
     // the plan's error bits (capacity, bad input) must survive the numeric phase
     return numeric_launch(ctx, dtype, false, A, B, crpt, ccol, cval, true, RowPart(), false, &z);
 }
@@ -1224,6 +1238,19 @@ int brm_autotune(brm_context ctx, brm_dtype dtype, int n, const brm_csr *A, cons
 }
 
 int brm_last_device_error(brm_context ctx) { return ctx ? ctx->last_err : -1; }
+
+int brm_checked_build(void) { return brm::kCheckedBuild ? 1 : 0; }
+
+int brm_last_check_failure(brm_context ctx, int *line, long long *index, long long *bound)
+{
+    if (!ctx || !line || !index || !bound)
+        return BRM_ERR_INVALID_VALUE;
+    const bool failed = (ctx->last_err & brm::kErrChecked) != 0;
+    *line = failed ? ctx->h_cnt->chk_line : 0;
+    *index = failed ? ctx->h_cnt->chk_idx : 0;
+    *bound = failed ? ctx->h_cnt->chk_bound : 0;
+    return BRM_SUCCESS;
+}
 
 int brm_symbolic(brm_context ctx, const brm_csr *A, const brm_csr *B, int *crpt, int *cnnz)
 {

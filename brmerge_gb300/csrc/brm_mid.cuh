@@ -25,6 +25,7 @@
 
 #include <climits>
 
+#include "brm_check.cuh"
 #include "brm_common.cuh"
 #include "brm_plan.h"
 #include "brm_rows.cuh"
@@ -460,8 +461,9 @@ __global__ void __launch_bounds__(kMidThreads) k_mid_numeric(CsrDev A, CsrDev B,
 #pragma unroll
                 for (int i = 0; i < kGatherBatch; i++) {
                     if (i < n) {
-                        c[i] = bcol[addr[i]];
-                        bv[i] = bval[addr[i]];
+                        const bool in = BRM_IN(P.cnt, addr[i], B.nnz);
+                        c[i] = in ? bcol[addr[i]] : 0;
+                        bv[i] = in ? bval[addr[i]] : T(0);
                         av[i] = aval[t.s_a0[t.lslot[lid[i]]] + t.lleaf[lid[i]]];
                     }
                 }
@@ -574,8 +576,10 @@ __global__ void __launch_bounds__(kMidThreads) k_mid_numeric(CsrDev A, CsrDev B,
                         v = sr.finish();
                     }
                 }
-                ccol[o] = col[e];
-                cval[o] = v;
+                if (BRM_IN(P.cnt, o, SCRATCH ? P.mid_cap : P.c_cap)) {
+                    ccol[o] = col[e];
+                    cval[o] = v;
+                }
                 h++;
             }
         }
@@ -654,7 +658,9 @@ __global__ void __launch_bounds__(256) k_mid_compact(PlanDev P, int M, const int
             src = P.mid_pre[row];
         }
         const long long dst = crpt[row];
-        const int n = P.nnz[row];
+        int n = P.nnz[row];
+        if (n > 0 && !(BRM_IN(P.cnt, dst + n - 1, P.c_cap) && BRM_IN(P.cnt, src + n - 1, P.mid_cap)))
+            n = 0;  // checked build: a row outside C or the scratch is skipped
         // four elements per lane in flight before the stores
         int i = lane;
         for (; i + 96 < n; i += 128) {

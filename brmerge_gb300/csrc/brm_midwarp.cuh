@@ -28,6 +28,7 @@
 
 #include <climits>
 
+#include "brm_check.cuh"
 #include "brm_common.cuh"
 #include "brm_mid.cuh"
 #include "brm_plan.h"
@@ -282,7 +283,7 @@ __device__ __forceinline__ void mw_reduce_balanced(const unsigned *key, const un
                                                    const unsigned short *loff,
                                                    const T *__restrict__ arow,
                                                    const T *__restrict__ bval, int cmin, int *ccol,
-                                                   T *cval)
+                                                   T *cval, Counters *cnt, long long bnnz)
 {
     constexpr unsigned imask = (1u << IDX) - 1u;
     // first run that starts at or after product q (len if none)
@@ -316,7 +317,8 @@ __device__ __forceinline__ void mw_reduce_balanced(const unsigned *key, const un
                 const int e = (int)(key[p0 + q] & imask);
                 const int j = plist[e];
                 lf[q] = lleaf[j];
-                v[q] = vmul(arow[lf[q]], bval[lbs[j] + (e - loff[j])]);
+                const long long bi = (long long)lbs[j] + (e - loff[j]);
+                v[q] = BRM_IN(cnt, bi, bnnz) ? vmul(arow[lf[q]], bval[bi]) : T(0);
             }
         }
 #pragma unroll
@@ -425,7 +427,8 @@ __global__ void __launch_bounds__(mw_threads<SID>(), 2) k_mid_warp(CsrDev A, Csr
                     if (e < F) {
                         while (e >= loff[j + 1])
                             j++;
-                        c[u] = bcol[lbs[j] + (e - loff[j])];
+                        const long long bi = (long long)lbs[j] + (e - loff[j]);
+                        c[u] = BRM_IN(P.cnt, bi, B.nnz) ? bcol[bi] : cmin;
                     }
                     jj[u] = j;
                 }
@@ -492,14 +495,21 @@ __global__ void __launch_bounds__(mw_threads<SID>(), 2) k_mid_warp(CsrDev A, Csr
         }
         if ((MODE == kMwUpper || MODE == kMwScratch) && t == 0)
             P.nnz[row] = len;
+        // the row's output must lie inside C (or the scratch): checked build
+        if (!BRM_IN(P.cnt, base + len - 1, MODE == kMwScratch ? P.mid_cap : P.c_cap)) {
+            grp_sync<G>(gid);
+            continue;
+        }
         // gathers in flight: two runs a thread within 80 registers, four
         // with 128
         if (k <= 32)
             mw_reduce_balanced<T, NT, IDX, 6, 4>(src, dst, len, F, t, plist, lleaf, lbs, loff,
-                                                 aval + a0, bval, cmin, ccol + base, cval + base);
+                                                 aval + a0, bval, cmin, ccol + base, cval + base,
+                                                 P.cnt, B.nnz);
         else
             mw_reduce_balanced<T, NT, IDX, 9, 4>(src, dst, len, F, t, plist, lleaf, lbs, loff,
-                                                 aval + a0, bval, cmin, ccol + base, cval + base);
+                                                 aval + a0, bval, cmin, ccol + base, cval + base,
+                                                 P.cnt, B.nnz);
         grp_sync<G>(gid);
     }
 }
@@ -628,7 +638,8 @@ __global__ void __launch_bounds__(kMwThreads, 2) k_mid_tile(CsrDev A, CsrDev B, 
                     else
                         hi = m - 1;
                 }
-                const int c = bcol[lbs[lo] + (i - loff[lo])];
+                const long long bi = (long long)lbs[lo] + (i - loff[lo]);
+                const int c = BRM_IN(P.cnt, bi, B.nnz) ? bcol[bi] : cmin;
                 key[q] = ((unsigned)(c - cmin) << IDX) | (unsigned)i;
                 plist[i] = (unsigned char)lo;
             }
@@ -717,14 +728,17 @@ __global__ void __launch_bounds__(kMwThreads, 2) k_mid_tile(CsrDev A, CsrDev B, 
             P.nnz[row] = len;
         const T *arow = aval + a0;
         constexpr unsigned imask = (1u << IDX) - 1u;
-        for (int h = lt; h < len; h += TW) {
+        // the row's output must lie inside C (or the scratch): checked build
+        const bool out_in = BRM_IN(P.cnt, base + len - 1, MODE == kMwScratch ? P.mid_cap : P.c_cap);
+        for (int h = out_in ? lt : len; h < len; h += TW) {
             const int p = (int)shead[h], m = (int)shead[h + 1] - p;
             const unsigned *run = skey + p;
             auto leaf = [&](int i) { return (int)lleaf[plist[run[i] & imask]]; };
             auto val = [&](int i) {
                 const int e = (int)(run[i] & imask);
                 const int j = plist[e];
-                return vmul(arow[lleaf[j]], bval[lbs[j] + (e - loff[j])]);
+                const long long bi = (long long)lbs[j] + (e - loff[j]);
+                return BRM_IN(P.cnt, bi, B.nnz) ? vmul(arow[lleaf[j]], bval[bi]) : T(0);
             };
             const T v = k <= 32 ? mw_run_value<T, 6>(m, leaf, val) : mw_run_value<T, 9>(m, leaf, val);
             ccol[base + h] = cmin + (int)(run[0] >> IDX);

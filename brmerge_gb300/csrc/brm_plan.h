@@ -83,6 +83,7 @@ enum DevErr : int {
     kErrOverflow = 8,        // an int32 quantity overflowed
     kErrBadInput = 16,       // an index out of range seen by a kernel
     kErrCapacity = 32,       // a batch exceeded a captured pipeline's capacities
+    kErrChecked = 64,        // a bounds check of the checked build failed (brm_check.cuh)
 };
 
 // Row classes assigned by the analysis kernel.
@@ -131,6 +132,10 @@ struct Counters {
     // does not fit its buffers; every kernel that writes at data-dependent
     // offsets then returns at once (the call reports BRM_ERR_CAPACITY)
     int abort;
+    // first failed bounds check of the checked build: source line, index, bound
+    int chk_line;
+    long long chk_idx;
+    long long chk_bound;
 };
 
 // Descriptor slots reserved for a heavy row with F products and the cut
@@ -233,6 +238,11 @@ struct PlanDev {
     // policy knobs (see kMinSegCut): heavy-row cut target, mid-row weight limit
     int seg_cut;
     int mid_limit;
+    // entries of the arrays the numeric kernels write (C, or C_bar for
+    // Upper) and of the one-call mid-row scratch; the bounds of the checked
+    // build
+    long long c_cap;
+    long long mid_cap;
     Counters *cnt;
 };
 

@@ -25,6 +25,7 @@
 
 #include <climits>
 
+#include "brm_check.cuh"
 #include "brm_common.cuh"
 #include "brm_plan.h"
 
@@ -583,8 +584,10 @@ __device__ __forceinline__ void numeric_row(const CsrDev &A, const CsrDev &B, co
                     }
                 }
                 const long long o = out_base + written + u;
-                ccol[o] = ocol[u];
-                cval[o] = v;
+                if (BRM_IN(P.cnt, o, P.c_cap)) {
+                    ccol[o] = ocol[u];
+                    cval[o] = v;
+                }
             }
             written += Uw;
             {
@@ -779,8 +782,10 @@ __global__ void __launch_bounds__(256) k_warp_numeric(CsrDev A, CsrDev B, PlanDe
         const long long base = UPPER ? P.scan_flop[row] : (long long)crpt[row];
         if (active) {
             const long long o = base + __popc(outm & lanemask_lt());
-            ccol[o] = c;
-            cval[o] = v;
+            if (BRM_IN(P.cnt, o, P.c_cap)) {
+                ccol[o] = c;
+                cval[o] = v;
+            }
         }
         if (lane == 0) {
             if (UPPER)
@@ -814,8 +819,12 @@ __global__ void __launch_bounds__(256) k_copy_numeric(CsrDev A, CsrDev B, PlanDe
         const int j = A.rpt[row] + P.copy_leaf[row];
         const int b = A.col[j];
         const T a = ((const T *)A.val)[j];
-        const int s = B.rpt[b], len = B.rpt[b + 1] - s;
+        const int s = B.rpt[b];
+        int len = B.rpt[b + 1] - s;
         const long long base = UPPER ? P.scan_flop[row] : (long long)crpt[row];
+        if (len > 0 && !(BRM_IN(P.cnt, base + len - 1, P.c_cap) &&
+                         BRM_IN(P.cnt, (long long)s + len - 1, B.nnz)))
+            len = 0;  // checked build: a row outside C or B is skipped
         const int *__restrict__ bcol = B.col;
         const T *__restrict__ bval = (const T *)B.val;
         // four elements per lane in flight before the stores
@@ -931,7 +940,7 @@ __global__ void __launch_bounds__(32) k_spill_numeric(CsrDev A, CsrDev B, PlanDe
         }
         const int len = nl == 1 ? lo[src][1] : 0;
         const long long ob = UPPER ? P.scan_flop[row] : (long long)crpt[row];
-        for (int q = 0; q < len; q++) {
+        for (int q = 0; q < (len > 0 && BRM_IN(P.cnt, ob + len - 1, P.c_cap) ? len : 0); q++) {
             ccol[ob + q] = col[src][q];
             cval[ob + q] = val[src][q];
         }

@@ -36,6 +36,7 @@
 
 #include <climits>
 
+#include "brm_check.cuh"
 #include "brm_common.cuh"
 #include "brm_mid.cuh"
 #include "brm_plan.h"
@@ -379,12 +380,14 @@ __global__ void __launch_bounds__(kPlanThreads) k_heavy_plan(CsrDev A, CsrDev B,
                     plan_group_starts(g, h, ph, run,
                                       h > dense ? ccnt + dix[g] * kPlanGroupBits : ccnt, cut,
                                       dense, [&](int c, unsigned pe, unsigned ue) {
-                                          SegDesc &d = P.seg[base + nseg + r];
-                                          d.row = row;
-                                          d.c_lo = lo + kPlanGroupBits * g + c;
-                                          d.u_off = (int)(u_chunk + (long long)ue);
-                                          d.bidx = nseg + r;
-                                          d.nprod = (int)pe;  // prefix; a count below
+                                          if (BRM_IN(P.cnt, base + nseg + r, P.cnt->seg_cap)) {
+                                              SegDesc &d = P.seg[base + nseg + r];
+                                              d.row = row;
+                                              d.c_lo = lo + kPlanGroupBits * g + c;
+                                              d.u_off = (int)(u_chunk + (long long)ue);
+                                              d.bidx = nseg + r;
+                                              d.nprod = (int)pe;  // prefix; a count below
+                                          }
                                           r++;
                                       });
                     run += ((unsigned long long)h << 32) | (unsigned)gpop[g];
@@ -445,8 +448,11 @@ __global__ void __launch_bounds__(kPlanThreads) k_heavy_plan(CsrDev A, CsrDev B,
                 (long long)(((unsigned long long)(unsigned)misc[3] << 32) | (unsigned)misc[2]);
             const int lpos = misc[1];
             for (int i = tid; i < nseg; i += NT) {
-                P.seg[base + i].tab = tab;
-                P.seg_list[lpos + i] = (int)(base + i);
+                if (BRM_IN(P.cnt, base + i, P.cnt->seg_cap) &&
+                    BRM_IN(P.cnt, lpos + i, P.cnt->seg_cap)) {
+                    P.seg[base + i].tab = tab;
+                    P.seg_list[lpos + i] = (int)(base + i);
+                }
             }
         }
         __syncthreads();
@@ -492,8 +498,9 @@ __global__ void __launch_bounds__(256) k_split(CsrDev A, CsrDev B, PlanDev P)
         for (int l = threadIdx.x; l < k; l += blockDim.x) {
             const int s = P.abs[a0 + l];
             const int e = s + P.alen[a0 + l];
-            t0[l] = (b == 0) ? s : lower_bound_idx(bcol, s, e, c_lo);
-            if (b == nseg - 1)
+            if (BRM_IN(P.cnt, tab + (long long)b * k + l, P.cnt->table_cap))
+                t0[l] = (b == 0) ? s : lower_bound_idx(bcol, s, e, c_lo);
+            if (b == nseg - 1 && BRM_IN(P.cnt, tab + (long long)(b + 1) * k + l, P.cnt->table_cap))
                 t0[k + l] = e;
         }
     }
@@ -705,8 +712,9 @@ __global__ void __launch_bounds__(kSegThreads, 512 / kSegThreads) k_seg_numeric(
 #pragma unroll
                 for (int i = 0; i < kGatherBatch; i++) {
                     if (i < n) {
-                        c[i] = bcol[addr[i]];
-                        bv[i] = bval[addr[i]];
+                        const bool in = BRM_IN(P.cnt, addr[i], B.nnz);
+                        c[i] = in ? bcol[addr[i]] : d.c_lo;
+                        bv[i] = in ? bval[addr[i]] : T(0);
                         av[i] = aval[a0 + lleaf[lid[i]]];
                     }
                 }
@@ -821,7 +829,7 @@ __global__ void __launch_bounds__(kSegThreads, 512 / kSegThreads) k_seg_numeric(
             const int ci = flat ? rc >> 5 : pu[p];
             const int u = cwr[ci] + __popc(cw[ci] & ((1u << (rc & 31)) - 1u));
             pu[p] = (unsigned short)u;
-            if (!nodup)
+            if (!nodup && BRM_IN(P.cnt, u, U))
                 ia[p] = (unsigned short)atomicAdd(&ucnt[u], 1);
         }
         __syncthreads();
@@ -830,7 +838,8 @@ __global__ void __launch_bounds__(kSegThreads, 512 / kSegThreads) k_seg_numeric(
         if (nodup) {
             // every column has one contribution: position u holds product e
             for (int p = p0; p < p1; p++)
-                S[pu[p]] = (unsigned short)p;
+                if (BRM_IN(P.cnt, pu[p], nprod))
+                    S[pu[p]] = (unsigned short)p;
         } else {
             // exclusive scan of the column counts (in place), then scatter
             const int cpt = (U + NT - 1) / NT;
@@ -849,7 +858,8 @@ __global__ void __launch_bounds__(kSegThreads, 512 / kSegThreads) k_seg_numeric(
                 ucnt[U] = nprod;
             __syncthreads();
             for (int p = p0; p < p1; p++)
-                S[ucnt[pu[p]] + ia[p]] = (unsigned short)p;
+                if (BRM_IN(P.cnt, ucnt[pu[p]] + ia[p], nprod))
+                    S[ucnt[pu[p]] + ia[p]] = (unsigned short)p;
         }
         __syncthreads();
         // one thread per output column of one or two products (consecutive
@@ -883,8 +893,10 @@ __global__ void __launch_bounds__(kSegThreads, 512 / kSegThreads) k_seg_numeric(
                     longu[li] = (unsigned short)u;
                 continue;
             }
-            ccol[obase + u] = d.c_lo + prc[e0];
-            cval[obase + u] = v;
+            if (BRM_IN(P.cnt, obase + u, P.c_cap)) {
+                ccol[obase + u] = d.c_lo + prc[e0];
+                cval[obase + u] = v;
+            }
         }
         __syncthreads();
         const int n34 = misc[3], nmid = n34 + misc[4];
@@ -938,8 +950,10 @@ __global__ void __launch_bounds__(kSegThreads, 512 / kSegThreads) k_seg_numeric(
                         sr.push(l8[j], v8[j]);
                 v = sr.finish();
             }
-            ccol[obase + u] = d.c_lo + prc[e0];
-            cval[obase + u] = v;
+            if (BRM_IN(P.cnt, obase + u, P.c_cap)) {
+                ccol[obase + u] = d.c_lo + prc[e0];
+                cval[obase + u] = v;
+            }
         }
         __syncthreads();
         // columns with more than eight products: one warp each puts them in
@@ -1008,7 +1022,8 @@ __global__ void __launch_bounds__(kSegThreads, 512 / kSegThreads) k_seg_numeric(
                         P.long_leaf[leo + r] = pleaf[p];
                         lval[leo + r] = pval[p];
                     } else {
-                        ia[i0 + r] = (unsigned short)p;
+                        if (BRM_IN(P.cnt, i0 + r, nprod))
+                            ia[i0 + r] = (unsigned short)p;
                     }
                 }
                 if (lci < P.long_cap_cols && lane == 0) {
@@ -1026,16 +1041,20 @@ __global__ void __launch_bounds__(kSegThreads, 512 / kSegThreads) k_seg_numeric(
                     const int e = ia[i0 + (lane < len ? lane : 0)];
                     const T r = warp_trie<T>(pleaf[e], pval[e], len);
                     if (lane == 0) {
-                        ccol[obase + u] = d.c_lo + prc[e];
-                        cval[obase + u] = r;
+                        if (BRM_IN(P.cnt, obase + u, P.c_cap)) {
+                            ccol[obase + u] = d.c_lo + prc[e];
+                            cval[obase + u] = r;
+                        }
                     }
                 } else if (lane == 0) {
                     ShiftReduce<T, 17> sr;
                     sr.init(pleaf[ia[i0]], pval[ia[i0]]);
                     for (int i = i0 + 1; i < i1; i++)
                         sr.push(pleaf[ia[i]], pval[ia[i]]);
-                    ccol[obase + u] = d.c_lo + prc[ia[i0]];
-                    cval[obase + u] = sr.finish();
+                    if (BRM_IN(P.cnt, obase + u, P.c_cap)) {
+                        ccol[obase + u] = d.c_lo + prc[ia[i0]];
+                        cval[obase + u] = sr.finish();
+                    }
                 }
                 __syncwarp();
               }
@@ -1148,14 +1167,19 @@ __global__ void __launch_bounds__(128) k_long_reduce(PlanDev P, int *ccol, T *cv
         c.len = 0;
         if (i < n)
             c = P.long_col[i];
+        if (c.len > 0 && !BRM_IN(P.cnt, c.off + c.len - 1, P.long_cap_elems))
+            c.len = 0;  // checked build: a record outside the scratch is skipped
         const int last = c.len > 0 ? (int)lleaf[c.off + c.len - 1] : 0;
         const bool mine = c.len > 0 && long_by_thread(c, last);
         // the stack depth follows the warp's largest last leaf
         const int top = __reduce_max_sync(kFull, mine ? last : 0);
         if (mine) {
-            ccol[c.out] = c.col;
-            cval[c.out] = top < 256 ? long_run<T, 9>(lleaf, lval, c.off, c.off + c.len)
+            if (BRM_IN(P.cnt, c.out, P.c_cap) &&
+                BRM_IN(P.cnt, c.off + c.len - 1, P.long_cap_elems)) {
+                ccol[c.out] = c.col;
+                cval[c.out] = top < 256 ? long_run<T, 9>(lleaf, lval, c.off, c.off + c.len)
                                     : long_run<T, 13, 4>(lleaf, lval, c.off, c.off + c.len);
+            }
         }
     }
 }
@@ -1178,6 +1202,8 @@ __global__ void __launch_bounds__(128) k_long_warp(PlanDev P, int *ccol, T *cval
         c.len = 0;
         if (i < n)
             c = P.long_col[i];
+        if (c.len > 0 && !BRM_IN(P.cnt, c.off + c.len - 1, P.long_cap_elems))
+            c.len = 0;  // checked build: a record outside the scratch is skipped
         const int last = c.len > 0 ? (int)lleaf[c.off + c.len - 1] : 0;
         unsigned lm = __ballot_sync(kFull, c.len > 0 && !long_by_thread(c, last));
         while (lm) {
@@ -1187,8 +1213,11 @@ __global__ void __launch_bounds__(128) k_long_warp(PlanDev P, int *ccol, T *cval
             const int len = __shfl_sync(kFull, c.len, src);
             const T r = warp_long_column<T>(lleaf, lval, off, len, s_cnt[wid], s_val[wid]);
             if (lane == src) {
-                ccol[c.out] = c.col;
-                cval[c.out] = r;
+                if (BRM_IN(P.cnt, c.out, P.c_cap) &&
+                    BRM_IN(P.cnt, c.off + c.len - 1, P.long_cap_elems)) {
+                    ccol[c.out] = c.col;
+                    cval[c.out] = r;
+                }
             }
         }
     }

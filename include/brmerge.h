@@ -152,6 +152,16 @@ int brm_autotune(brm_context ctx, brm_dtype dtype, int n, const brm_csr *A, cons
  * (cudaFuncAttributes.binaryVersion: 103 for the sm_103a build).
  * Diagnostics; no counterpart in the reference. */
 int brm_device_code_version(int *sm);
+/* 1 when the library was built with -DBRM_CHECKED: the device code then
+ * checks the index of every data-dependent access (writes into C and the
+ * scratch arrays, computed shared-memory slots, gathers from B) against its
+ * bound, skips a failing access, and the call returns BRM_ERR_INTERNAL; the
+ * first failure's source line (in the library's kernel sources), index and
+ * bound are reported by brm_last_check_failure (all 0 when none failed).
+ * Diagnostics for testing the kernels without a sanitizer; no counterpart
+ * in the reference. */
+int brm_checked_build(void);
+int brm_last_check_failure(brm_context ctx, int *line, long long *index, long long *bound);
 /* Device-side error bits of the last call on this context (diagnostics). */
 int brm_last_device_error(brm_context ctx);
 const char *brm_status_string(int status);
