@@ -969,6 +969,14 @@ def run_ours(args):
     upper = method_entry(up_ms, products, alg_bytes, peak)
     upper["verified_vs_precise"] = same_csr(Cu.to_host(), Cref)
     del Cu
+    # the split path (brm_symbolic + brm_numeric): a structure-only symbolic
+    # pass, then the values written straight into C -- the A/B of the
+    # one-call form, which computes the mid rows during planning and moves
+    # them into C afterwards
+    sp_ms, Csp = device_steps(lambda: ctx.precise(dA, dA), dev, stream, flush, args.steps)
+    split = method_entry(sp_ms, products, alg_bytes, peak)
+    split["verified_vs_precise"] = same_csr(Csp.to_host(), Cref)
+    del Csp
     # the hash SpGEMM comparator: same structure, values in hardware order
     h_ms, Chs = device_steps(lambda: ctx.hash_device(dA, dA), dev, stream, flush, args.steps)
     hashc = method_entry(h_ms, products, alg_bytes, peak)
@@ -1031,12 +1039,14 @@ def run_ours(args):
         "gpu_launches": int(launches),
     }
     line["upper"] = dict(upper, call="brm_upper_device (one call)")
+    line["split_path"] = dict(split, call="brm_symbolic + brm_numeric (no mid-row scratch)")
     line["hash_comparator"] = dict(hashc, call="brm_hash_device (values not in merge order)")
     if cpu is not None:
         line["cpu_baseline"] = cpu
     line.update(side)
     checks = {"precise_vs_oracle": precise_ok, "e2e_vs_precise": e2e_ok,
               "upper_vs_precise": upper["verified_vs_precise"],
+              "split_vs_precise": split["verified_vs_precise"],
               "hash_vs_precise_1e-9": hashc["verified_vs_precise_1e-9"]}
     for k, v in side.items():
         if isinstance(v, dict) and "verified" in v:
