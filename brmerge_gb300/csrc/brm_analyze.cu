@@ -179,8 +179,8 @@ __global__ void __launch_bounds__(kAnaThreads) k_analyze(CsrDev A, CsrDev B, Pla
         else if (f <= kMg2F && a1 - a0 <= kMidMaxK)  // unless the column range is too wide
             bin = f <= kMtF    ? kBinMidTile
                   : f <= kMt2F ? kBinMidTile2
-                  : f <= kMwF  ? kBinMidWarp
-                  : f <= kMgF  ? kBinMidGroup
+                  : (f <= kMwF && a1 - a0 <= kMwMaxK) ? kBinMidWarp
+                  : (f <= kMgF && a1 - a0 <= kMwMaxK) ? kBinMidGroup
                                : kBinMidGroup2;
         else if (f <= P.mid_limit && 2 * nl <= P.mid_limit && a1 - a0 <= kMidMaxK)
             bin = kBinBatch;

@@ -1,6 +1,6 @@
 // brm_midwarp.cuh -- one warp (or four) per mid row: merged product keys, no block barriers.
 //
-// Rows with at most kMgF products (and at most kMidMaxK A entries, a column
+// Rows with at most kMg2F products (and at most kMidMaxK A entries, a column
 // range below 2^kMwRangeBits / 2^kMgRangeBits) are the bulk of regular
 // products (a 27-point stencil squared: 729 products, 27 lists, 125 outputs
 // per row) and of uneven batches.  A warp (rows up to kMwF products) or a
@@ -51,6 +51,7 @@ struct MwShape<1> {
     static constexpr int RANGE = kMwRangeBits;
     static constexpr int GROUPS = 12;
     static constexpr int BIN = kBinMidWarp;
+    static constexpr int KMAX = kMwMaxK;
 };
 template <>
 struct MwShape<4> {
@@ -60,6 +61,7 @@ struct MwShape<4> {
     static constexpr int RANGE = kMgRangeBits;
     static constexpr int GROUPS = 3;
     static constexpr int BIN = kBinMidGroup;
+    static constexpr int KMAX = kMwMaxK;
 };
 template <>
 struct MwShape<5> {
@@ -69,6 +71,7 @@ struct MwShape<5> {
     static constexpr int RANGE = kMg2RangeBits;
     static constexpr int GROUPS = 2;
     static constexpr int BIN = kBinMidGroup2;
+    static constexpr int KMAX = kMidMaxK;
 };
 constexpr int kMwThreads = 384;  // threads of the tile kernels
 template <int SID>
@@ -93,9 +96,10 @@ struct MidWarpLayout {
     static constexpr size_t o_k1 = o_k0 + mid_a16((FM + 1) * 4);
     static constexpr size_t o_plist = o_k1 + mid_a16((FM + 1) * 4);  // list of each product
     static constexpr size_t o_loff = o_plist + mid_a16(FM);           // list product offsets
-    static constexpr size_t o_lbs = o_loff + mid_a16((kMidMaxK + 2) * 2);
-    static constexpr size_t o_lleaf = o_lbs + (kMidMaxK + 1) * 4;
-    static constexpr size_t o_gs = o_lleaf + mid_a16(kMidMaxK + 1);    // group scan scratch
+    static constexpr int KM = MwShape<SID>::KMAX;
+    static constexpr size_t o_lbs = o_loff + mid_a16((KM + 2) * 2);
+    static constexpr size_t o_lleaf = o_lbs + (KM + 1) * 4;
+    static constexpr size_t o_gs = o_lleaf + mid_a16(KM + 1);  // group scan scratch
     static constexpr size_t per_group = mid_a16(o_gs + 4 * (G + 1));
     static constexpr size_t bytes = per_group * MwShape<SID>::GROUPS;
 };
@@ -397,7 +401,8 @@ __global__ void __launch_bounds__(mw_threads<SID>(), 2) k_mid_warp(CsrDev A, Csr
             nl += tot >> 16;
             F += tot & 0xffff;
         }
-        if (F > S::F || cr.y - cmin >= (1 << S::RANGE)) {  // the analysis bins prevent this
+        // the analysis bins prevent this
+        if (F > S::F || k > S::KMAX || cr.y - cmin >= (1 << S::RANGE)) {
             if (t == 0)
                 atomicOr(&P.cnt->err, kErrWindowOverflow);
             grp_sync<G>(gid);
@@ -507,9 +512,9 @@ __global__ void __launch_bounds__(mw_threads<SID>(), 2) k_mid_warp(CsrDev A, Csr
                                                  aval + a0, bval, cmin, ccol + base, cval + base,
                                                  P.cnt, B.nnz);
         else
-            mw_reduce_balanced<T, NT, IDX, 9, 4>(src, dst, len, F, t, plist, lleaf, lbs, loff,
-                                                 aval + a0, bval, cmin, ccol + base, cval + base,
-                                                 P.cnt, B.nnz);
+            mw_reduce_balanced<T, NT, IDX, (S::KMAX <= 64 ? 7 : 9), 4>(
+                src, dst, len, F, t, plist, lleaf, lbs, loff, aval + a0, bval, cmin, ccol + base,
+                cval + base, P.cnt, B.nnz);
         grp_sync<G>(gid);
     }
 }

@@ -34,11 +34,15 @@ constexpr int kMidMaxK = 255;
 constexpr int kMidMaxRows = kMidCap / (kWarpMaxFlop + 1) + 2;
 
 // Warp mid rows: more than kWarpMaxFlop and at most kMwF products, at most
-// kMidMaxK A entries, columns within a range below 2^kMwRangeBits; one warp
-// each.  Group rows: up to kMgF products, range below 2^kMgRangeBits, four
-// warps each.  Both take precedence over the batched mid rows and over the
-// segmented heavy rows.
+// kMwMaxK A entries, columns within a range below 2^kMwRangeBits; one warp
+// each.  Group rows: up to kMgF products and kMwMaxK A entries, range below
+// 2^kMgRangeBits, four warps each; longer group rows (up to kMg2F products,
+// kMidMaxK A entries) in their own class.  All take precedence over the
+// batched mid rows and over the segmented heavy rows.  Holding the first two
+// classes to 64 lists keeps their merge-tree stacks at seven levels and
+// their kernels within 80 registers without spills.
 constexpr int kMwF = 768;
+constexpr int kMwMaxK = 64;
 constexpr int kMwRangeBits = 22;
 constexpr int kMtF = 64;          // tile rows: at most 64 products, half a warp each
 constexpr int kMt2F = 128;        // second tile class: at most 128 products

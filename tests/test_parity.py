@@ -460,13 +460,23 @@ def test_mid_rows_wide_column_range(ctx, oracle_mod):
     assert_same_csr(gpu_upper(ctx, A, B), R, "wide upper")
 
 
-def test_mid_rows_list_counts(ctx, oracle_mod):
-    """Warp rows with 31, 32, 33 and 255 lists (register stack of 6 or 9
-    levels), many repeated columns so that long runs are reduced."""
+@pytest.mark.parametrize("blen,ks", [
+    # warp rows (at most 768 products) with 31, 32, 33 lists (register stack
+    # of 6 or 7 levels) and 63, 64 lists; 65, 100 and 255 lists go to the
+    # longer four-warp rows (stack of 9 levels)
+    ((4, 8), (31, 32, 33, 63, 64, 65, 100, 255)),
+    # four-warp rows (769 .. 3072 products) with 64 lists, and with 65 and 200
+    # lists (longer four-warp rows)
+    ((14, 20), (64, 65, 200)),
+])
+def test_mid_rows_list_counts(ctx, oracle_mod, blen, ks):
+    """Mid rows around the list limits of the warp and four-warp classes, many
+    repeated columns so that long runs are reduced."""
     rng = np.random.default_rng(43)
-    K, N = 400, 60
-    Brows = [sorted(rng.choice(N, int(rng.integers(1, 4)), replace=False)) for _ in range(K)]
-    Arows = [sorted(rng.choice(K, k, replace=False)) for k in (31, 32, 33, 100, 255)]
+    K, N = 400, 60 * blen[1]
+    Brows = [sorted(rng.choice(N, int(rng.integers(blen[0], blen[1] + 1)), replace=False))
+             for _ in range(K)]
+    Arows = [sorted(rng.choice(K, k, replace=False)) for k in ks]
     A, B = _csr(Arows, K, 3), _csr(Brows, N, 4)
     R = oracle_mod.precise(A, B)
     assert_same_csr(gpu_precise(ctx, A, B), R, "list counts")
