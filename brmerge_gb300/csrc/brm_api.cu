@@ -379,6 +379,7 @@ int plan_phase(brm_context ctx, const brm_csr *A, const brm_csr *B, int *crpt, b
     ctx->plan.r_lo = 0;
     ctx->plan.r_hi = A->M;
     ctx->plan.seg_range = nullptr;
+    ctx->plan.live = brm::kLiveAll;
     brm::PlanDev P = ctx->plan;
     cudaStream_t s = ctx->stream;
     ev_record(ctx, timed, kEvStart);
@@ -397,6 +398,23 @@ int plan_phase(brm_context ctx, const brm_csr *A, const brm_csr *B, int *crpt, b
                                cudaMemcpyDeviceToHost, s));
     }
     BRM_CK(cudaStreamSynchronize(s));
+    {
+        // row classes with rows (the analysis has binned every row): the
+        // kernels of the others are not launched
+        const brm::Counters &hc = *ctx->h_cnt;
+        unsigned live = 0;
+        for (int b = 0; b < brm::kNumBins; b++)
+            if (hc.bin_count[b] > 0)
+                live |= brm::live_bit(b);
+        // batched mid rows are counted in batches, the longest heavy rows apart
+        if (hc.n_batch > 0)
+            live |= brm::live_bit(brm::kBinBatch);
+        if (hc.n_huge > 0)
+            live |= brm::live_bit(brm::kBinHeavy);
+        if (live & brm::live_bit(brm::kBinHeavy))
+            live |= brm::kLiveSegs;  // until the planning says no row was segmented
+        P.live = ctx->plan.live = live;
+    }
     if (fused) {
         // batched mid rows at mid_pre[row], warp mid rows after them
         const long long tot = ctx->h_mid[0] + ctx->h_mid[1];
@@ -455,6 +473,8 @@ int plan_phase(brm_context ctx, const brm_csr *A, const brm_csr *B, int *crpt, b
     BRM_CK(cudaStreamSynchronize(s));
     ctx->last_err = ctx->h_cnt->err;
     BRM_TRY(device_err_status(ctx->h_cnt->err));
+    if (ctx->h_cnt->n_seg == 0)
+        ctx->plan.live &= ~brm::kLiveSegs;
     ctx->planned = true;
     ctx->a_rpt = A->rpt;
     ctx->a_col = A->col;
@@ -964,6 +984,7 @@ int brm::precise_pipe(brm_context ctx, brm_dtype dtype, const brm_csr *A, const 
     ctx->plan.r_lo = 0;
     ctx->plan.r_hi = A->M;
     ctx->plan.seg_range = nullptr;
+    ctx->plan.live = brm::kLiveAll;  // the counts are on the device only
     ctx->planned = false;
     const brm::PlanDev P = ctx->plan;
     cudaStream_t s = ctx->stream;
@@ -1041,6 +1062,7 @@ int brm_create(brm_context *out)
     ctx->device = dev;
     ctx->plan.seg_cut = brm::kSegCut;
     ctx->plan.mid_limit = brm::kMidFlop;
+    ctx->plan.live = brm::kLiveAll;
     cudaError_t e = cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, dev);
     if (e == cudaSuccess)
         e = cudaMallocHost(&ctx->h_cnt, sizeof(brm::Counters));

@@ -778,20 +778,25 @@ inline void launch_mid_tile(const CsrDev &A, const CsrDev &B, const PlanDev &P, 
 
 // The warp rows, the four-warp group rows and the tile rows of one mode.
 // which: kMidGroups (the four-warp groups), kMidWarps (warp and tile rows) or
-// both.
+// both; classes without rows are not launched.
 template <typename T, int MODE>
 inline void launch_mid_warp(const CsrDev &A, const CsrDev &B, const PlanDev &P, const int *crpt,
                             int *ccol, T *cval, int num_sms, cudaStream_t s,
                             int which = kMidGroups | kMidWarps)
 {
     if (which & kMidGroups) {
-        launch_mid_group<T, MODE, 5>(A, B, P, crpt, ccol, cval, num_sms, s);
-        launch_mid_group<T, MODE, 4>(A, B, P, crpt, ccol, cval, num_sms, s);
+        if (plan_live(P, live_bit(kBinMidGroup2)))
+            launch_mid_group<T, MODE, 5>(A, B, P, crpt, ccol, cval, num_sms, s);
+        if (plan_live(P, live_bit(kBinMidGroup)))
+            launch_mid_group<T, MODE, 4>(A, B, P, crpt, ccol, cval, num_sms, s);
     }
     if (which & kMidWarps) {
-        launch_mid_group<T, MODE, 1>(A, B, P, crpt, ccol, cval, num_sms, s);
-        launch_mid_tile<T, MODE, 8>(A, B, P, crpt, ccol, cval, num_sms, s);
-        launch_mid_tile<T, MODE, 4>(A, B, P, crpt, ccol, cval, num_sms, s);
+        if (plan_live(P, live_bit(kBinMidWarp)))
+            launch_mid_group<T, MODE, 1>(A, B, P, crpt, ccol, cval, num_sms, s);
+        if (plan_live(P, live_bit(kBinMidTile2)))
+            launch_mid_tile<T, MODE, 8>(A, B, P, crpt, ccol, cval, num_sms, s);
+        if (plan_live(P, live_bit(kBinMidTile)))
+            launch_mid_tile<T, MODE, 4>(A, B, P, crpt, ccol, cval, num_sms, s);
     }
 }
 

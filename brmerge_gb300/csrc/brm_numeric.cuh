@@ -25,53 +25,67 @@ void numeric_phase(const CsrDev &A, const CsrDev &B, const PlanDev &P, const int
         cudaStreamWaitEvent(fk.aux, fk.fork, 0);
         s = fk.aux;
     }
-    k_copy_numeric<T, UPPER><<<num_sms * 8, 256, 0, s>>>(A, B, P, crpt, ccol, cval);
-    count_launch();
-    k_warp_numeric<T, UPPER><<<num_sms * 8, 256, 0, s>>>(A, B, P, crpt, ccol, cval);
-    count_launch();
+    // (kernels of row classes without rows are not launched)
+    if (plan_live(P, live_bit(kBinCopy))) {
+        k_copy_numeric<T, UPPER><<<num_sms * 8, 256, 0, s>>>(A, B, P, crpt, ccol, cval);
+        count_launch();
+    }
+    if (plan_live(P, live_bit(kBinWarp))) {
+        k_warp_numeric<T, UPPER><<<num_sms * 8, 256, 0, s>>>(A, B, P, crpt, ccol, cval);
+        count_launch();
+    }
     if (mid_col) {
         // mid rows were computed with the plan (one-call Precise): move them
-        k_mid_compact<T><<<num_sms * 8, 256, 0, s>>>(P, A.M, mid_col, (const T *)mid_val,
-                                                          crpt, ccol, cval);
-        count_launch();
+        if (plan_live(P, kLiveMidRows)) {
+            k_mid_compact<T><<<num_sms * 8, 256, 0, s>>>(P, A.M, mid_col, (const T *)mid_val,
+                                                              crpt, ccol, cval);
+            count_launch();
+        }
     } else {
         launch_mid_warp<T, UPPER ? kMwUpper : kMwPrecise>(A, B, P, crpt, ccol, cval, num_sms,
                                                           s);
-        const size_t msm = MidNumLayout<T>::bytes;
-        cudaFuncSetAttribute(k_mid_numeric<T, UPPER>,
-                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)msm);
-        k_mid_numeric<T, UPPER><<<num_sms * 2, kMidThreads, msm, s>>>(A, B, P, crpt, ccol,
-                                                                            cval);
-        count_launch();
+        if (plan_live(P, live_bit(kBinBatch))) {
+            const size_t msm = MidNumLayout<T>::bytes;
+            cudaFuncSetAttribute(k_mid_numeric<T, UPPER>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)msm);
+            k_mid_numeric<T, UPPER><<<num_sms * 2, kMidThreads, msm, s>>>(A, B, P, crpt, ccol,
+                                                                                cval);
+            count_launch();
+        }
     }
     if (fk.aux)
         cudaEventRecord(fk.join, fk.aux);
     s = s0;
-    k_split<0><<<num_sms * 8, 256, 0, s>>>(A, B, P);
-    count_launch();
-    const size_t ssm = SegLayout<T>::bytes;
-    cudaFuncSetAttribute(k_seg_numeric<T, UPPER>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)ssm);
-    // as many segment CTAs as fit on every SM (shared memory and registers)
-    static int seg_per_sm = 0;
-    if (seg_per_sm <= 0) {
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&seg_per_sm, k_seg_numeric<T, UPPER>,
-                                                          kSegThreads, ssm) != cudaSuccess ||
-            seg_per_sm <= 0)
-            seg_per_sm = 1;
+    if (plan_live(P, kLiveSegs)) {
+        k_split<0><<<num_sms * 8, 256, 0, s>>>(A, B, P);
+        count_launch();
+        const size_t ssm = SegLayout<T>::bytes;
+        cudaFuncSetAttribute(k_seg_numeric<T, UPPER>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ssm);
+        // as many segment CTAs as fit on every SM (shared memory and registers)
+        static int seg_per_sm = 0;
+        if (seg_per_sm <= 0) {
+            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&seg_per_sm,
+                                                              k_seg_numeric<T, UPPER>,
+                                                              kSegThreads, ssm) != cudaSuccess ||
+                seg_per_sm <= 0)
+                seg_per_sm = 1;
+        }
+        k_seg_numeric<T, UPPER><<<num_sms * seg_per_sm, kSegThreads, ssm, s>>>(A, B, P, crpt,
+                                                                                ccol, cval);
+        count_launch();
+        k_long_reduce<T><<<num_sms * 4, 128, 0, s>>>(P, ccol, cval);
+        count_launch();
+        k_long_warp<T><<<num_sms * 4, 128, 0, s>>>(P, ccol, cval);
+        count_launch();
     }
-    k_seg_numeric<T, UPPER><<<num_sms * seg_per_sm, kSegThreads, ssm, s>>>(A, B, P, crpt, ccol,
-                                                                            cval);
-    count_launch();
-    k_long_reduce<T><<<num_sms * 4, 128, 0, s>>>(P, ccol, cval);
-    count_launch();
-    k_long_warp<T><<<num_sms * 4, 128, 0, s>>>(P, ccol, cval);
-    count_launch();
-    const size_t smem = NumLayout<T>::bytes;
-    cudaFuncSetAttribute(k_rows_numeric<T, UPPER>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)smem);
-    k_rows_numeric<T, UPPER><<<num_sms, kRowThreads, smem, s>>>(A, B, P, crpt, ccol, cval);
-    count_launch();
+    if (plan_live(P, live_bit(kBinMid))) {
+        const size_t smem = NumLayout<T>::bytes;
+        cudaFuncSetAttribute(k_rows_numeric<T, UPPER>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        k_rows_numeric<T, UPPER><<<num_sms, kRowThreads, smem, s>>>(A, B, P, crpt, ccol, cval);
+        count_launch();
+    }
     if (spill_bytes) {
         k_spill_numeric<T, UPPER><<<num_sms * 4, 32, 0, s>>>(
             A, B, P, crpt, ccol, cval, (unsigned char *)spill_scratch, spill_bytes);
@@ -103,7 +117,7 @@ void launch_mid_scratch_t(const CsrDev &A, const CsrDev &B, const PlanDev &P, in
 {
     if (A.M <= 0)
         return;
-    if (which & kMidGroups) {
+    if ((which & kMidGroups) && plan_live(P, live_bit(kBinBatch))) {
         const size_t msm = MidNumLayout<T>::bytes;
         cudaFuncSetAttribute(k_mid_numeric<T, false, true>,
                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)msm);

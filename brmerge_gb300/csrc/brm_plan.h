@@ -248,7 +248,22 @@ struct PlanDev {
     long long c_cap;
     long long mid_cap;
     Counters *cnt;
+    // host side only: the launches the plan needs (kLive* bits); all ones
+    // when the host does not know the class counts (a captured pipeline)
+    unsigned live;
 };
+
+// Launch mask of a plan (PlanDev::live): bit b set when row class b (RowBin)
+// has rows, kLiveSegs when heavy rows were cut into segments.  The launchers
+// skip the kernels of empty classes, which for small products are most of
+// the launches of a call.
+constexpr unsigned kLiveSegs = 1u << 30;
+constexpr unsigned kLiveAll = 0xffffffffu;
+constexpr unsigned live_bit(int bin) { return 1u << bin; }
+constexpr unsigned kLiveMidRows = live_bit(kBinBatch) | live_bit(kBinMidWarp) |
+                                  live_bit(kBinMidGroup) | live_bit(kBinMidTile) |
+                                  live_bit(kBinMidTile2) | live_bit(kBinMidGroup2);
+inline bool plan_live(const PlanDev &P, unsigned bits) { return (P.live & bits) != 0; }
 
 // Capacities of a captured batch pipeline: every buffer sized by a count the
 // planning computes on the device is grown to these once, and admission

@@ -23,22 +23,31 @@ void launch_symbolic(const CsrDev &A, const CsrDev &B, const PlanDev &P, int num
     if (A.M <= 0)
         return;
     if (!only_heavy) {
-        k_warp_symbolic<0><<<num_sms * 8, 256, 0, s>>>(A, B, P);
-        count_launch();
-        if (!skip_mid) {
-            const size_t msm = MidSymLayout::bytes;
-            cudaFuncSetAttribute(k_mid_symbolic<0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)msm);
-            k_mid_symbolic<0><<<num_sms * 2, kMidThreads, msm, s>>>(A, B, P);
+        if (plan_live(P, live_bit(kBinWarp))) {
+            k_warp_symbolic<0><<<num_sms * 8, 256, 0, s>>>(A, B, P);
             count_launch();
+        }
+        if (!skip_mid) {
+            if (plan_live(P, live_bit(kBinBatch))) {
+                const size_t msm = MidSymLayout::bytes;
+                cudaFuncSetAttribute(k_mid_symbolic<0>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)msm);
+                k_mid_symbolic<0><<<num_sms * 2, kMidThreads, msm, s>>>(A, B, P);
+                count_launch();
+            }
             launch_mid_warp<double, kMwSymbolic>(A, B, P, nullptr, nullptr, nullptr, num_sms, s);
         }
     }
     // heavy rows: exact nnz and segment plan (both Precise and Upper)
-    const size_t psm = PlanLayout::bytes;
-    cudaFuncSetAttribute(k_heavy_plan<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)psm);
-    k_heavy_plan<0><<<num_sms * 3, kPlanThreads, psm, s>>>(A, B, P);
-    count_launch();
+    if (plan_live(P, live_bit(kBinHeavy))) {
+        const size_t psm = PlanLayout::bytes;
+        cudaFuncSetAttribute(k_heavy_plan<0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)psm);
+        k_heavy_plan<0><<<num_sms * 3, kPlanThreads, psm, s>>>(A, B, P);
+        count_launch();
+    }
+    if (!plan_live(P, live_bit(kBinMid)))
+        return;
     const size_t smem = SymLayout::bytes;
     if (only_heavy) {
         cudaFuncSetAttribute(k_rows_symbolic<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,

@@ -511,3 +511,24 @@ def test_heavy_segments_list_counts(ctx, oracle_mod):
     assert_same_csr(gpu_upper(ctx, A, B), R, "segment lists upper")
     C32 = gpu_precise(ctx, A.astype(np.float32), B.astype(np.float32))
     assert_same_csr(C32, oracle_mod.precise(A.astype(np.float32), B.astype(np.float32)), "f32")
+
+
+def test_empty_row_classes_are_not_launched(ctx, oracle_mod):
+    """Kernels of row classes without rows are skipped: a product whose rows
+    all have at most 64 products (one tile class) launches far fewer kernels
+    than one with rows of every class, and both stay bit-exact."""
+    from brmerge_gb300 import _native
+    L = _native.lib()
+    small = brm.gen_er(4096, 8, seed=5)
+    mixed = brm.gen_rmat(13, 8 << 13, seed=6)
+    counts = {}
+    for name, A in (("small", small), ("mixed", mixed)):
+        dA = brm.DeviceCSR.from_host(A)
+        R = oracle_mod.precise(A, A)
+        assert_same_csr(ctx.precise_device(dA, dA).to_host(), R, name)  # warm-up
+        l0 = L.brm_kernel_launches()
+        C = ctx.precise_device(dA, dA)
+        counts[name] = L.brm_kernel_launches() - l0
+        assert_same_csr(C.to_host(), R, name)
+        assert_same_csr(ctx.upper(dA, dA).to_host(), R, name + " upper")
+    assert counts["small"] + 8 <= counts["mixed"], counts
