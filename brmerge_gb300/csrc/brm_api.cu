@@ -1180,7 +1180,7 @@ int brm_set_tuning(brm_context ctx, const brm_tuning *t)
     const int cut = t ? t->seg_cut : brm::kSegCut;
     const int mid = t ? t->mid_flop : brm::kMidFlop;
     const long long ls = (t && t->long_scratch) ? t->long_scratch : kLongElems;
-    if (cut < brm::kMinSegCut || cut > brm::kSegCut || mid < brm::kMinMidFlop ||
+    if (cut < brm::kMinSegCut || cut > brm::kSegMaxCut || mid < brm::kMinMidFlop ||
         mid > brm::kMidFlop || ls < 1 || ls > (1ll << 31))
         return BRM_ERR_INVALID_VALUE;
     ctx->plan.seg_cut = cut;

@@ -69,7 +69,15 @@ constexpr int kMidWarps = 2;      // the warp and tile rows
 #endif
 constexpr int kSegThreads = BRM_SEG_THREADS;
 constexpr int kSegCap = BRM_SEG_CAP;
-constexpr int kSegCut = kSegCap / 2;      // target products between cuts
+// Target products between cuts (a runtime knob, brm_tuning.seg_cut): the
+// default and the largest accepted.  Segments average about the target, so a
+// larger one means fewer segments (less fixed work per product in the
+// segment kernel, a smaller split table) but more dense planning groups
+// (above kSegCap - target products), whose columns are counted one by one.
+// R-MAT n=2^18 C = A*A one-call Precise: 1536 -> 3.10 ms, 2048 -> 3.02,
+// 2304 -> 2.94, 2560 -> 3.11, 2688 -> 3.11 (same output).
+constexpr int kSegCut = kSegCap * 3 / 4;
+constexpr int kSegMaxCut = kSegCap * 7 / 8;
 constexpr int kSegMaxK = 65535;           // leaf index stored in 16 bits
 constexpr int kHugeFlop = 16 * kSegCap;   // heavy rows planned first (longest first)
 constexpr int kMaxParts = 16;             // row parts of a numeric phase run part by part
@@ -143,20 +151,22 @@ struct Counters {
 };
 
 // Descriptor slots reserved for a heavy row with F products and the cut
-// target `cut` (<= kSegCut): the cut rule makes at most F / cut cuts at
-// product thresholds (plus one per chunk), 2 per dense group (a group with
-// more than kSegCap - cut >= cut products; at most F / cut of them) and at
-// most 2 h / cut + 1 inside a dense group of h products, plus one chunk start
-// per kPlanBits columns.
+// target `cut`: the cut rule makes at most F / cut cuts at product
+// thresholds (plus one per chunk), 2 per dense group (a group with more than
+// dense = kSegCap - cut products; at most F / dense of them) and at most
+// 2 h / cut + 1 inside a dense group of h products, plus one chunk start per
+// kPlanBits columns: at most 3 F / cut + 3 F / dense <= 6 F / min(cut, dense)
+// and the chunk terms.
 __host__ __device__ inline unsigned long long seg_bound(long long F, int N, int cut)
 {
-    return 6ull * (unsigned long long)((F + cut - 1) / cut) +
+    const int m = cut < kSegCap - cut ? cut : kSegCap - cut;
+    return 6ull * (unsigned long long)((F + m - 1) / m) +
            2ull * ((unsigned)N / (unsigned)kPlanBits) + 8ull;
 }
 
 // Runtime policy knobs of the row classes (chosen by brm_autotune or
 // brm_set_tuning; every capacity stays compile-time): the heavy-row cut
-// target seg_cut in [kMinSegCut, kSegCut] (segments hold at most kSegCap
+// target seg_cut in [kMinSegCut, kSegMaxCut] (segments hold at most kSegCap
 // products whatever the target) and the mid-row weight limit mid_flop in
 // [kMinMidFlop, kMidFlop] (batches hold at most 2 * mid_flop <= kMidCap).
 // The results do not depend on them: only where rows and segments are cut.

@@ -138,7 +138,7 @@ __device__ __forceinline__ void plan_products(const PlanDev &P, const int *__res
 // order and calls f(column_in_group, product_prefix, distinct_prefix) for
 // each.  `run` packs (products << 32 | distinct columns) before group g and
 // ph is the product count of group g-1.  A dense group (more than
-// dense = kSegCap - cut >= cut products) is always cut before and after;
+// dense = kSegCap - cut products) is always cut before and after;
 // inside it, a new segment starts at a column when the running product count
 // would exceed `cut` (a single column above `cut` is a segment of its own).
 // Any other group starts a segment when the group before it crossed a
@@ -202,8 +202,8 @@ __global__ void __launch_bounds__(kPlanThreads) k_heavy_plan(CsrDev A, CsrDev B,
     const int nrows = P.cnt->bin_count[kBinHeavy] + nhuge;
     const int *rows = P.rows + (size_t)kBinHeavy * M;
     const int *__restrict__ bcol = B.col;
-    const unsigned cut = (unsigned)P.seg_cut;                // <= kSegCut
-    const unsigned dense = (unsigned)(kSegCap - P.seg_cut);  // >= cut
+    const unsigned cut = (unsigned)P.seg_cut;                // <= kSegMaxCut
+    const unsigned dense = (unsigned)(kSegCap - P.seg_cut);  // >= kSegCap / 4
     for (int i = tid; i < kPlanWords; i += NT)
         bm[i] = 0;
     for (int i = tid; i < kPlanGroups; i += NT)

@@ -121,7 +121,7 @@ int brm_set_validate(brm_context ctx, int on);
 /* Row-class policy of a context.  The reference balances rows over threads
  * by flop (spgemm.h:496-503); here rows are binned and heavy rows cut into
  * segments, and two thresholds of that are runtime knobs: seg_cut, the
- * products between cuts of a heavy row (256 .. 1536; segments hold at most
+ * products between cuts of a heavy row (256 .. 2688; segments hold at most
  * 3072 products), and mid_flop, the largest row weight of the batched
  * mid-row kernels (128 .. 2048; batches hold at most 4096).  Results do not
  * depend on them, only speed does. */
@@ -135,14 +135,14 @@ typedef struct brm_tuning {
     long long long_scratch;
 } brm_tuning;
 
-/* NULL restores the defaults (1536, 2048, 0); out-of-range values are
+/* NULL restores the defaults (2304, 2048, 0); out-of-range values are
  * BRM_ERR_INVALID_VALUE. */
 int brm_set_tuning(brm_context ctx, const brm_tuning *t);
 int brm_get_tuning(brm_context ctx, brm_tuning *t);
 
 /* Times the one-call Precise form on the caller's own input (n == 1:
  * brm_precise_device on A[0], B[0]; n > 1: brm_batch_precise on the n pairs)
- * under each candidate setting (seg_cut in {1536, 1024, 768, 512} x mid_flop
+ * under each candidate setting (seg_cut in {2304, 1536, 1152, 768} x mid_flop
  * in {2048, 1024, 512}, best of two runs each after one warm-up), keeps the
  * fastest in the context and returns it in *best (may be NULL).  No
  * counterpart in the reference. */

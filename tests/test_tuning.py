@@ -14,8 +14,13 @@ from conftest import assert_same_csr
 pytestmark = pytest.mark.gpu
 
 
+# the largest heavy-row cut target accepted: seven eighths of the 3072
+# products a segment holds
+MAX_CUT = 2688
+
+
 def _defaults():
-    """The context defaults: the largest cut target and mid-row weight."""
+    """The context defaults: cut target and the largest mid-row weight."""
     c = brm.Context()
     t = c.tuning()
     c.close()
@@ -24,8 +29,8 @@ def _defaults():
 
 def _settings():
     cut, mid = _defaults()
-    return [(cut, mid), (cut * 2 // 3, mid // 2), (cut // 2, mid // 4), (cut // 3, mid),
-            (256, 128)]
+    return [(cut, mid), (MAX_CUT, mid // 2), (cut * 2 // 3, mid // 2), (cut // 2, mid // 4),
+            (cut // 3, mid), (256, 128)]
 
 
 @pytest.fixture(scope="module")
@@ -58,7 +63,7 @@ def test_every_setting_gives_the_same_result(ctx, oracle_mod, name, A, B):
 
 def test_out_of_range_rejected(ctx):
     cut, mid = _defaults()
-    for c, m in [(100, mid), (cut + 1, mid), (cut, 2 * mid), (cut, 64)]:
+    for c, m in [(100, mid), (MAX_CUT + 1, mid), (cut, 2 * mid), (cut, 64)]:
         with pytest.raises(brm.BrmError):
             ctx.set_tuning(seg_cut=c, mid_flop=m)
     assert ctx.tuning() == {"seg_cut": cut, "mid_flop": mid, "long_scratch": 0}
