@@ -45,6 +45,7 @@ template <int SID>
 struct MwShape;
 template <>
 struct MwShape<1> {
+    static constexpr int W = 0;  // index of the shape's work counter
     static constexpr int G = 1;
     static constexpr int F = kMwF;
     static constexpr int IDX = 10;
@@ -55,6 +56,7 @@ struct MwShape<1> {
 };
 template <>
 struct MwShape<4> {
+    static constexpr int W = 1;
     static constexpr int G = 4;
     static constexpr int F = kMgF;
     static constexpr int IDX = 12;
@@ -65,6 +67,7 @@ struct MwShape<4> {
 };
 template <>
 struct MwShape<5> {
+    static constexpr int W = 2;
     static constexpr int G = 4;
     static constexpr int F = kMg2F;
     static constexpr int IDX = 13;
@@ -99,7 +102,7 @@ struct MidWarpLayout {
     static constexpr int KM = MwShape<SID>::KMAX;
     static constexpr size_t o_lbs = o_loff + mid_a16((KM + 2) * 2);
     static constexpr size_t o_lleaf = o_lbs + (KM + 1) * 4;
-    static constexpr size_t o_gs = o_lleaf + mid_a16(KM + 1);  // group scan scratch
+    static constexpr size_t o_gs = o_lleaf + mid_a16(KM + 1);  // group scan scratch, next row
     static constexpr size_t per_group = mid_a16(o_gs + 4 * (G + 1));
     static constexpr size_t bytes = per_group * MwShape<SID>::GROUPS;
 };
@@ -374,9 +377,18 @@ __global__ void __launch_bounds__(mw_threads<SID>(), 2) k_mid_warp(CsrDev A, Csr
     const int *__restrict__ bcol = B.col;
     const T *__restrict__ bval = (const T *)B.val;
     const T *__restrict__ aval = (const T *)A.val;
-    const int g0 = blockIdx.x * S::GROUPS + gid;
-    const int ng = gridDim.x * S::GROUPS;
-    for (int it = g0; it < n; it += ng) {
+    // rows are taken one at a time from a counter (the classes span a
+    // fourfold range of products, so a fixed share per group leaves a long
+    // tail); gs[G] passes the item to the group
+    int *work = &P.cnt->work_mw[S::W];
+    for (;;) {
+        if (t == 0)
+            gs[G] = atomicAdd(work, 1);
+        grp_sync<G>(gid);
+        const int it = gs[G];
+        grp_sync<G>(gid);  // every thread has the item before gs[G] is reused
+        if (it >= n)
+            break;
         const int row = rows[it];
         if (row < P.r_lo || row >= P.r_hi)
             continue;
@@ -516,6 +528,15 @@ __global__ void __launch_bounds__(mw_threads<SID>(), 2) k_mid_warp(CsrDev A, Csr
                 src, dst, len, F, t, plist, lleaf, lbs, loff, aval + a0, bval, cmin, ccol + base,
                 cval + base, P.cnt, B.nnz);
         grp_sync<G>(gid);
+    }
+    // the last group of the launch clears the counters for the next launch
+    // (its own taken items and every other group's are ordered before)
+    if (t == 0) {
+        __threadfence();
+        if (atomicAdd(&P.cnt->done_mw[S::W], 1) == (int)gridDim.x * S::GROUPS - 1) {
+            atomicExch(work, 0);
+            atomicExch(&P.cnt->done_mw[S::W], 0);
+        }
     }
 }
 

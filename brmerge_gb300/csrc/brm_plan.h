@@ -148,6 +148,12 @@ struct Counters {
     int chk_line;
     long long chk_idx;
     long long chk_bound;
+    // dynamic row counters of the warp / four-warp mid-row kernels (one per
+    // shape) and the groups of a launch that have finished; the last group
+    // of a launch sets both back to zero, so every launch starts from zero
+    // whatever phase or pipeline runs it
+    int work_mw[3];
+    int done_mw[3];
 };
 
 // Descriptor slots reserved for a heavy row with F products and the cut
