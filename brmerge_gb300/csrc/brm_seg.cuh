@@ -45,8 +45,9 @@ namespace brm {
 
 constexpr int kPlanThreads = 512;
 // Segment cuts are placed at planning-group boundaries (kPlanGroupBits
-// columns); a dense group (more than kSegCap - cut products) gets per-column counts
-// (at most kDenseGroups such groups per chunk).
+// columns); a dense group (more than kSegCap - cut products) is a segment of
+// its own, and one above kSegCap products gets per-column counts and is cut
+// inside (at most kDenseGroups such groups per chunk).
 constexpr int kPlanGroupLog2 = 7;
 constexpr int kPlanGroupBits = 1 << kPlanGroupLog2;      // 128 columns
 constexpr int kPlanGroupWords = kPlanGroupBits / 32;     // 4 bitmap words
@@ -138,12 +139,12 @@ __device__ __forceinline__ void plan_products(const PlanDev &P, const int *__res
 // order and calls f(column_in_group, product_prefix, distinct_prefix) for
 // each.  `run` packs (products << 32 | distinct columns) before group g and
 // ph is the product count of group g-1.  A dense group (more than
-// dense = kSegCap - cut products) is always cut before and after;
-// inside it, a new segment starts at a column when the running product count
-// would exceed `cut` (a single column above `cut` is a segment of its own).
-// Any other group starts a segment when the group before it crossed a
-// multiple of `cut`, so a segment holds less than cut + dense = kSegCap
-// products.
+// dense = kSegCap - cut products) is always cut before and after; it is one
+// segment when it holds at most kSegCap products, and inside a larger one a
+// new segment starts at a column when the running product count would exceed
+// `cut` (a single column above `cut` is a segment of its own).  Any other
+// group starts a segment when the group before it crossed a multiple of
+// `cut`, so a segment holds less than cut + dense = kSegCap products.
 template <typename Fn>
 __device__ __forceinline__ void plan_group_starts(int g, unsigned h, unsigned ph,
                                                   unsigned long long run,
@@ -152,6 +153,10 @@ __device__ __forceinline__ void plan_group_starts(int g, unsigned h, unsigned ph
 {
     const unsigned pe = (unsigned)(run >> 32);
     const unsigned ue = (unsigned)(run & 0xffffffffu);
+    if (h > dense && h <= (unsigned)kSegCap) {
+        f(0, pe, ue);
+        return;
+    }
     if (h > dense) {
         f(0, pe, ue);
         unsigned acc = 0, pp = pe, uu = ue;
@@ -188,7 +193,8 @@ __global__ void __launch_bounds__(kPlanThreads) k_heavy_plan(CsrDev A, CsrDev B,
     unsigned *hist = (unsigned *)(smem + PlanLayout::o_hist);
     unsigned short *gpop = (unsigned short *)(smem + PlanLayout::o_gpop);
     unsigned short *dix = (unsigned short *)(smem + PlanLayout::o_dix);
-    // per-column product counts of dense groups, two 16-bit counters a word
+    // per-column product counts of groups above kSegCap products, two 16-bit
+    // counters a word
     unsigned *ccnt2 = (unsigned *)(smem + PlanLayout::o_ccnt);
     const unsigned short *ccnt = (const unsigned short *)(smem + PlanLayout::o_ccnt);
     int *lst = (int *)(smem + PlanLayout::o_lst);
@@ -244,8 +250,8 @@ __global__ void __launch_bounds__(kPlanThreads) k_heavy_plan(CsrDev A, CsrDev B,
             const int ng = (span + kPlanGroupBits - 1) >> kPlanGroupLog2;
             // bm and hist are zero here: cleared at the start and after every chunk
             if (tid == 0) {
-                misc[4] = INT_MAX;  // first dense group
-                misc[5] = -1;       // last dense group
+                misc[4] = INT_MAX;  // first group cut per column
+                misc[5] = -1;       // last group cut per column
             }
             __syncthreads();
             // pass over the chunk's products: column bitmap and products per
@@ -285,7 +291,8 @@ __global__ void __launch_bounds__(kPlanThreads) k_heavy_plan(CsrDev A, CsrDev B,
             __syncthreads();
             const int gpt = (ng + NT - 1) / NT;
             const int g0 = min(tid * gpt, ng), g1 = min(g0 + gpt, ng);
-            // distinct columns per group; dense groups get per-column counts
+            // distinct columns per group; groups above kSegCap products get
+            // per-column counts
             int nd_local = 0, dlo = INT_MAX, dhi = -1;
             unsigned long long sp = 0;
             for (int g = g0; g < g1; g++) {
@@ -295,7 +302,7 @@ __global__ void __launch_bounds__(kPlanThreads) k_heavy_plan(CsrDev A, CsrDev B,
                 for (int q = 0; q < kPlanGroupWords; q++)
                     pc += __popc(bm[g * kPlanGroupWords + q]);
                 gpop[g] = (unsigned short)pc;
-                if (h > dense) {
+                if (h > (unsigned)kSegCap) {
                     nd_local++;
                     dlo = min(dlo, g);
                     dhi = g;
@@ -313,19 +320,19 @@ __global__ void __launch_bounds__(kPlanThreads) k_heavy_plan(CsrDev A, CsrDev B,
                 fail = true;  // uniform
             if (!fail && nd > 0) {
                 for (int g = g0; g < g1; g++)
-                    if (hist[g] > dense)
+                    if (hist[g] > (unsigned)kSegCap)
                         dix[g] = (unsigned short)dx++;
                 for (int i = tid; i < nd * kPlanGroupBits / 2; i += NT)
                     ccnt2[i] = 0;
                 __syncthreads();
-                // only the columns from the first to the last dense group
+                // only the columns from the first to the last such group
                 const int dlo_c = lo + kPlanGroupBits * misc[4];
                 const int dhi_c = (int)min((long long)chi,
                                            (long long)lo + (long long)kPlanGroupBits * (misc[5] + 1));
                 plan_products<NT>(P, bcol, a0, k, true, dlo_c, dhi_c, lo, lst, loffs, ws, [&](int rc) {
                     if ((unsigned)rc < (unsigned)span) {
                         const int g = rc >> kPlanGroupLog2;
-                        if (hist[g] > dense) {
+                        if (hist[g] > (unsigned)kSegCap) {
                             const int slot = dix[g] * kPlanGroupBits + (rc & (kPlanGroupBits - 1));
                             atomicAdd(&ccnt2[slot >> 1], 1u << (16 * (slot & 1)));
                         }
@@ -347,7 +354,7 @@ __global__ void __launch_bounds__(kPlanThreads) k_heavy_plan(CsrDev A, CsrDev B,
                 for (int g = g0; g < g1; g++) {
                     const unsigned h = hist[g];
                     plan_group_starts(g, h, ph, run,
-                                      h > dense ? ccnt + dix[g] * kPlanGroupBits : ccnt, cut,
+                                      h > (unsigned)kSegCap ? ccnt + dix[g] * kPlanGroupBits : ccnt, cut,
                                       dense, [&](int, unsigned, unsigned) { nstart++; });
                     run += ((unsigned long long)h << 32) | (unsigned)gpop[g];
                     ph = h;
@@ -378,7 +385,7 @@ __global__ void __launch_bounds__(kPlanThreads) k_heavy_plan(CsrDev A, CsrDev B,
                 for (int g = g0; g < g1; g++) {
                     const unsigned h = hist[g];
                     plan_group_starts(g, h, ph, run,
-                                      h > dense ? ccnt + dix[g] * kPlanGroupBits : ccnt, cut,
+                                      h > (unsigned)kSegCap ? ccnt + dix[g] * kPlanGroupBits : ccnt, cut,
                                       dense, [&](int c, unsigned pe, unsigned ue) {
                                           if (BRM_IN(P.cnt, base + nseg + r, P.cnt->seg_cap)) {
                                               SegDesc &d = P.seg[base + nseg + r];
