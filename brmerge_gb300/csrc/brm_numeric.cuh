@@ -37,10 +37,7 @@ void numeric_phase(const CsrDev &A, const CsrDev &B, const PlanDev &P, const int
     if (mid_col) {
         // mid rows were computed with the plan (one-call Precise): move them
         if (plan_live(P, kLiveMidRows)) {
-#ifndef BRM_COMPACT_CTAS
-#define BRM_COMPACT_CTAS 8
-#endif
-            k_mid_compact<T><<<num_sms * BRM_COMPACT_CTAS, 256, 0, s>>>(P, A.M, mid_col, (const T *)mid_val,
+            k_mid_compact<T><<<num_sms * 8, 256, 0, s>>>(P, A.M, mid_col, (const T *)mid_val,
                                                               crpt, ccol, cval);
             count_launch();
         }

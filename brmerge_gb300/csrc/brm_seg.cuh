@@ -557,13 +557,8 @@ struct SegLayout {
     static_assert(NW * kSegPWords * 6 <= kSegCap * 4, "cw region holds the warp bitmaps");
 };
 
-#ifdef BRM_SEG_MAXNREG
-#define BRM_SEG_BOUNDS __maxnreg__(BRM_SEG_MAXNREG)
-#else
-#define BRM_SEG_BOUNDS __launch_bounds__(kSegThreads, 512 / kSegThreads)
-#endif
 template <typename T, bool UPPER>
-__global__ void BRM_SEG_BOUNDS k_seg_numeric(CsrDev A, CsrDev B, PlanDev P,
+__global__ void __launch_bounds__(kSegThreads, 512 / kSegThreads) k_seg_numeric(CsrDev A, CsrDev B, PlanDev P,
                                                              const int *crpt, int *ccol, T *cval)
 {
     if (P.cnt->abort)  // a capacity check of a captured pipeline failed
