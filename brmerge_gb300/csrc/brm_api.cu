@@ -440,9 +440,12 @@ int plan_phase(brm_context ctx, const brm_csr *A, const brm_csr *B, int *crpt, b
     if (fused) {
         // the batched and four-warp group mid rows (values into the scratch)
         // on the second stream, beside the warp-row counts, the heavy-row
-        // planning and then the warp and tile mid rows
+        // planning and then the warp and tile mid rows; the planning is
+        // enqueued first, so its longest rows start before the mid rows
+        // take the SMs
         const brm::Fork &fk = ctx->fork;
         BRM_CK(cudaEventRecord(fk.fork, s));
+        brm::launch_symbolic(a, b, P, ctx->num_sms, upper, fused, s);
         BRM_CK(cudaStreamWaitEvent(fk.aux, fk.fork, 0));
         if (fused_dtype == BRM_F64)
             brm::launch_mid_scratch_f64(a, b, P, ctx->mid_col, ctx->mid_val, ctx->num_sms, fk.aux,
@@ -451,8 +454,9 @@ int plan_phase(brm_context ctx, const brm_csr *A, const brm_csr *B, int *crpt, b
             brm::launch_mid_scratch_f32(a, b, P, ctx->mid_col, ctx->mid_val, ctx->num_sms, fk.aux,
                                         brm::kMidGroups);
         BRM_CK(cudaEventRecord(fk.join, fk.aux));
+    } else {
+        brm::launch_symbolic(a, b, P, ctx->num_sms, upper, fused, s);
     }
-    brm::launch_symbolic(a, b, P, ctx->num_sms, upper, fused, s);
     if (fused) {
         if (fused_dtype == BRM_F64)
             brm::launch_mid_scratch_f64(a, b, P, ctx->mid_col, ctx->mid_val, ctx->num_sms, s,
@@ -992,8 +996,11 @@ int brm::precise_pipe(brm_context ctx, brm_dtype dtype, const brm_csr *A, const 
     brm::launch_analyze(a, b, P, s);
     brm::launch_batches(P, A->M, ctx->scan_tmp, s);
     brm::launch_pipe_admit(P, A->M, caps, 0, s);
+    // as in plan_phase: the heavy-row planning is enqueued before the mid
+    // rows of the second stream
     const brm::Fork &fk = ctx->fork;
     BRM_CK(cudaEventRecord(fk.fork, s));
+    brm::launch_symbolic(a, b, P, ctx->num_sms, false, true, s);
     BRM_CK(cudaStreamWaitEvent(fk.aux, fk.fork, 0));
     if (dtype == BRM_F64)
         brm::launch_mid_scratch_f64(a, b, P, ctx->mid_col, ctx->mid_val, ctx->num_sms, fk.aux,
@@ -1002,7 +1009,6 @@ int brm::precise_pipe(brm_context ctx, brm_dtype dtype, const brm_csr *A, const 
         brm::launch_mid_scratch_f32(a, b, P, ctx->mid_col, ctx->mid_val, ctx->num_sms, fk.aux,
                                     brm::kMidGroups);
     BRM_CK(cudaEventRecord(fk.join, fk.aux));
-    brm::launch_symbolic(a, b, P, ctx->num_sms, false, true, s);
     if (dtype == BRM_F64)
         brm::launch_mid_scratch_f64(a, b, P, ctx->mid_col, ctx->mid_val, ctx->num_sms, s,
                                     brm::kMidWarps);
