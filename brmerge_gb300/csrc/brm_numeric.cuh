@@ -40,8 +40,11 @@ void numeric_phase(const CsrDev &A, const CsrDev &B, const PlanDev &P, const int
     // latency-bound column reducers that follow it (R-MAT n=2^18 one-call
     // Precise 2.875 -> 2.838 ms; the two reducers on separate streams as
     // well: 2.917 ms)
+    // A numeric phase run in row parts (the host drop-in copies each part
+    // back while the next computes) keeps the compaction first: there the
+    // parts' completion order matters more than the overlap.
     const bool compact = mid_col && plan_live(P, kLiveMidRows);
-    const bool compact_late = compact && fk.aux && plan_live(P, kLiveSegs);
+    const bool compact_late = compact && fk.aux && plan_live(P, kLiveSegs) && !P.seg_range;
     if (mid_col) {
         if (compact && !compact_late) {
             k_mid_compact<T><<<num_sms * 8, 256, 0, s>>>(P, A.M, mid_col, (const T *)mid_val,
