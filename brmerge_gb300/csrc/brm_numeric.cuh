@@ -34,15 +34,13 @@ void numeric_phase(const CsrDev &A, const CsrDev &B, const PlanDev &P, const int
         k_warp_numeric<T, UPPER><<<num_sms * 8, 256, 0, s>>>(A, B, P, crpt, ccol, cval);
         count_launch();
     }
-    // the mid rows computed with the plan (one-call Precise) are moved into
-    // C by a bandwidth-bound copy; with heavy-row segments it waits for the
+    // The mid rows computed with the plan (one-call Precise) are moved into
+    // C by a bandwidth-bound copy.  With heavy-row segments it waits for the
     // segment kernel (which holds every SM's registers) and runs beside the
     // latency-bound column reducers that follow it (R-MAT n=2^18 one-call
     // Precise 2.875 -> 2.838 ms; the two reducers on separate streams as
-    // well: 2.917 ms)
-    // A numeric phase run in row parts (the host drop-in copies each part
-    // back while the next computes) keeps the compaction first: there the
-    // parts' completion order matters more than the overlap.
+    // well: 2.917 ms).  A numeric phase run in row parts (the host drop-in
+    // copies each part back while the next computes) keeps it first.
     const bool compact = mid_col && plan_live(P, kLiveMidRows);
     const bool compact_late = compact && fk.aux && plan_live(P, kLiveSegs) && !P.seg_range;
     if (mid_col) {
